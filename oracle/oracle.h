@@ -1,0 +1,95 @@
+/*
+ * CPU oracle for the Tahoe implicit hex8 solid path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain FP64 C++ restatement of the
+ * reference algorithms (shape functions, kinematics, materials, element
+ * residual/stiffness, equation numbering, MSR sparsity and assembly, Krylov
+ * and Newton solvers).  Only the tests, the smoke check and the CPU-baseline
+ * leg of the benchmark may load it; the product library never links it.
+ *
+ * Parity pin: the oracle is checked against the golden nodal outputs that the
+ * reference's own regression suite commits (benchmark_XML level.0/level.1
+ * `.run` files, extracted into tests/golden by tests/golden/make_golden.py).
+ *
+ * Conventions (identical to the reference):
+ *   - Voigt order [11,22,33,23,13,12]; strains carry tensor shear components,
+ *     the 6x6 moduli act on engineering shear (dSymMatrixT::A_ijkl_B_kl).
+ *   - hex8 node order and Gauss points: toolbox/src/geometry/HexahedronT.cpp:23-25,
+ *     1540-1548 (8 points at +-1/sqrt(3) in node order, weight 1).
+ *   - equation numbers 1-based, node-major / dof-minor, prescribed dofs -1
+ *     (tahoe/src/nodes/NodeManagerT.cpp:712-760, FieldT.h:48-50).
+ */
+#ifndef TAHOE_ORACLE_H
+#define TAHOE_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* formulations */
+enum { ORC_SMALL_STRAIN = 0, ORC_TOTAL_LAGRANGIAN = 1 };
+
+/* material kinds (parameter layout in oracle.cpp: orc_set_material) */
+enum {
+  ORC_MAT_SS_HOOKEAN = 0,  /* small_strain_StVenant / small_strain_Hookean: p = C(36) col-major */
+  ORC_MAT_SS_J2 = 1,       /* small_strain_StVenant_J2: p = {E, nu, a (slope), b (yield)} */
+  ORC_MAT_FS_SIMO = 2,     /* Simo_isotropic: p = {mu, kappa} */
+  ORC_MAT_FS_STVENANT = 3  /* large_strain_StVenant: p = {E, nu} */
+};
+
+/* J2 flags (J2SSC0HardeningT.h:32-34) plus a marker for unallocated cards */
+enum { ORC_J2_PLASTIC = 0, ORC_J2_ELASTIC = 1, ORC_J2_RESET = 3, ORC_J2_UNALLOCATED = 7 };
+
+void* orc_model_create(int nnd, const double* X, int nel, const int* conn);
+void orc_model_free(void* m);
+int orc_set_formulation(void* m, int form);
+int orc_set_material(void* m, int block, int kind, const double* p, int np);
+int orc_set_element_blocks(void* m, const int* block_of_element);
+int orc_set_schedule(void* m, int npts, const double* x, const double* y);
+int orc_add_kbc(void* m, int node, int dof, double value, int scheduled);
+int orc_add_force(void* m, int node, int dof, double value);
+int orc_add_traction(void* m, int elem, int facet, const double* t3);
+int orc_set_threads(void* m, int nthreads);
+
+/* equations: returns number of active equations; eqnos is nnd*3 */
+int orc_equations(void* m, int* eqnos);
+/* MSR structure (MSRBuilderT::GenerateMSR): bindx[0..n] row starts (offset n+1),
+ * then sorted 0-based off-diagonal columns.  Returns length; writes when
+ * bindx != NULL and cap is large enough. */
+long long orc_msr_pattern(void* m, int upper_only, int* bindx, long long cap);
+
+/* element level (uses the model's material/formulation and J2 state) */
+int orc_element(void* m, int e, const double* u_nodal, int iteration, double* Ke, double* fint);
+
+/* global residual (R = Fext - Fint on active eqs) at time t and, when
+ * val != NULL, the MSR (upper, symmetric) tangent values aligned with bindx. */
+int orc_form(void* m, const double* u_nodal, double t, int iteration, double* R, double* val);
+
+/* MSR symmetric product (MSRMatrixT::Multx). */
+int orc_msr_multx(void* m, const double* val, const double* x, double* y);
+
+/* Jacobi PCG on the assembled MSR matrix; returns iterations (<0 on failure). */
+int orc_pcg(void* m, const double* val, const double* b, double* x, double rel_tol, int max_it,
+            double* rel_res);
+
+/* Newton (NLSolver) over nsteps load steps with time step dt.
+ * solver: 0 dense Cholesky, 1 Jacobi PCG (lin_tol).  u_hist: nsteps*nnd*3
+ * nodal displacements after each converged step; its_hist: Newton iterations
+ * per step.  Returns 0 on success, step index+1 of the first failure otherwise. */
+int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its,
+            double div_tol, int solver, double lin_tol, double* u_hist, int* its_hist);
+
+/* J2 state after the last converged step (nel*8 each; alpha per IP). */
+int orc_j2_state(void* m, signed char* flags, double* alpha, double* eps_p);
+/* reactions (Fint at every dof, nnd*3) at the current displacement */
+int orc_nodal_internal_force(void* m, const double* u_nodal, int iteration, double* f);
+/* the displacement currently held by the model (nnd*3) */
+int orc_get_u(void* m, double* u);
+int orc_set_u(void* m, const double* u);
+/* J2 step bookkeeping (exposed for stepwise parity tests) */
+int orc_close_step(void* m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
