@@ -1,0 +1,343 @@
+"""Benchmark of the GB300 hex8 implicit path.
+
+Workload (configuration 2 of the benchmark set): total-Lagrangian compressible
+neo-Hookean block, 64^3 hex8 (274,625 nodes, 823,875 dofs), mu=1, kappa=10,
+interior nodes jittered +-0.2h (seed 0), bottom fixed, top compressed 1% in the
+first of 10 load steps.  Synthetic, seeded input (no dataset exists).
+
+A timed step is one Newton iteration of that load step: FP32 element tangent
++ deterministic block-CSR assembly + Jacobi PCG (FP32 vectors, FP64 dots) to
+the inner tolerance + update + FP64 element residual and norm.  Every step
+starts from the same device snapshot of the step-start state, so the K steps
+do identical work.  The metric is the Newton-step time (ms per iteration,
+lower is better).  Inputs stay resident in HBM; the block-CSR matrix (about
+290 MB) is larger than the 129 MB L2, so no flush is needed between steps.
+
+`e2e` repeats the step through the C ABI with host buffers: displacement
+uploaded from host memory, residual at the step start, the iteration, and the
+displacement read back, all inside the timed region.
+
+--impl reference times the reference algorithm on the host cores instead
+(the CPU oracle restatement: the reference's own build needs its CMake
+system), on a bounded sample of the same workload.
+
+Multi-GPU: independent replicas (the single-mesh path has a real halo
+exchange that is not built); --gpus N under torchrun runs N replicas.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LIN_TOL = 1e-4          # inner PCG relative tolerance (inexact Newton)
+NEWTON_TOL = 1e-8       # outer relative tolerance on the FP64 residual
+C2_PCG_ITERS_FP64 = None  # filled from the run when available
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for ln in f:
+                parts = [p.strip() for p in ln.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def setup_c2(device, precision):
+    from tahoe_gb300 import workloads
+    mesh, model, run = workloads.c2(add=None)
+    model.device = device
+    model.setup()
+    # load step 1: prescribed increment through the linearised predictor
+    model.apply_step(1.0, (precision, 0, LIN_TOL))
+    ctx = model.ctx
+    ctx.set_iteration(-1)
+    ctx.residual(want_vector=False)
+    ctx.checkpoint()
+    return mesh, model, ctx
+
+
+def one_iteration(ctx, precision, lin_tol):
+    ctx.rollback()
+    ctx.set_iteration(-1)
+    return ctx.newton_iteration(precision=precision, lin_rel_tol=lin_tol, lin_max_it=20000)
+
+
+def cpu_baseline(mesh, gpu_pcg_iters, threads, n_pcg=10):
+    """Oracle port timed on the host cores: one residual + tangent + MSR
+    assembly pass over all elements and n_pcg Jacobi-PCG iterations on the
+    assembled system, extrapolated to the GPU's inner iteration count."""
+    from oracle.pyoracle import OracleModel
+    from tahoe_gb300 import workloads
+    _, om, _ = workloads.c2(add=lambda X, conn, form, mat: OracleModel(X, conn, form, mat, threads=threads))
+    u = np.zeros((mesh.nnd, 3))
+    top = mesh.face_nodes(2, 1)
+    u[top, 2] = -0.01
+    om.equations()
+    t0 = time.perf_counter()
+    R, val, bindx = om.form(u, 1.0, -1, want_K=True)
+    t_form = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    om.pcg(val, R, 1e-30, n_pcg)
+    t_pcg = (time.perf_counter() - t0) / n_pcg
+    ms = 1e3 * (t_form + gpu_pcg_iters * t_pcg)
+    return ms, t_form, t_pcg
+
+
+def run_ours(args):
+    ws, rank, local = dist_init()
+    from tahoe_gb300 import lib, workloads
+    prec = lib.MIXED if args.precision == "mixed" else lib.FP64
+    mesh, model, ctx = setup_c2(local, prec)
+
+    # warm-up (also captures the PCG graph)
+    its_seen = []
+    for _ in range(max(args.warmup, 1)):
+        nrm, its = one_iteration(ctx, prec, LIN_TOL)
+        its_seen.append(its)
+
+    sampler = ClockSampler(local)
+    barrier(ws)
+    sampler.start()
+    launches0 = ctx.launches
+    ctx.timer_start()
+    pcg_its = []
+    for _ in range(args.steps):
+        nrm, its = one_iteration(ctx, prec, LIN_TOL)
+        pcg_its.append(its)
+    ms_total = ctx.timer_stop()
+    launches = ctx.launches - launches0
+    clocks = sampler.stop()
+    barrier(ws)
+    ms_total = max_over_ranks(ws, ms_total)
+    ms_step = ms_total / args.steps
+
+    # e2e through the C ABI with host buffers
+    ctx.rollback()
+    u0 = ctx.get_u().copy()
+    nnd = mesh.nnd
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.set_u(u0)
+        ctx.set_iteration(-1)
+        ctx.residual(want_vector=False)
+        ctx.newton_iteration(precision=prec, lin_rel_tol=LIN_TOL)
+        u_out = ctx.get_u()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = max_over_ranks(ws, e2e_ms)
+    # back to the step-start snapshot for the kernel timings below
+    ctx.set_u(u0)
+    ctx.set_iteration(-1)
+    ctx.residual(want_vector=False)
+    ctx.checkpoint()
+
+    # per-kernel device times (CUDA events on the context stream)
+    ctx.tangent(prec)
+    t_spmv = ctx.time_kernel(0, 20)
+    t_upd = ctx.time_kernel(1, 20)
+    t_tan = ctx.time_kernel(2, 5)
+    t_asm = ctx.time_kernel(3, 5)
+    t_res = ctx.time_kernel(4, 5)
+    s_val = 4 if prec == lib.MIXED else 8
+    nnzb = ctx.block_nnz
+    bytes_spmv = workloads.spmv_bytes(nnzb, nnd, s_val)
+    peak, peak_kind = peaks()
+    achieved = bytes_spmv / (t_spmv * 1e-3) / 1e9
+    elements_per_s = mesh.nel / ((t_tan + t_asm) * 1e-3)
+
+    # full load step to NEWTON_TOL in both forms: Newton iterations, time, agreement
+    extra = {}
+    if not args.quick:
+        res = {}
+        for name, p in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
+            ctx.rollback()
+            ctx.timer_start()
+            rc, rep = ctx.newton(rel_tol=NEWTON_TOL, abs_tol=0.0, div_tol=10.0, max_iterations=20, precision=p,
+                                 lin_rel_tol=LIN_TOL, lin_max_it=20000, check=False)
+            ms = ctx.timer_stop()
+            res[name] = (ctx.get_u().copy(), rep, ms, rc)
+        uf, um = res["fp64"][0], res["mixed"][0]
+        extra = {
+            "load_step": {k: {"ms": round(v[2], 3), "newton_iterations": v[1].iterations,
+                              "pcg_iterations": v[1].pcg_iterations, "status": v[3],
+                              "ms_per_newton_iteration": round(v[2] / max(v[1].iterations, 1), 3)}
+                          for k, v in res.items()},
+            "rel_err_mixed_vs_fp64": float(np.abs(um - uf).max() / np.abs(uf).max()),
+        }
+
+    line = {
+        "metric": "Newton-step time",
+        "value": round(ms_step, 4),
+        "unit": "ms/Newton iteration",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 tangent+PCG, fp64 residual/dots" if prec == lib.MIXED else "fp64",
+        "data": "synthetic (seeded 64^3 jittered hex8 block)",
+        "config": {"workload": "C2: 64^3 hex8 total-Lagrangian Simo neo-Hookean (mu=1, kappa=10), jitter 0.2h seed 0, "
+                               "load step 1/10, one Newton iteration (inner Jacobi-PCG rel tol %g)" % LIN_TOL,
+                   "nel": mesh.nel, "nodes": nnd, "dofs": nnd * 3, "equations": ctx.neq, "block_nnz": nnzb,
+                   "scalar_nnz": int(nnzb * 9), "parallelism": "replicas x%d" % ws,
+                   "l2": "inputs larger than L2 (block CSR %.0f MB)" % (nnzb * (9 * s_val + 4) / 1e6)},
+        "pcg_iterations_per_step": float(np.mean(pcg_its)),
+        "elements_assembled_per_s": round(elements_per_s, 1),
+        "kernel_ms": {"pcg_spmv": round(t_spmv, 5), "pcg_update": round(t_upd, 5), "tangent": round(t_tan, 4),
+                      "assembly": round(t_asm, 4), "residual": round(t_res, 4)},
+        "roofline": {"kernel": "pcg_spmv_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "algorithmic_bytes": int(bytes_spmv), "traffic": None},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/Newton iteration", "h2d_bytes_per_step": nnd * 32,
+                "d2h_bytes_per_step": nnd * 32},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    line.update(extra)
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cms, t_form, t_pcg = cpu_baseline(mesh, float(np.mean(pcg_its)), threads)
+        line["cpu_baseline"] = {
+            "value": round(cms, 1), "unit": "ms/Newton iteration", "cores": threads, "kind": "port",
+            "sample": "oracle: one residual+tangent+MSR assembly pass over all %d elements (%.2f s, %d threads) and "
+                      "10 serial Jacobi-PCG iterations on the MSR system (%.1f ms each), extrapolated to %.0f inner "
+                      "iterations" % (mesh.nel, t_form, threads, t_pcg * 1e3, float(np.mean(pcg_its)))}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_reference(args):
+    ws, rank, local = dist_init()
+    if rank != 0:
+        return
+    from tahoe_gb300.meshgen import BoxMesh
+    mesh = BoxMesh(64, 64, 64, jitter=0.2, seed=0)
+    threads = os.cpu_count() or 1
+    n_its = args.ref_pcg_iters
+    times = []
+    for k in range(args.warmup + args.steps):
+        ms, t_form, t_pcg = cpu_baseline(mesh, n_its, threads, n_pcg=5)
+        if k >= args.warmup:
+            times.append(ms)
+    v = float(np.mean(times))
+    line = {
+        "impl": "reference", "metric": "Newton-step time", "value": round(v, 1), "unit": "ms/Newton iteration",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 1),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded 64^3 jittered hex8 block)",
+        "config": {"workload": "C2: 64^3 hex8 total-Lagrangian Simo neo-Hookean (mu=1, kappa=10), jitter 0.2h seed 0, "
+                               "load step 1/10, one Newton iteration (inner Jacobi-PCG rel tol %g)" % LIN_TOL},
+        "cpu_baseline": {"value": round(v, 1), "unit": "ms/Newton iteration", "cores": threads, "kind": "port",
+                         "sample": "per step: residual+tangent+MSR assembly over all elements + 5 Jacobi-PCG "
+                                   "iterations, extrapolated to %d inner iterations" % n_its},
+        "e2e": {"value": round(v, 1), "unit": "ms/Newton iteration", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--quick", action="store_true", help="skip the full load-step comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--ref-pcg-iters", type=int, default=600)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,224 @@
+/*
+ * tahoe_gb300 -- C ABI of the GB300 implicit hex8 solid path.
+ *
+ * The entry points below are what a Tahoe host build binds when a deck
+ * selects the GPU element group and the GPU matrix/solver type.  They replace
+ * the per-element virtual calls and the CPU global-matrix classes of the
+ * reference; each declaration names the reference interface it stands in for
+ * (paths relative to the Tahoe source tree).
+ *
+ * Conventions
+ *   - every entry point returns an int status: TG_OK (0) or a negative
+ *     TG_ERR_* code; nothing throws across the ABI and no kernel traps;
+ *   - equation numbers are the reference's: 1-based, node-major/dof-minor,
+ *     <= 0 for prescribed dofs (NodeManagerT::SetEquationNumbers);
+ *   - "nodal" arrays are nnd*3 doubles, node-major (x,y,z per node);
+ *     "equation" arrays are neq doubles indexed by equation number - 1;
+ *   - one CUDA stream per context; a context is not thread-safe.
+ */
+#ifndef TAHOE_GB300_H
+#define TAHOE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tg_context tg_context;
+
+enum tg_status {
+  TG_OK = 0,
+  TG_ERR_ARG = -1,            /* bad argument or call order */
+  TG_ERR_CUDA = -2,           /* CUDA runtime error (text in tg_last_error) */
+  TG_ERR_OOM = -3,            /* device allocation failed */
+  TG_ERR_BAD_JACOBIAN = -4,   /* det J <= 0 or J <= 0 (ExceptionT::kBadJacobianDet) */
+  TG_ERR_NAN = -5,            /* non-finite residual or Krylov scalar */
+  TG_ERR_NOT_CONVERGED = -6,  /* iteration limit hit (NLSolver kFailed) */
+  TG_ERR_DIVERGED = -7,       /* relative error above divergence tolerance */
+  TG_ERR_CAPACITY = -8        /* size above a fixed capacity */
+};
+
+enum tg_formulation { TG_SMALL_STRAIN = 0, TG_TOTAL_LAGRANGIAN = 1 };
+
+enum tg_material_kind {
+  TG_MAT_SS_HOOKEAN = 0,  /* small_strain_StVenant / small_strain_Hookean: {E,nu} or C[36] row-major */
+  TG_MAT_SS_J2 = 1,       /* small_strain_StVenant_J2: {E, nu, a, b[, elastic_iterations]} */
+  TG_MAT_FS_SIMO = 2,     /* Simo_isotropic: {mu, kappa} */
+  TG_MAT_FS_STVENANT = 3  /* large_strain_StVenant: {E, nu} */
+};
+
+/* TG_FP64: plain form (FP64 tangent, FP64 CSR, FP64 PCG).
+ * TG_MIXED: FP32 element tangent, FP32 CSR and inner PCG vectors, FP64
+ *           residual, FP64 Krylov dot products/norms and FP64 Newton test. */
+enum tg_precision { TG_FP64 = 0, TG_MIXED = 1 };
+enum tg_precond { TG_PRECOND_JACOBI = 0, TG_PRECOND_BLOCK_JACOBI = 1 };
+
+/* J2 integration-point flags (J2SSC0HardeningT.h:32-34) plus "never yielded"
+ * (the reference leaves such ElementCardT storage unallocated). */
+enum tg_j2_flag { TG_J2_PLASTIC = 0, TG_J2_ELASTIC = 1, TG_J2_RESET = 3, TG_J2_UNALLOCATED = 7 };
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Creates a context on a CUDA device (one stream).  Stands in for the
+ * construction of an element group + global matrix (ElementListT::NewElement,
+ * ElementListT.cpp:649; SolverT::SetGlobalMatrix, SolverT.cpp:1073). */
+int tg_create(tg_context** ctx, int device);
+int tg_destroy(tg_context* ctx);
+/* text of the last error on this context (never NULL) */
+const char* tg_last_error(const tg_context* ctx);
+/* number of kernels this library launched on the context so far (graph
+ * launches count every kernel node they run) */
+long long tg_launch_count(const tg_context* ctx);
+
+/* ---- mesh, equations, materials ---------------------------------------- */
+
+/* Uploads the element block: coordinates as structure-of-arrays
+ * (x[0..nnd), y[..], z[..]), hex8 connectivity (nel*8, 0-based, reference
+ * node order HexahedronT.cpp:23-25) and the equation array (nnd*3).
+ * Replaces ContinuumElementT::TakeParameterList geometry set-up
+ * (ContinuumElementT.cpp:1330) + ElementBaseT::Equations (ElementBaseT.cpp:196)
+ * + GlobalMatrixT::AddEquationSet/Initialize (MSRMatrixT.cpp:35-57). */
+int tg_mesh_upload(tg_context* ctx, int nnd, const double* coords_soa, int nel, const int* conn,
+                   const int* eqnos);
+/* small_strain / total_lagrangian (ElementListT.cpp:738,752) */
+int tg_element_set(tg_context* ctx, int formulation);
+/* material of element block `block` (SSSolidMatList3DT.cpp:199-207,
+ * FSSolidMatList3DT.cpp:409-415) */
+int tg_material_set(tg_context* ctx, int block, int kind, const double* params, int nparams);
+/* block index of every element (nel ints); default all 0 */
+int tg_element_blocks(tg_context* ctx, const int* block_of_element);
+
+/* Scalar CSR structure over the active equations, rows and columns 0-based
+ * equation indices, columns sorted.  upper_only keeps col >= row (the MSR
+ * symmetric pattern of MSRBuilderT::GenerateMSR, MSRBuilderT.cpp:134, with
+ * the diagonal stored in-row).  Call with row_ptr == NULL to get *nnz. */
+int tg_pattern_build(tg_context* ctx, int upper_only, int* row_ptr, int* col_idx, long long* nnz);
+/* number of active equations / structural block nonzeros */
+int tg_sizes(const tg_context* ctx, int* neq, long long* block_nnz);
+
+/* ---- state, loads -------------------------------------------------------- */
+
+/* nodal displacement (nnd*3), host <-> device */
+int tg_set_displacement(tg_context* ctx, const double* u_nodal);
+int tg_get_displacement(tg_context* ctx, double* u_nodal);
+/* prescribed values at `n` dofs (index node*3+dof) -- FieldT::InitStep /
+ * ConsistentKBC (FieldT.cpp:261-322) */
+int tg_set_prescribed(tg_context* ctx, int n, const int* dof_index, const double* values);
+/* reference nodal external force (nnd*3) and its current load factor:
+ * Fext = factor * f (force_BC and traction nodal forces; ScheduleT value) */
+int tg_set_external_force(tg_context* ctx, const double* f_nodal);
+int tg_set_load_factor(tg_context* ctx, double factor);
+/* consistent nodal forces of uniform Cartesian tractions on hex8 facets in
+ * the reference configuration (ContinuumElementT::ApplyTractionBC,
+ * ContinuumElementT.cpp:514-665); host-only helper, accumulates into f_nodal */
+int tg_traction_forces(int nnd, const double* coords_soa, int nel, const int* conn, int nfacets,
+                       const int* elem, const int* facet, const double* traction3, double* f_nodal);
+/* group iteration number seen by history materials (SolverT fNumIteration,
+ * SolverT.cpp:148; read by J2SSKStV::s_ij, J2SSKStV.cpp:69) */
+int tg_set_iteration(tg_context* ctx, int iteration);
+
+/* ---- element group: residual and tangent -------------------------------- */
+
+/* R = Fext - Fint(u) on the active equations in FP64 (SolidElementT::
+ * ElementRHSDriver, SolidElementT.cpp:1166, + SolverT::AssembleRHS,
+ * SolverT.cpp:446).  R_out (neq) may be NULL (kept on the device); norm_out
+ * receives ||R||_2 (SolverT::Residual, SolverT.cpp:848). */
+int tg_form_residual(tg_context* ctx, double* R_out, double* norm_out);
+/* element stiffness + deterministic CSR assembly + preconditioner in the
+ * given precision, device resident (SolidElementT::ElementLHSDriver,
+ * SolidElementT.cpp:1100 + MSRMatrixT::Assemble, MSRMatrixT.cpp:66) */
+int tg_form_tangent(tg_context* ctx, int precision);
+/* assembled values of the last tangent on the tg_pattern_build structure
+ * (MSRMatrixT::GenerateRCV, MSRMatrixT.cpp:474, for parity dumps) */
+int tg_get_tangent_csr(tg_context* ctx, int upper_only, double* vals);
+/* element matrices/internal forces of elements [first, first+count) at the
+ * current u, FP64 (Ke 24x24 row-major, fint 24), for parity dumps */
+int tg_element_dump(tg_context* ctx, int first, int count, double* Ke, double* fint);
+
+/* ---- Krylov solve and update ------------------------------------------- */
+
+/* Solves K du = rhs with (block-)Jacobi PCG on the last tangent.  rhs == NULL
+ * uses the device residual of tg_form_residual; du == NULL keeps the result
+ * on the device for tg_apply_update.  Replaces GlobalMatrixT::Solve
+ * (GlobalMatrixT.cpp:77) with the Krylov solve of the spec path. */
+int tg_pcg_solve(tg_context* ctx, const double* rhs, double* du, double rel_tol, int max_it, int precond,
+                 int* iterations, double* rel_res);
+/* u += du on the active dofs (FEManagerT::Update -> FieldT::ApplyUpdate,
+ * FieldT.cpp:531-563) */
+int tg_apply_update(tg_context* ctx);
+
+/* ---- history ------------------------------------------------------------ */
+
+/* J2 history update after a converged step / reset after a failed one
+ * (ContinuumElementT::CloseStep/ResetStep, ContinuumElementT.cpp:148,178;
+ * J2SSC0HardeningT::Update/Reset, J2SSC0HardeningT.cpp:204,244) */
+int tg_close_step(tg_context* ctx);
+int tg_reset_step(tg_context* ctx);
+/* per-integration-point flags (nel*8, tg_j2_flag) -- the active set */
+int tg_get_active_set(tg_context* ctx, signed char* flags);
+/* equivalent plastic strain alpha (nel*8) and plastic strain (nel*8*6) */
+int tg_get_j2_state(tg_context* ctx, double* alpha, double* eps_p);
+
+/* ---- Newton (NLSolver) --------------------------------------------------- */
+
+typedef struct tg_newton_params {
+  double rel_tol;       /* NLSolver rel_tolerance */
+  double abs_tol;       /* NLSolver abs_tolerance */
+  double div_tol;       /* NLSolver divergence_tolerance */
+  int max_iterations;   /* NLSolver max_iterations */
+  int precision;        /* tg_precision */
+  int precond;          /* tg_precond */
+  double lin_rel_tol;   /* inner PCG relative tolerance */
+  int lin_max_it;       /* inner PCG iteration cap */
+} tg_newton_params;
+
+typedef struct tg_newton_report {
+  int iterations;       /* Newton iterations taken */
+  int pcg_iterations;   /* total inner PCG iterations */
+  double error0;        /* ||R|| at the first residual */
+  double error;         /* ||R|| at exit */
+  double ms_residual, ms_tangent, ms_solve; /* device time by phase */
+} tg_newton_report;
+
+/* One Newton iteration of NLSolver::Solve's loop body (NLSolver.cpp:137-188):
+ * tangent + assembly, PCG on the device residual, u += du, iteration + 1, new
+ * residual.  *norm receives the new ||R||; *pcg_iterations the inner count. */
+int tg_newton_iteration(tg_context* ctx, const tg_newton_params* params, double* norm, int* pcg_iterations);
+
+/* Load-step predictor for prescribed displacements: with u at the last
+ * converged state and the step's load factor set, solves
+ * K(u) du = R(u) - K(u)[du_p] for the free dofs (du_p = new - current values
+ * at the n prescribed dofs), then sets u_p to the new values and u_f += du_f.
+ * The reference applies the jump to the prescribed dofs alone before the
+ * first residual (FieldT::InitStep, FieldT.cpp:261-322), which is fine for its
+ * direct solvers but can leave an indefinite first tangent that breaks CG on
+ * fine finite-strain meshes; the converged step is the same either way.
+ * History variables are not modified. */
+int tg_predict_prescribed(tg_context* ctx, int n, const int* dof_index, const double* values,
+                          const tg_newton_params* params, int* pcg_iterations);
+
+/* Device snapshot of the displacement and residual, and its restore: the
+ * last-converged-state reset of FEManagerT::ResetStep (FEManagerT.cpp:247-262)
+ * used for step cuts; also lets a caller repeat an identical iteration. */
+int tg_checkpoint(tg_context* ctx);
+int tg_rollback(tg_context* ctx);
+
+/* One load step of NLSolver::Solve (NLSolver.cpp:57-262) with its exit test
+ * (NLSolver::ExitIteration, NLSolver.cpp:675-755): the caller has applied the
+ * step's prescribed values and load factor.  Iteration numbers run from -1
+ * as in SolverT::InitStep.  Does not close the step. */
+int tg_newton_solve(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report);
+
+/* ---- measurement helpers (no reference counterpart) --------------------- */
+
+/* CUDA events on the context stream around caller-defined work */
+int tg_timer_start(tg_context* ctx);
+int tg_timer_stop(tg_context* ctx, double* ms);
+/* average device time of `reps` standalone launches of one hot kernel on the
+ * current state: 0 PCG SpMV, 1 PCG vector update, 2 element tangent,
+ * 3 assembly, 4 element residual (+gather) */
+int tg_time_kernel(tg_context* ctx, int which, int reps, double* ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TAHOE_GB300_H */

@@ -686,8 +686,9 @@ int pcg(const Model& M, const double* val, const double* b, double* x, double to
   return -maxit;
 }
 
-/* dense Cholesky solve of the MSR system (stand-in for the reference's
- * direct profile/SPOOLES factorisation on small decks) */
+/* dense LU (partial pivoting) solve of the MSR system: stands in for the
+ * reference's direct profile / SPOOLES factorisations on small decks, which
+ * accept symmetric indefinite tangents */
 int dense_solve(const Model& M, const double* val, const double* b, double* x) {
   int n = M.neq;
   std::vector<double> A((size_t)n * n, 0.0);
@@ -698,27 +699,28 @@ int dense_solve(const Model& M, const double* val, const double* b, double* x) {
       A[(size_t)r * n + c] = A[(size_t)c * n + r] = val[j];
     }
   }
-  for (int j = 0; j < n; ++j) {
-    double d = A[(size_t)j * n + j];
-    for (int k = 0; k < j; ++k) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
-    if (!(d > 0)) return -1;
-    d = std::sqrt(d);
-    A[(size_t)j * n + j] = d;
-    for (int i = j + 1; i < n; ++i) {
-      double s = A[(size_t)i * n + j];
-      for (int k = 0; k < j; ++k) s -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
-      A[(size_t)i * n + j] = s / d;
+  std::vector<double> y(b, b + n);
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(A[(size_t)i * n + k]) > std::fabs(A[(size_t)piv * n + k])) piv = i;
+    if (A[(size_t)piv * n + k] == 0.0) return -1;
+    if (piv != k) {
+      for (int j = 0; j < n; ++j) std::swap(A[(size_t)k * n + j], A[(size_t)piv * n + j]);
+      std::swap(y[k], y[piv]);
     }
-  }
-  std::vector<double> y(n);
-  for (int i = 0; i < n; ++i) {
-    double s = b[i];
-    for (int k = 0; k < i; ++k) s -= A[(size_t)i * n + k] * y[k];
-    y[i] = s / A[(size_t)i * n + i];
+    const double d = A[(size_t)k * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      const double l = A[(size_t)i * n + k] / d;
+      if (l == 0.0) continue;
+      A[(size_t)i * n + k] = l;
+      for (int j = k + 1; j < n; ++j) A[(size_t)i * n + j] -= l * A[(size_t)k * n + j];
+      y[i] -= l * y[k];
+    }
   }
   for (int i = n - 1; i >= 0; --i) {
     double s = y[i];
-    for (int k = i + 1; k < n; ++k) s -= A[(size_t)k * n + i] * x[k];
+    for (int j = i + 1; j < n; ++j) s -= A[(size_t)i * n + j] * x[j];
     x[i] = s / A[(size_t)i * n + i];
   }
   return 0;

@@ -1,0 +1,457 @@
+// C ABI of the tahoe_gb300 library: context, mesh/equation set-up, state and
+// load management, and the Newton driver (NLSolver equivalent) over the
+// device kernels.  Host code only; kernels live in the .cu files.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tg_internal.h"
+
+namespace tg {
+
+bool ok(Context* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+void dfree(Context* c, void* p) {
+  if (!p) return;
+  cudaFree(p);
+  auto it = std::find(c->allocations.begin(), c->allocations.end(), p);
+  if (it != c->allocations.end()) c->allocations.erase(it);
+}
+
+namespace {
+
+void free_all(Context* c) {
+  if (c->ev_a) cudaEventDestroy(c->ev_a);
+  if (c->ev_b) cudaEventDestroy(c->ev_b);
+  c->ev_a = c->ev_b = nullptr;
+  c->d_u_ckpt = c->d_R_ckpt = nullptr;
+  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
+  c->pcg_graph = nullptr;
+  for (void* p : c->allocations) cudaFree(p);
+  c->allocations.clear();
+  if (c->h_pcg) cudaFreeHost(c->h_pcg);
+  if (c->h_resid) cudaFreeHost(c->h_resid);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  c->h_pcg = nullptr;
+  c->h_resid = nullptr;
+  c->h_status = nullptr;
+}
+
+int set_device(Context* c) { return ok(c, cudaSetDevice(c->device), "cudaSetDevice") ? TG_OK : TG_ERR_CUDA; }
+
+// read back the device status word and residual norm; clears the status
+int sync_status(Context* c) {
+  if (!ok(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "status"))
+    return TG_ERR_CUDA;
+  if (!ok(c, cudaStreamSynchronize(c->stream), "sync")) return TG_ERR_CUDA;
+  const int st = *c->h_status;
+  if (st) {
+    cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+    if (st & kStatusBadJacobian) {
+      c->err = "non-positive Jacobian determinant";
+      return TG_ERR_BAD_JACOBIAN;
+    }
+    c->err = "non-finite value";
+    return TG_ERR_NAN;
+  }
+  return TG_OK;
+}
+
+bool valid_material(int kind, const double* p, int np, MatParams& m) {
+  std::memset(&m, 0, sizeof(m));
+  m.kind = kind;
+  auto set_E_nu = [&](double E, double nu) {  // IsotropicT::Set_E_nu (IsotropicT.cpp:32-44)
+    if (E < 0.0 || nu > 0.5 || nu < -1.0) return false;
+    m.mu = 0.5 * E / (1.0 + nu);
+    m.lambda = 2.0 * m.mu * nu / (1.0 - 2.0 * nu);
+    m.kappa = m.lambda + 2.0 / 3.0 * m.mu;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) m.C[i * 6 + j] = m.lambda + (i == j ? 2.0 * m.mu : 0.0);
+    for (int i = 3; i < 6; ++i) m.C[i * 6 + i] = m.mu;
+    return true;
+  };
+  switch (kind) {
+    case TG_MAT_SS_HOOKEAN:
+      if (np == 36) {
+        std::memcpy(m.C, p, sizeof(m.C));
+        return true;
+      }
+      return np == 2 && set_E_nu(p[0], p[1]);
+    case TG_MAT_SS_J2:
+      if (np < 4 || !set_E_nu(p[0], p[1])) return false;
+      m.hard_a = p[2];
+      m.hard_b = p[3];
+      m.elastic_its = np > 4 ? (int)p[4] : 0;
+      return true;
+    case TG_MAT_FS_SIMO:  // IsotropicT::Set_mu_kappa (IsotropicT.cpp:46-57)
+      if (np != 2 || p[0] < 0.0 || p[1] < 0.0) return false;
+      m.mu = p[0];
+      m.kappa = p[1];
+      return true;
+    case TG_MAT_FS_STVENANT:
+      return np == 2 && set_E_nu(p[0], p[1]);
+    default:
+      return false;
+  }
+}
+
+}  // namespace
+}  // namespace tg
+
+using namespace tg;
+
+
+extern "C" {
+
+int tg_create(tg_context** out, int device) {
+  if (!out) return TG_ERR_ARG;
+  *out = nullptr;
+  tg_context* c = new tg_context();
+  c->device = device;
+  c->mats.nblocks = 1;
+  c->mats.formulation = TG_SMALL_STRAIN;
+  if (set_device(c) || !ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
+      !ok(c, cudaMallocHost((void**)&c->h_pcg, sizeof(PcgScalars)), "pinned") ||
+      !ok(c, cudaMallocHost((void**)&c->h_resid, sizeof(ResidScalars)), "pinned") ||
+      !ok(c, cudaMallocHost((void**)&c->h_status, sizeof(int)), "pinned")) {
+    free_all(c);
+    delete c;
+    return TG_ERR_CUDA;
+  }
+  *out = c;
+  return TG_OK;
+}
+
+int tg_destroy(tg_context* c) {
+  if (!c) return TG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_all(c);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return TG_OK;
+}
+
+const char* tg_last_error(const tg_context* c) { return c ? c->err.c_str() : "null context"; }
+long long tg_launch_count(const tg_context* c) { return c ? c->launches : 0; }
+
+int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const int* conn, const int* eqnos) {
+  if (!c || nnd <= 0 || nel <= 0 || !coords || !conn || !eqnos) return TG_ERR_ARG;
+  if ((long long)nel * 64 >= (1LL << 31)) {
+    c->err = "too many elements for the 32-bit contribution map";
+    return TG_ERR_CAPACITY;
+  }
+  for (long long k = 0; k < (long long)nel * 8; ++k)
+    if (conn[k] < 0 || conn[k] >= nnd) {
+      c->err = "connectivity out of range";
+      return TG_ERR_ARG;
+    }
+  if (set_device(c)) return TG_ERR_CUDA;
+  cudaStreamSynchronize(c->stream);
+  free_all(c);
+  if (!ok(c, cudaMallocHost((void**)&c->h_pcg, sizeof(PcgScalars)), "pinned") ||
+      !ok(c, cudaMallocHost((void**)&c->h_resid, sizeof(ResidScalars)), "pinned") ||
+      !ok(c, cudaMallocHost((void**)&c->h_status, sizeof(int)), "pinned"))
+    return TG_ERR_CUDA;
+  c->pcg_vec_precision = -1;
+  c->pcg_graph_key = -1;
+  c->tangent_precision = -1;
+  c->d_x = c->d_r = c->d_z = c->d_p = c->d_q = nullptr;
+  c->d_Ke32 = nullptr;
+  c->d_Ke64 = nullptr;
+  c->d_vals32 = nullptr;
+  c->d_vals64 = nullptr;
+  c->d_minv32 = nullptr;
+  c->d_minv64 = nullptr;
+  c->d_block = nullptr;
+  c->have_blocks = false;
+  c->have_du = false;
+  c->nnd = nnd;
+  c->nel = nel;
+  c->h_conn.assign(conn, conn + (size_t)nel * 8);
+  c->h_eqnos.assign(eqnos, eqnos + (size_t)nnd * 3);
+  c->h_coords.assign(coords, coords + (size_t)nnd * 3);
+  // active equations must be 1..neq in node-major / dof-minor order
+  int neq = 0;
+  std::vector<uint8_t> mask(nnd, 0);
+  c->h_eq_slot.clear();
+  for (int n = 0; n < nnd; ++n)
+    for (int d = 0; d < 3; ++d) {
+      const int q = eqnos[n * 3 + d];
+      if (q > 0) {
+        if (q != neq + 1) {
+          c->err = "equation numbers must be ascending node-major from 1";
+          return TG_ERR_ARG;
+        }
+        ++neq;
+        mask[n] |= (uint8_t)(1u << d);
+        c->h_eq_slot.push_back(n * 4 + d);
+      }
+    }
+  c->neq = neq;
+
+  build_block_pattern(nnd, nel, conn, c->h_rowptr, c->h_col);
+  std::vector<int> cptr, contrib, nptr, nlist;
+  build_contrib_map(nnd, nel, conn, c->h_rowptr, c->h_col, cptr, contrib);
+  build_node_elem(nnd, nel, conn, nptr, nlist);
+  c->nnzb = c->h_rowptr[nnd];
+  c->nnzb_pad = (c->nnzb + 31) / 32 * 32;
+
+  const size_t nip = (size_t)nel * 8;
+  bool good = dalloc(c, &c->d_X, (size_t)nnd * 3) && dalloc(c, &c->d_conn, (size_t)nel * 8) &&
+              dalloc(c, &c->d_mask, (size_t)nnd) && dalloc(c, &c->d_eq_slot, (size_t)std::max(neq, 1)) &&
+              dalloc(c, &c->d_node_elem_ptr, (size_t)nnd + 1) && dalloc(c, &c->d_node_elem, nip) &&
+              dalloc(c, &c->d_rowptr, (size_t)nnd + 1) && dalloc(c, &c->d_col, (size_t)c->nnzb) &&
+              dalloc(c, &c->d_contrib_ptr, (size_t)c->nnzb + 1) && dalloc(c, &c->d_contrib, (size_t)nel * 64) &&
+              dalloc(c, &c->d_u, (size_t)nnd) && dalloc(c, &c->d_fext, (size_t)nnd) && dalloc(c, &c->d_R, (size_t)nnd) &&
+              dalloc(c, &c->d_fint, nip) && dalloc(c, &c->d_status, 1) && dalloc(c, &c->d_resid, 1) &&
+              dalloc(c, &c->d_pcg, 1);
+  c->partials_cap = 4096;
+  good = good && dalloc(c, &c->d_partials, (size_t)c->partials_cap * 2);
+  good = good && dalloc(c, &c->d_j2_flags, nip) && dalloc(c, &c->d_j2_alloc, (size_t)nel) &&
+         dalloc(c, &c->d_j2_alpha, nip) && dalloc(c, &c->d_j2_dgamma, nip) && dalloc(c, &c->d_j2_norm, nip) &&
+         dalloc(c, &c->d_j2_epsp, nip * 6) && dalloc(c, &c->d_j2_nhat, nip * 6);
+  if (!good) return TG_ERR_OOM;
+  cudaStream_t s = c->stream;
+  good = ok(c, cudaMemcpyAsync(c->d_X, coords, sizeof(double) * nnd * 3, cudaMemcpyHostToDevice, s), "X") &&
+         ok(c, cudaMemcpyAsync(c->d_conn, conn, sizeof(int) * nel * 8, cudaMemcpyHostToDevice, s), "conn") &&
+         ok(c, cudaMemcpyAsync(c->d_mask, mask.data(), nnd, cudaMemcpyHostToDevice, s), "mask") &&
+         ok(c, cudaMemcpyAsync(c->d_eq_slot, c->h_eq_slot.data(), sizeof(int) * neq, cudaMemcpyHostToDevice, s), "slot") &&
+         ok(c, cudaMemcpyAsync(c->d_node_elem_ptr, nptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, s), "np") &&
+         ok(c, cudaMemcpyAsync(c->d_node_elem, nlist.data(), sizeof(int) * nip, cudaMemcpyHostToDevice, s), "nl") &&
+         ok(c, cudaMemcpyAsync(c->d_rowptr, c->h_rowptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, s), "rp") &&
+         ok(c, cudaMemcpyAsync(c->d_col, c->h_col.data(), sizeof(int) * c->nnzb, cudaMemcpyHostToDevice, s), "col") &&
+         ok(c, cudaMemcpyAsync(c->d_contrib_ptr, cptr.data(), sizeof(int) * (c->nnzb + 1), cudaMemcpyHostToDevice, s), "cp") &&
+         ok(c, cudaMemcpyAsync(c->d_contrib, contrib.data(), sizeof(int) * (size_t)nel * 64, cudaMemcpyHostToDevice, s), "ct") &&
+         ok(c, cudaMemsetAsync(c->d_u, 0, sizeof(double4_32a) * nnd, s), "u") &&
+         ok(c, cudaMemsetAsync(c->d_fext, 0, sizeof(double4_32a) * nnd, s), "f") &&
+         ok(c, cudaMemsetAsync(c->d_R, 0, sizeof(double4_32a) * nnd, s), "R") &&
+         ok(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s), "st") &&
+         ok(c, cudaMemsetAsync(c->d_resid, 0, sizeof(ResidScalars), s), "rs") &&
+         ok(c, cudaMemsetAsync(c->d_pcg, 0, sizeof(PcgScalars), s), "pcg") &&
+         ok(c, cudaMemsetAsync(c->d_j2_flags, TG_J2_UNALLOCATED, nip, s), "fl") &&
+         ok(c, cudaMemsetAsync(c->d_j2_alloc, 0, nel, s), "al") &&
+         ok(c, cudaMemsetAsync(c->d_j2_alpha, 0, sizeof(double) * nip, s), "a") &&
+         ok(c, cudaMemsetAsync(c->d_j2_dgamma, 0, sizeof(double) * nip, s), "dg") &&
+         ok(c, cudaMemsetAsync(c->d_j2_norm, 0, sizeof(double) * nip, s), "nr") &&
+         ok(c, cudaMemsetAsync(c->d_j2_epsp, 0, sizeof(double) * nip * 6, s), "ep") &&
+         ok(c, cudaMemsetAsync(c->d_j2_nhat, 0, sizeof(double) * nip * 6, s), "nh") &&
+         ok(c, cudaStreamSynchronize(s), "upload sync");
+  return good ? TG_OK : TG_ERR_CUDA;
+}
+
+int tg_element_set(tg_context* c, int formulation) {
+  if (!c || (formulation != TG_SMALL_STRAIN && formulation != TG_TOTAL_LAGRANGIAN)) return TG_ERR_ARG;
+  c->formulation = formulation;
+  c->mats.formulation = formulation;
+  return TG_OK;
+}
+
+int tg_material_set(tg_context* c, int block, int kind, const double* params, int np) {
+  if (!c || block < 0 || block >= kMaxBlocks || !params) return TG_ERR_ARG;
+  MatParams m;
+  if (!valid_material(kind, params, np, m)) {
+    c->err = "invalid material parameters";
+    return TG_ERR_ARG;
+  }
+  c->mats.m[block] = m;
+  c->mats.nblocks = std::max(c->mats.nblocks, block + 1);
+  c->has_j2 = false;
+  for (int b = 0; b < c->mats.nblocks; ++b) c->has_j2 |= c->mats.m[b].kind == TG_MAT_SS_J2;
+  return TG_OK;
+}
+
+int tg_element_blocks(tg_context* c, const int* blocks) {
+  if (!c || !blocks || c->nel <= 0) return TG_ERR_ARG;
+  std::vector<int8_t> b(c->nel);
+  for (int e = 0; e < c->nel; ++e) {
+    if (blocks[e] < 0 || blocks[e] >= kMaxBlocks) return TG_ERR_ARG;
+    b[e] = (int8_t)blocks[e];
+  }
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (!c->d_block && !dalloc(c, &c->d_block, (size_t)c->nel)) return TG_ERR_OOM;
+  c->have_blocks = true;
+  return ok(c, cudaMemcpy(c->d_block, b.data(), c->nel, cudaMemcpyHostToDevice), "blocks") ? TG_OK : TG_ERR_CUDA;
+}
+
+int tg_sizes(const tg_context* c, int* neq, long long* nnzb) {
+  if (!c) return TG_ERR_ARG;
+  if (neq) *neq = c->neq;
+  if (nnzb) *nnzb = c->nnzb;
+  return TG_OK;
+}
+
+// Scalar expansion of the block pattern over active equations.
+int tg_pattern_build(tg_context* c, int upper_only, int* row_ptr, int* col_idx, long long* nnz) {
+  if (!c || c->nnd <= 0) return TG_ERR_ARG;
+  const int* eq = c->h_eqnos.data();
+  long long count = 0;
+  if (row_ptr) row_ptr[0] = 0;
+  int row = 0;
+  for (int I = 0; I < c->nnd; ++I)
+    for (int p = 0; p < 3; ++p) {
+      const int r = eq[I * 3 + p];
+      if (r <= 0) continue;
+      for (int k = c->h_rowptr[I]; k < c->h_rowptr[I + 1]; ++k) {
+        const int J = c->h_col[k];
+        for (int q = 0; q < 3; ++q) {
+          const int cc = eq[J * 3 + q];
+          if (cc <= 0 || (upper_only && cc < r)) continue;
+          if (col_idx) col_idx[count] = cc - 1;
+          ++count;
+        }
+      }
+      ++row;
+      if (row_ptr) row_ptr[row] = (int)count;
+    }
+  if (nnz) *nnz = count;
+  return TG_OK;
+}
+
+int tg_set_displacement(tg_context* c, const double* u) {
+  if (!c || !u || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  std::vector<double4_32a> h(c->nnd);
+  for (int n = 0; n < c->nnd; ++n) h[n] = make_double4_32a(u[n * 3], u[n * 3 + 1], u[n * 3 + 2], 0.0);
+  return ok(c, cudaMemcpyAsync(c->d_u, h.data(), sizeof(double4_32a) * c->nnd, cudaMemcpyHostToDevice, c->stream), "u") &&
+                 ok(c, cudaStreamSynchronize(c->stream), "sync")
+             ? TG_OK
+             : TG_ERR_CUDA;
+}
+
+int tg_get_displacement(tg_context* c, double* u) {
+  if (!c || !u || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  std::vector<double4_32a> h(c->nnd);
+  if (!ok(c, cudaMemcpyAsync(h.data(), c->d_u, sizeof(double4_32a) * c->nnd, cudaMemcpyDeviceToHost, c->stream), "u") ||
+      !ok(c, cudaStreamSynchronize(c->stream), "sync"))
+    return TG_ERR_CUDA;
+  for (int n = 0; n < c->nnd; ++n) {
+    u[n * 3] = h[n].x;
+    u[n * 3 + 1] = h[n].y;
+    u[n * 3 + 2] = h[n].z;
+  }
+  return TG_OK;
+}
+
+int tg_set_prescribed(tg_context* c, int n, const int* idx, const double* val) {
+  if (!c || n < 0 || (n > 0 && (!idx || !val))) return TG_ERR_ARG;
+  if (n == 0) return TG_OK;
+  for (int k = 0; k < n; ++k)
+    if (idx[k] < 0 || idx[k] >= c->nnd * 3) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int* d_idx = nullptr;
+  double* d_val = nullptr;
+  if (!ok(c, cudaMallocAsync((void**)&d_idx, sizeof(int) * n, c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&d_val, sizeof(double) * n, c->stream), "alloc"))
+    return TG_ERR_OOM;
+  int s = TG_OK;
+  if (!ok(c, cudaMemcpyAsync(d_idx, idx, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream), "idx") ||
+      !ok(c, cudaMemcpyAsync(d_val, val, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream), "val"))
+    s = TG_ERR_CUDA;
+  if (!s) s = launch_set_prescribed(c, n, d_idx, d_val);
+  cudaFreeAsync(d_idx, c->stream);
+  cudaFreeAsync(d_val, c->stream);
+  if (!s && !ok(c, cudaStreamSynchronize(c->stream), "sync")) s = TG_ERR_CUDA;
+  return s;
+}
+
+int tg_set_external_force(tg_context* c, const double* f) {
+  if (!c || !f || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  std::vector<double4_32a> h(c->nnd);
+  for (int n = 0; n < c->nnd; ++n) h[n] = make_double4_32a(f[n * 3], f[n * 3 + 1], f[n * 3 + 2], 0.0);
+  return ok(c, cudaMemcpyAsync(c->d_fext, h.data(), sizeof(double4_32a) * c->nnd, cudaMemcpyHostToDevice, c->stream), "f") &&
+                 ok(c, cudaStreamSynchronize(c->stream), "sync")
+             ? TG_OK
+             : TG_ERR_CUDA;
+}
+
+int tg_set_load_factor(tg_context* c, double factor) {
+  if (!c) return TG_ERR_ARG;
+  c->load_factor = factor;
+  return TG_OK;
+}
+
+int tg_set_iteration(tg_context* c, int it) {
+  if (!c) return TG_ERR_ARG;
+  c->iteration = it;
+  return TG_OK;
+}
+
+// HexahedronT::NodesOnFacet (HexahedronT.cpp:1913-1918) facet node lists and a
+// 2x2 Gauss rule on each facet in the reference configuration.
+int tg_traction_forces(int nnd, const double* X, int nel, const int* conn, int nf, const int* elem, const int* facet,
+                       const double* t3, double* f) {
+  static const int fn[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+  if (nnd <= 0 || nel <= 0 || !X || !conn || nf < 0 || (nf > 0 && (!elem || !facet || !t3)) || !f) return TG_ERR_ARG;
+  const double g = 1.0 / std::sqrt(3.0);
+  const double qr[4] = {-g, g, g, -g}, qs[4] = {-g, -g, g, g};
+  const double nr[4] = {-1, 1, 1, -1}, ns[4] = {-1, -1, 1, 1};
+  for (int k = 0; k < nf; ++k) {
+    if (elem[k] < 0 || elem[k] >= nel || facet[k] < 0 || facet[k] > 5) return TG_ERR_ARG;
+    int nodes[4];
+    for (int i = 0; i < 4; ++i) nodes[i] = conn[elem[k] * 8 + fn[facet[k]][i]];
+    for (int q = 0; q < 4; ++q) {
+      double Na[4], dr[4], ds[4];
+      for (int i = 0; i < 4; ++i) {
+        Na[i] = 0.25 * (1 + qr[q] * nr[i]) * (1 + qs[q] * ns[i]);
+        dr[i] = 0.25 * nr[i] * (1 + qs[q] * ns[i]);
+        ds[i] = 0.25 * ns[i] * (1 + qr[q] * nr[i]);
+      }
+      double m1[3] = {0, 0, 0}, m2[3] = {0, 0, 0};
+      for (int i = 0; i < 4; ++i)
+        for (int d = 0; d < 3; ++d) {
+          m1[d] += X[d * nnd + nodes[i]] * dr[i];
+          m2[d] += X[d * nnd + nodes[i]] * ds[i];
+        }
+      const double n3[3] = {m1[1] * m2[2] - m1[2] * m2[1], m1[2] * m2[0] - m1[0] * m2[2], m1[0] * m2[1] - m1[1] * m2[0]};
+      const double jw = std::sqrt(n3[0] * n3[0] + n3[1] * n3[1] + n3[2] * n3[2]);
+      for (int i = 0; i < 4; ++i)
+        for (int d = 0; d < 3; ++d) f[nodes[i] * 3 + d] += jw * t3[k * 3 + d] * Na[i];
+    }
+  }
+  return TG_OK;
+}
+
+int tg_form_residual(tg_context* c, double* R_out, double* norm_out) {
+  if (!c || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int s = launch_residual(c);
+  if (s) return s;
+  if (!ok(c, cudaMemcpyAsync(c->h_resid, c->d_resid, sizeof(ResidScalars), cudaMemcpyDeviceToHost, c->stream), "norm"))
+    return TG_ERR_CUDA;
+  double* d_eq = nullptr;
+  if (R_out && c->neq > 0) {
+    if (!ok(c, cudaMallocAsync((void**)&d_eq, sizeof(double) * c->neq, c->stream), "alloc")) return TG_ERR_OOM;
+    s = launch_gather_eq(c, c->d_R, d_eq);
+    if (!s && !ok(c, cudaMemcpyAsync(R_out, d_eq, sizeof(double) * c->neq, cudaMemcpyDeviceToHost, c->stream), "R"))
+      s = TG_ERR_CUDA;
+    cudaFreeAsync(d_eq, c->stream);
+    if (s) return s;
+  }
+  s = sync_status(c);
+  if (s) return s;
+  const double n2 = c->h_resid->norm2;
+  if (!std::isfinite(n2)) {
+    c->err = "non-finite residual";
+    return TG_ERR_NAN;
+  }
+  if (norm_out) *norm_out = std::sqrt(n2);
+  return TG_OK;
+}
+
+int tg_form_tangent(tg_context* c, int precision) {
+  if (!c || c->nnd <= 0 || (precision != TG_FP64 && precision != TG_MIXED)) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  return form_tangent(c, precision);
+}
+
+}  // extern "C"

@@ -1,0 +1,197 @@
+// Deterministic, atomic-free global assembly on sm_103a.
+//
+// The global tangent is CSR over 3x3 node blocks (rows = nodes), values kept
+// as nine structure-of-arrays planes vals[k*stride + blk] so a warp reading
+// consecutive blocks of a row issues unit-stride loads.  Every block gathers
+// its element contributions through the destination-sorted map built on the
+// host (ascending element order), so the sum order is fixed and the result is
+// bitwise repeatable.  Rows of prescribed dofs are zeroed; restricted to the
+// active rows and columns the values are the reference's "active equations
+// only" assembly (MSRMatrixT::Assemble, MSRMatrixT.cpp:96-143).  The diagonal block's (block-)Jacobi inverse is
+// produced in the same pass (DiagonalMatrixT, DiagonalMatrixT.cpp:91,313):
+// minv[0 .. 9*nnd) holds the Jacobi inverse, minv[9*nnd .. 18*nnd) the 3x3
+// block-Jacobi inverse, so the solve can pick either.
+#include "tg_internal.h"
+
+namespace tg {
+
+namespace {
+
+__device__ __forceinline__ int upper_slot(int a, int b) { return a * 8 - a * (a - 1) / 2 + (b - a); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ col,
+                                                       const int* __restrict__ cptr,
+                                                       const int* __restrict__ contrib, const T* __restrict__ Ke,
+                                                       const uint8_t* __restrict__ mask, T* __restrict__ vals,
+                                                       long long stride, T* __restrict__ minv) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nnd; I += warps) {
+    const uint8_t mI = mask[I];
+    const int r0 = rowptr[I], r1 = rowptr[I + 1];
+    for (int j = r0 + lane; j < r1; j += 32) {
+      T acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] = T(0);
+      const int c1 = cptr[j + 1];
+      for (int c = cptr[j]; c < c1; ++c) {
+        const int code = contrib[c];
+        const int e = code >> 6, a = (code >> 3) & 7, b = code & 7;
+        if (a <= b) {
+          const T* src = Ke + ((long long)e * kSlots + upper_slot(a, b)) * kKeBlock;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) acc[k] += src[k];
+        } else {
+          const T* src = Ke + ((long long)e * kSlots + upper_slot(b, a)) * kKeBlock;
+#pragma unroll
+          for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) acc[p * 3 + q] += src[q * 3 + p];
+        }
+      }
+      const int J = col[j];
+      // rows of prescribed dofs are zeroed; columns are kept so that a
+      // product with a prescribed-increment vector gives the coupling
+      // K_fp du_p (PCG vectors are zero at prescribed dofs, so the kept
+      // columns never enter the solve)
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+        if (!((mI >> p) & 1))
+#pragma unroll
+          for (int q = 0; q < 3; ++q) acc[p * 3 + q] = T(0);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) vals[k * stride + j] = acc[k];
+      if (J == I) {
+        // (block-)Jacobi inverse of the diagonal block; inactive dofs get
+        // identity in the inverse's input and zero in its output.
+        T A[9];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            A[p * 3 + q] = (((mI >> p) & 1) && ((mI >> q) & 1)) ? acc[p * 3 + q] : (p == q ? T(1) : T(0));
+        // Jacobi: inverse diagonal; block-Jacobi: inverse of the 3x3 block
+        T B[9], Dg[9];
+        const T d = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                    A[2] * (A[3] * A[7] - A[4] * A[6]);
+        const T id = T(1) / d;
+        B[0] = (A[4] * A[8] - A[5] * A[7]) * id;
+        B[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+        B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+        B[3] = (A[5] * A[6] - A[3] * A[8]) * id;
+        B[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+        B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+        B[6] = (A[3] * A[7] - A[4] * A[6]) * id;
+        B[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+        B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Dg[k] = T(0);
+        Dg[0] = T(1) / A[0];
+        Dg[4] = T(1) / A[4];
+        Dg[8] = T(1) / A[8];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            if (!((mI >> p) & 1) || !((mI >> q) & 1)) {
+              B[p * 3 + q] = T(0);
+              Dg[p * 3 + q] = T(0);
+            }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          minv[(long long)I * 9 + k] = Dg[k];
+          minv[((long long)nnd + I) * 9 + k] = B[k];
+        }
+      }
+    }
+  }
+}
+
+__global__ void set_prescribed_kernel(int n, const int* __restrict__ idx, const double* __restrict__ val,
+                                      double4_32a* __restrict__ u) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int node = idx[k] / 3, d = idx[k] % 3;
+  double* p = reinterpret_cast<double*>(u + node);
+  p[d] = val[k];
+}
+
+template <typename V>
+__global__ void apply_update_kernel(int nnd, const V* __restrict__ du, double4_32a* __restrict__ u) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnd) return;
+  const V d = du[n];
+  double4_32a x = u[n];
+  x.x += (double)d.x;
+  x.y += (double)d.y;
+  x.z += (double)d.z;
+  u[n] = x;
+}
+
+__global__ void gather_eq_kernel(int neq, const int* __restrict__ slot, const double4_32a* __restrict__ nodal,
+                                 double* __restrict__ eq) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= neq) return;
+  const int s = slot[k];
+  eq[k] = reinterpret_cast<const double*>(nodal)[s];
+}
+
+__global__ void scatter_eq_kernel(int neq, const int* __restrict__ slot, const double* __restrict__ eq,
+                                  double4_32a* __restrict__ nodal) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= neq) return;
+  reinterpret_cast<double*>(nodal)[slot[k]] = eq[k];
+}
+
+}  // namespace
+
+int launch_assemble(Context* c, int precision) {
+  const int warps_per_block = 8;
+  int grid = (c->nnd + warps_per_block - 1) / warps_per_block;
+  grid = std::min(grid, kNumSMs * 16);
+  if (precision == TG_MIXED)
+    assemble_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_contrib_ptr,
+                                                        c->d_contrib, c->d_Ke32, c->d_mask, c->d_vals32,
+                                                        c->nnzb_pad, c->d_minv32);
+  else
+    assemble_kernel<double><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_contrib_ptr,
+                                                         c->d_contrib, c->d_Ke64, c->d_mask, c->d_vals64,
+                                                         c->nnzb_pad, c->d_minv64);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "assemble_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_set_prescribed(Context* c, int n, const int* d_idx, const double* d_val) {
+  if (n <= 0) return TG_OK;
+  set_prescribed_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(n, d_idx, d_val, c->d_u);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "set_prescribed_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_apply_update(Context* c) {
+  const int grid = (c->nnd + 255) / 256;
+  if (c->pcg_vec_precision == TG_MIXED)
+    apply_update_kernel<float4><<<grid, 256, 0, c->stream>>>(c->nnd, (const float4*)c->d_x, c->d_u);
+  else
+    apply_update_kernel<double4_32a><<<grid, 256, 0, c->stream>>>(c->nnd, (const double4_32a*)c->d_x, c->d_u);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "apply_update_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_gather_eq(Context* c, const double4_32a* d_nodal, double* d_eq) {
+  if (c->neq == 0) return TG_OK;
+  gather_eq_kernel<<<(c->neq + 255) / 256, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, d_nodal, d_eq);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "gather_eq_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_scatter_eq(Context* c, const double* d_eq, double4_32a* d_nodal) {
+  if (c->neq == 0) return TG_OK;
+  scatter_eq_kernel<<<(c->neq + 255) / 256, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, d_eq, d_nodal);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "scatter_eq_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+}  // namespace tg

@@ -1,0 +1,776 @@
+// Element group kernels of the hex8 implicit path on sm_103a.
+//
+//  * residual_kernel  (FP64): one thread per Gauss point, 8 lanes per element.
+//    Kinematics, material stress (with J2 return mapping and history writes)
+//    and the element internal force, reduced over the 8 points with an
+//    in-register shuffle reduce-scatter so lane a ends with node a's force.
+//    SmallStrainT::FormKd (SmallStrainT.cpp:255), TotalLagrangianT::FormKd
+//    (TotalLagrangianT.cpp:107).
+//  * gather_residual_kernel: R = factor*Fext - sum of element forces per node,
+//    in the fixed node->element incidence order (no atomics), fused with the
+//    FP64 norm (SolverT::Residual, SolverT.cpp:848).
+//  * tangent_kernel<T>: 8 elements per CTA.  64 threads stage per-point
+//    gradients, moduli and stress in shared memory; then one thread per
+//    upper node-pair block (36 per element) integrates its 3x3 block of
+//    B^T c B (+ geometric stiffness for TL) over the 8 points.
+//    SmallStrainT::FormStiffness (SmallStrainT.cpp:285), TotalLagrangianT::
+//    FormStiffness (TotalLagrangianT.cpp:40), Set_B (SolidElementT.cpp:854).
+//
+// Conventions: Voigt [11,22,33,23,13,12]; strain vectors hold tensor shear,
+// 6x6 moduli act on engineering shear.  Hex8 node/Gauss-point order of
+// HexahedronT.cpp:23-25,1540-1548.
+#include <cmath>
+
+#include "tg_internal.h"
+
+namespace tg {
+
+namespace {
+
+constexpr double kSqrt23 = 0.81649658092772603273;  // sqrt(2/3)
+constexpr double kYieldTol = 1.0e-10;                // J2SSC0HardeningT.cpp:17
+constexpr double kGauss = 0.57735026918962576451;    // 1/sqrt(3)
+
+// node sign patterns of HexahedronT.cpp:23-25
+__host__ __device__ constexpr double sr(int a) { return (((a + 1) >> 1) & 1) ? 1.0 : -1.0; }
+__host__ __device__ constexpr double ss(int a) { return ((a >> 1) & 1) ? 1.0 : -1.0; }
+__host__ __device__ constexpr double st(int a) { return ((a >> 2) & 1) ? 1.0 : -1.0; }
+
+// reference-domain derivatives of N_a at Gauss point ip (ParentDomainT)
+template <typename T>
+__device__ __forceinline__ void ref_grad(int ip, T dN[3][8]) {
+  const T r = T(kGauss) * T(sr(ip)), s = T(kGauss) * T(ss(ip)), t = T(kGauss) * T(st(ip));
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const T fr = T(1) + r * T(sr(a)), fs = T(1) + s * T(ss(a)), ft = T(1) + t * T(st(a));
+    dN[0][a] = T(0.125) * T(sr(a)) * fs * ft;
+    dN[1][a] = T(0.125) * T(ss(a)) * fr * ft;
+    dN[2][a] = T(0.125) * T(st(a)) * fr * fs;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T det3(const T A[9]) {
+  return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+         A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+template <typename T>
+__device__ __forceinline__ void inv3(const T A[9], T d, T B[9]) {
+  const T id = T(1) / d;
+  B[0] = (A[4] * A[8] - A[5] * A[7]) * id;
+  B[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  B[3] = (A[5] * A[6] - A[3] * A[8]) * id;
+  B[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  B[6] = (A[3] * A[7] - A[4] * A[6]) * id;
+  B[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
+// Jacobian, det and spatial gradients g[l][a] = dN_a/dX_l at one point
+// (ParentDomainT::ComputeDNa, ParentDomainT.cpp:426-470).
+template <typename T>
+__device__ __forceinline__ T point_gradients(const T (*Xe)[3], int ip, T g[3][8]) {
+  T dN[3][8];
+  ref_grad<T>(ip, dN);
+  T J[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      T acc = T(0);
+#pragma unroll
+      for (int a = 0; a < 8; ++a) acc += Xe[a][i] * dN[k][a];
+      J[i * 3 + k] = acc;
+    }
+  const T d = det3(J);
+  T Ji[9];
+  inv3(J, d, Ji);
+#pragma unroll
+  for (int l = 0; l < 3; ++l)
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+      g[l][a] = Ji[0 * 3 + l] * dN[0][a] + Ji[1 * 3 + l] * dN[1][a] + Ji[2 * 3 + l] * dN[2][a];
+  return d;
+}
+
+template <typename T>
+__device__ __forceinline__ void hooke(const double* C, const T e[6], T s[6]) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    s[i] = T(C[i * 6 + 0]) * e[0] + T(C[i * 6 + 1]) * e[1] + T(C[i * 6 + 2]) * e[2] +
+           T(2) * (T(C[i * 6 + 3]) * e[3] + T(C[i * 6 + 4]) * e[4] + T(C[i * 6 + 5]) * e[5]);
+}
+template <typename T>
+__device__ __forceinline__ T sym_dot(const T a[6], const T b[6]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + T(2) * (a[3] * b[3] + a[4] * b[4] + a[5] * b[5]);
+}
+template <typename T>
+__device__ __forceinline__ void deviatoric(const T a[6], T d[6]) {
+  const T m = (a[0] + a[1] + a[2]) / T(3);
+  d[0] = a[0] - m;
+  d[1] = a[1] - m;
+  d[2] = a[2] - m;
+  d[3] = a[3];
+  d[4] = a[4];
+  d[5] = a[5];
+}
+
+// SimoIso3D Cauchy stress and spatial moduli (SimoIso3D.cpp:16-53,102-135;
+// U(J) = kappa/2 (1/2 (J^2-1) - ln J), SimoIso3D.h:88-101).
+template <typename T>
+__device__ __forceinline__ bool simo(const MatParams& m, const T F[9], T s[6], T* D) {
+  T b[6];
+  b[0] = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+  b[1] = F[3] * F[3] + F[4] * F[4] + F[5] * F[5];
+  b[2] = F[6] * F[6] + F[7] * F[7] + F[8] * F[8];
+  b[3] = F[3] * F[6] + F[4] * F[7] + F[5] * F[8];
+  b[4] = F[0] * F[6] + F[1] * F[7] + F[2] * F[8];
+  b[5] = F[0] * F[3] + F[1] * F[4] + F[2] * F[5];
+  const T detb = b[0] * (b[1] * b[2] - b[3] * b[3]) - b[5] * (b[5] * b[2] - b[3] * b[4]) +
+                 b[4] * (b[5] * b[3] - b[1] * b[4]);
+  if (!(detb > T(0))) return false;
+  const T J = sqrt(detb);
+  const T sc = pow(J, T(-2.0 / 3.0));
+  T bb[6], dev[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) bb[k] = sc * b[k];
+  deviatoric(bb, dev);
+  const T mu = T(m.mu), kappa = T(m.kappa);
+  const T dU = T(0.5) * kappa * (J - T(1) / J);
+  const T ddU = T(0.5) * kappa * (T(1) + T(1) / (J * J));
+#pragma unroll
+  for (int k = 0; k < 6; ++k) s[k] = mu / J * dev[k];
+  s[0] += dU;
+  s[1] += dU;
+  s[2] += dU;
+  if (D) {
+    const T mubar = mu * (bb[0] + bb[1] + bb[2]) / (J * T(3));
+    const T c1 = dU + J * ddU;
+    const T c4 = T(-4) / (J * T(3)) * T(0.5) * mu;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        T v = T(0);
+        if (i < 3 && j < 3) v += c1 + T(2) * mubar * (i == j ? T(2.0 / 3.0) : T(-1.0 / 3.0));
+        if (i == j) v += T(-2) * dU * (i < 3 ? T(1) : T(0.5)) + (i >= 3 ? T(2) * mubar * T(0.5) : T(0));
+        const T Ii = i < 3 ? T(1) : T(0), Ij = j < 3 ? T(1) : T(0);
+        v += c4 * (dev[i] * Ij + Ii * dev[j]);
+        D[i * 6 + j] = v;
+      }
+  }
+  return true;
+}
+
+__host__ __device__ constexpr int vgt(int i, int j) {
+  return i == j ? i : ((i + j) == 1 ? 5 : ((i + j) == 2 ? 4 : 3));
+}
+
+// large_strain_StVenant: S = C:E, sigma = F S F^T / J, c = push-forward(C)/J
+// (FDHookeanMatT.cpp s_ij/c_ijkl with FDKStV isotropic C).
+template <typename T>
+__device__ __forceinline__ bool stvenant(const MatParams& m, const T F[9], T s[6], T* D) {
+  T Cg[9];
+#pragma unroll
+  for (int I = 0; I < 3; ++I)
+#pragma unroll
+    for (int J = 0; J < 3; ++J) Cg[I * 3 + J] = F[I] * F[J] + F[3 + I] * F[3 + J] + F[6 + I] * F[6 + J];
+  T E[6] = {T(0.5) * (Cg[0] - T(1)), T(0.5) * (Cg[4] - T(1)), T(0.5) * (Cg[8] - T(1)),
+            T(0.5) * Cg[5],          T(0.5) * Cg[2],          T(0.5) * Cg[1]};
+  T S6[6];
+  hooke<T>(m.C, E, S6);
+  const T S[9] = {S6[0], S6[5], S6[4], S6[5], S6[1], S6[3], S6[4], S6[3], S6[2]};
+  const T J = det3(F);
+  if (!(J > T(0))) return false;
+  T FS[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int K = 0; K < 3; ++K) FS[i * 3 + K] = F[i * 3 + 0] * S[0 * 3 + K] + F[i * 3 + 1] * S[1 * 3 + K] + F[i * 3 + 2] * S[2 * 3 + K];
+  T sig[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      sig[i * 3 + j] = (FS[i * 3 + 0] * F[j * 3 + 0] + FS[i * 3 + 1] * F[j * 3 + 1] + FS[i * 3 + 2] * F[j * 3 + 2]) / J;
+  s[0] = sig[0]; s[1] = sig[4]; s[2] = sig[8]; s[3] = sig[5]; s[4] = sig[2]; s[5] = sig[1];
+  if (D) {
+    const int pi[6] = {0, 1, 2, 1, 0, 0}, pj[6] = {0, 1, 2, 2, 2, 1};
+    for (int A = 0; A < 6; ++A)
+      for (int B = A; B < 6; ++B) {
+        const int i = pi[A], j = pj[A], k = pi[B], l = pj[B];
+        T acc = T(0);
+        for (int I = 0; I < 3; ++I)
+          for (int JJ = 0; JJ < 3; ++JJ) {
+            const T fij = F[i * 3 + I] * F[j * 3 + JJ];
+            for (int K = 0; K < 3; ++K)
+              for (int L = 0; L < 3; ++L)
+                acc += fij * F[k * 3 + K] * F[l * 3 + L] * T(m.C[vgt(I, JJ) * 6 + vgt(K, L)]);
+          }
+        D[A * 6 + B] = acc / J;
+        D[B * 6 + A] = acc / J;
+      }
+  }
+  return true;
+}
+
+// J2 consistent moduli C + ModuliCorrection (J2SSC0HardeningT.cpp:148-176)
+template <typename T>
+__device__ __forceinline__ void j2_moduli(const MatParams& m, bool plastic, double dgamma, double norm,
+                                          const T nh[6], T D[36]) {
+#pragma unroll
+  for (int k = 0; k < 36; ++k) D[k] = T(m.C[k]);
+  if (plastic) {
+    const T mu = T(m.mu);
+    const T th = T(2.0 * m.mu * dgamma / norm);
+    const T tb = T(3.0 / (3.0 + m.hard_a / m.mu)) - th;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) D[i * 6 + j] += T(-2) * mu * th * (i == j ? T(2.0 / 3.0) : T(-1.0 / 3.0));
+#pragma unroll
+    for (int i = 3; i < 6; ++i) D[i * 6 + i] += T(-2) * mu * th * T(0.5);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) D[i * 6 + j] += T(-2) * mu * tb * nh[i] * nh[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// residual
+// ---------------------------------------------------------------------------
+constexpr int kResElems = 32;  // elements per CTA (256 threads)
+
+struct J2View {
+  int8_t* flags;
+  int8_t* alloc;
+  double* alpha;
+  double* dgamma;
+  double* norm;
+  double* epsp;
+  double* nhat;
+  long long nip;
+};
+
+__global__ void __launch_bounds__(256) residual_kernel(const double* __restrict__ X, int nnd,
+                                                       const int* __restrict__ conn, const int8_t* __restrict__ blk,
+                                                       int nel, const double4_32a* __restrict__ u, MatTable mt,
+                                                       J2View j2, int iteration, int commit_state,
+                                                       double4_32a* __restrict__ fint, int* status) {
+  __shared__ double sX[kResElems][8][3];
+  __shared__ double sU[kResElems][8][3];
+  const int tid = threadIdx.x;
+  const int le = tid >> 3, ip = tid & 7;
+  const int e = blockIdx.x * kResElems + le;
+  const bool valid = e < nel;
+  if (valid) {
+    const int n = conn[e * 8 + ip];
+    sX[le][ip][0] = X[n];
+    sX[le][ip][1] = X[nnd + n];
+    sX[le][ip][2] = X[2 * nnd + n];
+    const double4_32a un = u[n];
+    sU[le][ip][0] = un.x;
+    sU[le][ip][1] = un.y;
+    sU[le][ip][2] = un.z;
+  }
+  __syncthreads();
+
+  double f[8][3];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) f[a][0] = f[a][1] = f[a][2] = 0.0;
+  bool bad = false;
+  const int bi = (valid && blk) ? blk[e] : 0;
+  const MatParams& m = mt.m[bi];
+  // J2 element-level "allocation" vote must be warp-uniform: evaluate the
+  // yield predicate for every lane (invalid lanes vote false).
+  bool yield_vote = false;
+  double eps[6] = {0, 0, 0, 0, 0, 0};
+  double g[3][8];
+  double wdet = 0.0;
+  if (valid) {
+    wdet = point_gradients<double>(sX[le], ip, g);  // weight 1 (HexahedronT.cpp:1545)
+    if (!(wdet > 0.0)) bad = true;
+  }
+  const bool is_j2 = valid && m.kind == TG_MAT_SS_J2;
+  bool j2_alloc = false;
+  double rel[6] = {0, 0, 0, 0, 0, 0};
+  double ftr = 0.0, nr = 0.0;
+  const long long gid = (long long)e * 8 + ip;
+  if (valid && !bad && mt.formulation == TG_SMALL_STRAIN) {
+    double H[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double acc = 0.0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) acc += sU[le][a][i] * g[j][a];
+        H[i * 3 + j] = acc;
+      }
+    eps[0] = H[0];
+    eps[1] = H[4];
+    eps[2] = H[8];
+    eps[3] = 0.5 * (H[5] + H[7]);
+    eps[4] = 0.5 * (H[2] + H[6]);
+    eps[5] = 0.5 * (H[1] + H[3]);
+    if (is_j2) {
+      j2_alloc = j2.alloc[e] != 0;
+      if (j2_alloc)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) eps[k] -= j2.epsp[k * j2.nip + gid];
+      if (iteration > m.elastic_its - 2) {
+        double dev[6];
+        deviatoric(eps, dev);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) rel[k] = 2.0 * m.mu * dev[k];
+        nr = sqrt(sym_dot(rel, rel));
+        const double alpha = j2_alloc ? j2.alpha[gid] : 0.0;
+        ftr = nr - kSqrt23 * (m.hard_a * alpha + m.hard_b);
+        yield_vote = ftr > kYieldTol;
+      }
+    }
+  }
+  // element-wide OR over the 8 lanes of this element
+  const unsigned ballot = __ballot_sync(0xffffffffu, yield_vote);
+  const unsigned group = (ballot >> ((threadIdx.x & 31) & ~7)) & 0xffu;
+
+  if (valid && !bad) {
+    double s[6];
+    if (mt.formulation == TG_SMALL_STRAIN) {
+      hooke<double>(m.C, eps, s);  // eps holds the elastic strain here
+      if (is_j2 && iteration > m.elastic_its - 2) {
+        // J2SSC0HardeningT::StressCorrection (:68-145) + PlasticLoading (:302-346)
+        const bool now_alloc = j2_alloc || group != 0u;
+        if (now_alloc) {
+          const bool plastic = ftr > kYieldTol;
+          double dg = 0.0;
+          if (plastic) {
+            dg = 0.5 * ftr / (m.mu + m.hard_a / 3.0);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s[k] += -2.0 * m.mu * dg * (rel[k] / nr);
+          }
+          if (commit_state) {
+            j2.flags[gid] = plastic ? (int8_t)TG_J2_PLASTIC : (int8_t)TG_J2_ELASTIC;
+            j2.dgamma[gid] = dg;
+            if (plastic) {
+              j2.norm[gid] = nr;
+#pragma unroll
+              for (int k = 0; k < 6; ++k) j2.nhat[k * j2.nip + gid] = rel[k] / nr;
+            }
+            if (!j2_alloc && ip == 0) j2.alloc[e] = 1;
+          }
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        f[a][0] = wdet * (g[0][a] * s[0] + g[2][a] * s[4] + g[1][a] * s[5]);
+        f[a][1] = wdet * (g[1][a] * s[1] + g[2][a] * s[3] + g[0][a] * s[5]);
+        f[a][2] = wdet * (g[2][a] * s[2] + g[1][a] * s[3] + g[0][a] * s[4]);
+      }
+    } else {
+      double F[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double acc = (i == j) ? 1.0 : 0.0;
+#pragma unroll
+          for (int a = 0; a < 8; ++a) acc += sU[le][a][i] * g[j][a];
+          F[i * 3 + j] = acc;
+        }
+      const double J = det3(F);
+      bool okm = J > 0.0;
+      if (okm) okm = (m.kind == TG_MAT_FS_SIMO) ? simo<double>(m, F, s, nullptr) : stvenant<double>(m, F, s, nullptr);
+      if (!okm) {
+        bad = true;
+      } else {
+        double Fi[9];
+        inv3(F, J, Fi);
+        const double scale = wdet * J;
+        // P/J = sigma F^-T; f_a,i = scale * sigma_ij dN_a/dx_j
+        const double sm[9] = {s[0], s[5], s[4], s[5], s[1], s[3], s[4], s[3], s[2]};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          double gx[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) gx[k] = g[0][a] * Fi[0 * 3 + k] + g[1][a] * Fi[1 * 3 + k] + g[2][a] * Fi[2 * 3 + k];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) f[a][i] = scale * (sm[i * 3 + 0] * gx[0] + sm[i * 3 + 1] * gx[1] + sm[i * 3 + 2] * gx[2]);
+        }
+      }
+    }
+  }
+  if (bad) {
+    atomicOr(status, kStatusBadJacobian);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) f[a][0] = f[a][1] = f[a][2] = 0.0;
+  }
+
+  // reduce-scatter over the 8 points of the element: lane ip ends with node ip
+  double h[4][3];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double keep = (ip & 4) ? f[4 + j][i] : f[j][i];
+      const double send = (ip & 4) ? f[j][i] : f[4 + j][i];
+      h[j][i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+  double q[2][3];
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double keep = (ip & 2) ? h[2 + j][i] : h[j][i];
+      const double send = (ip & 2) ? h[j][i] : h[2 + j][i];
+      q[j][i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+  double r[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double keep = (ip & 1) ? q[1][i] : q[0][i];
+    const double send = (ip & 1) ? q[0][i] : q[1][i];
+    r[i] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+  }
+  if (valid) fint[(long long)e * 8 + ip] = make_double4_32a(r[0], r[1], r[2], 0.0);
+}
+
+// R[node] = factor*Fext - sum_k fint[k] over incident (e,a), active dofs only;
+// partial sums of R.R reduced with a last-block-done pass (fixed order).
+__global__ void __launch_bounds__(256) gather_residual_kernel(
+    int nnd, const int* __restrict__ nptr, const int* __restrict__ nlist, const double4_32a* __restrict__ fint,
+    const double4_32a* __restrict__ fext, double factor, const uint8_t* __restrict__ mask, double4_32a* __restrict__ R,
+    double* partials, ResidScalars* sc) {
+  double local = 0.0;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gridDim.x * blockDim.x) {
+    const double4_32a fe = fext[n];
+    double rx = factor * fe.x, ry = factor * fe.y, rz = factor * fe.z;
+    for (int k = nptr[n]; k < nptr[n + 1]; ++k) {
+      const double4_32a v = fint[nlist[k]];
+      rx -= v.x;
+      ry -= v.y;
+      rz -= v.z;
+    }
+    const uint8_t mk = mask[n];
+    rx = (mk & 1) ? rx : 0.0;
+    ry = (mk & 2) ? ry : 0.0;
+    rz = (mk & 4) ? rz : 0.0;
+    R[n] = make_double4_32a(rx, ry, rz, 0.0);
+    local += rx * rx + ry * ry + rz * rz;
+  }
+  // block reduction (fixed tree)
+  __shared__ double red[256];
+  red[threadIdx.x] = local;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = red[0];
+    __threadfence();
+    const unsigned prev = atomicAdd(&sc->count, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) acc += ((volatile double*)partials)[b];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      sc->norm2 = red[0];
+      sc->count = 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tangent
+// ---------------------------------------------------------------------------
+constexpr int kTanElems = 8;                   // elements per CTA
+constexpr int kTanThreads = kTanElems * kSlots;  // 288
+
+__device__ __forceinline__ void slot_pair(int slot, int& a, int& b) {
+  int start = 0;
+  a = 0;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int len = 8 - r;
+    if (slot >= start && slot < start + len) {
+      a = r;
+      b = r + (slot - start);
+    }
+    start += len;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTanThreads) tangent_kernel(const double* __restrict__ X, int nnd,
+                                                              const int* __restrict__ conn,
+                                                              const int8_t* __restrict__ blk, int nel,
+                                                              const double4_32a* __restrict__ u, MatTable mt,
+                                                              J2View j2, T* __restrict__ Ke, int* status) {
+  __shared__ T sX[kTanElems][8][3];
+  __shared__ T sU[kTanElems][8][3];
+  __shared__ T sG[kTanElems][8][3][8];  // per point spatial gradients
+  __shared__ T sD[kTanElems][8][36];    // per point moduli (scaled)
+  __shared__ T sS[kTanElems][8][6];     // per point Cauchy stress (scaled, TL only)
+  const int tid = threadIdx.x;
+  const int e0 = blockIdx.x * kTanElems;
+
+  if (tid < kTanElems * 8) {
+    const int le = tid >> 3, a = tid & 7;
+    const int e = e0 + le;
+    if (e < nel) {
+      const int n0 = conn[e * 8];
+      const int n = conn[e * 8 + a];
+      // local origin at node 0 keeps FP32 coordinate differences accurate
+      sX[le][a][0] = T(X[n] - X[n0]);
+      sX[le][a][1] = T(X[nnd + n] - X[nnd + n0]);
+      sX[le][a][2] = T(X[2 * nnd + n] - X[2 * nnd + n0]);
+      const double4_32a un = u[n];
+      sU[le][a][0] = T(un.x);
+      sU[le][a][1] = T(un.y);
+      sU[le][a][2] = T(un.z);
+    }
+  }
+  __syncthreads();
+  if (tid < kTanElems * 8) {
+    const int le = tid >> 3, ip = tid & 7;
+    const int e = e0 + le;
+    if (e < nel) {
+      const MatParams& m = mt.m[blk ? blk[e] : 0];
+      T g[3][8];
+      const T detj = point_gradients<T>(sX[le], ip, g);
+      T D[36];
+      T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+      T scale = detj;
+      bool okm = detj > T(0);
+      if (mt.formulation == TG_SMALL_STRAIN) {
+        if (m.kind == TG_MAT_SS_J2) {
+          const long long gid = (long long)e * 8 + ip;
+          const bool plastic = j2.alloc[e] != 0 && j2.flags[gid] == TG_J2_PLASTIC;
+          T nh[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) nh[k] = plastic ? T(j2.nhat[k * j2.nip + gid]) : T(0);
+          j2_moduli<T>(m, plastic, plastic ? j2.dgamma[gid] : 0.0, plastic ? j2.norm[gid] : 1.0, nh, D);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 36; ++k) D[k] = T(m.C[k]);
+        }
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+#pragma unroll
+          for (int a = 0; a < 8; ++a) sG[le][ip][l][a] = g[l][a];
+      } else {
+        T F[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            T acc = (i == j) ? T(1) : T(0);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) acc += sU[le][a][i] * g[j][a];
+            F[i * 3 + j] = acc;
+          }
+        const T J = det3(F);
+        okm = okm && J > T(0);
+        if (okm) okm = (m.kind == TG_MAT_FS_SIMO) ? simo<T>(m, F, s, D) : stvenant<T>(m, F, s, D);
+        if (okm) {
+          T Fi[9];
+          inv3(F, J, Fi);
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+              sG[le][ip][k][a] = g[0][a] * Fi[0 * 3 + k] + g[1][a] * Fi[1 * 3 + k] + g[2][a] * Fi[2 * 3 + k];
+          scale = detj * J;
+        }
+      }
+      if (!okm) {
+        atomicOr(status, kStatusBadJacobian);
+        scale = T(0);
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+#pragma unroll
+          for (int a = 0; a < 8; ++a) sG[le][ip][l][a] = T(0);
+#pragma unroll
+        for (int k = 0; k < 36; ++k) D[k] = T(0);
+      }
+#pragma unroll
+      for (int k = 0; k < 36; ++k) sD[le][ip][k] = scale * D[k];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) sS[le][ip][k] = scale * s[k];
+    }
+  }
+  __syncthreads();
+
+  const int le = tid / kSlots, slot = tid - le * kSlots;
+  const int e = e0 + le;
+  if (e >= nel) return;
+  int a, b;
+  slot_pair(slot, a, b);
+  const bool tl = mt.formulation == TG_TOTAL_LAGRANGIAN;
+  T K[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) K[k] = T(0);
+  for (int ip = 0; ip < 8; ++ip) {
+    const T ga[3] = {sG[le][ip][0][a], sG[le][ip][1][a], sG[le][ip][2][a]};
+    const T gb[3] = {sG[le][ip][0][b], sG[le][ip][1][b], sG[le][ip][2][b]};
+    const T* D = sD[le][ip];
+    // h[V][j] = sum_n D[V][vgt(j,n)] gb[n];  K(i,j) += sum_m ga[m] h[vgt(i,m)][j]
+    T h[6][3];
+#pragma unroll
+    for (int V = 0; V < 6; ++V)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        h[V][j] = D[V * 6 + vgt(j, 0)] * gb[0] + D[V * 6 + vgt(j, 1)] * gb[1] + D[V * 6 + vgt(j, 2)] * gb[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        K[i * 3 + j] += ga[0] * h[vgt(i, 0)][j] + ga[1] * h[vgt(i, 1)][j] + ga[2] * h[vgt(i, 2)][j];
+    if (tl) {
+      const T* s = sS[le][ip];
+      const T sg0 = s[0] * gb[0] + s[5] * gb[1] + s[4] * gb[2];
+      const T sg1 = s[5] * gb[0] + s[1] * gb[1] + s[3] * gb[2];
+      const T sg2 = s[4] * gb[0] + s[3] * gb[1] + s[2] * gb[2];
+      const T geo = ga[0] * sg0 + ga[1] * sg1 + ga[2] * sg2;
+      K[0] += geo;
+      K[4] += geo;
+      K[8] += geo;
+    }
+  }
+  T* out = Ke + ((long long)e * kSlots + slot) * kKeBlock;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) out[k] = K[k];
+}
+
+// J2 history update / reset (J2SSC0HardeningT::Update/Reset, :204-250);
+// one thread per element.
+__global__ void j2_close_kernel(int nel, J2View j2, int reset) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel || !j2.alloc[e]) return;
+  const long long base = (long long)e * 8;
+  if (reset) {
+    for (int ip = 0; ip < 8; ++ip) j2.flags[base + ip] = TG_J2_RESET;
+    return;
+  }
+  if (j2.flags[base] == TG_J2_RESET) {
+    for (int ip = 0; ip < 8; ++ip) j2.flags[base + ip] = TG_J2_ELASTIC;
+    return;
+  }
+  for (int ip = 0; ip < 8; ++ip) {
+    const long long gid = base + ip;
+    if (j2.flags[gid] == TG_J2_PLASTIC) {
+      j2.flags[gid] = TG_J2_RESET;
+      const double dg = j2.dgamma[gid];
+      j2.alpha[gid] += kSqrt23 * dg;
+      for (int k = 0; k < 6; ++k) j2.epsp[k * j2.nip + gid] += dg * j2.nhat[k * j2.nip + gid];
+    }
+  }
+}
+
+J2View j2view(Context* c) {
+  J2View v;
+  v.flags = c->d_j2_flags;
+  v.alloc = c->d_j2_alloc;
+  v.alpha = c->d_j2_alpha;
+  v.dgamma = c->d_j2_dgamma;
+  v.norm = c->d_j2_norm;
+  v.epsp = c->d_j2_epsp;
+  v.nhat = c->d_j2_nhat;
+  v.nip = (long long)c->nel * 8;
+  return v;
+}
+
+int residual_impl(Context* c, int commit_state) {
+  const int grid = (c->nel + kResElems - 1) / kResElems;
+  residual_kernel<<<grid, 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats,
+                                               j2view(c), c->iteration, commit_state, c->d_fint, c->d_status);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "residual_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+}  // namespace
+
+int launch_residual_commit(Context* c, int commit);
+int launch_residual(Context* c) { return launch_residual_commit(c, 1); }
+int launch_residual_nocommit(Context* c) { return launch_residual_commit(c, 0); }
+
+int launch_residual_commit(Context* c, int commit) {
+  int s = residual_impl(c, commit);
+  if (s) return s;
+  const int grid = std::min((c->nnd + 255) / 256, c->partials_cap);
+  gather_residual_kernel<<<grid, 256, 0, c->stream>>>(c->nnd, c->d_node_elem_ptr, c->d_node_elem, c->d_fint,
+                                                      c->d_fext, c->load_factor, c->d_mask, c->d_R, c->d_partials,
+                                                      c->d_resid);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "gather_residual_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_tangent(Context* c, int precision) {
+  const int grid = (c->nel + kTanElems - 1) / kTanElems;
+  if (precision == TG_MIXED) {
+    tangent_kernel<float><<<grid, kTanThreads, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u,
+                                                               c->mats, j2view(c), c->d_Ke32, c->d_status);
+  } else {
+    tangent_kernel<double><<<grid, kTanThreads, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u,
+                                                                c->mats, j2view(c), c->d_Ke64, c->d_status);
+  }
+  c->launches++;
+  return ok(c, cudaGetLastError(), "tangent_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+// FP64 element matrices (full 24x24) and forces for a range of elements,
+// without committing history (parity dumps).
+namespace {
+__global__ void expand_ke_kernel(int first, int count, const double* __restrict__ Ke, const double4_32a* __restrict__ fint,
+                                 double* __restrict__ outK, double* __restrict__ outF) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const int e = first + k;
+  for (int t = threadIdx.x; t < 576; t += blockDim.x) {
+    const int p = t / 24, q = t % 24;
+    const int a = p / 3, i = p % 3, b = q / 3, j = q % 3;
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    const int slot = lo * 8 - lo * (lo - 1) / 2 + (hi - lo);
+    const double* blkp = Ke + ((long long)e * kSlots + slot) * kKeBlock;
+    outK[(long long)k * 576 + t] = (a <= b) ? blkp[i * 3 + j] : blkp[j * 3 + i];
+  }
+  if (threadIdx.x < 24) {
+    const int a = threadIdx.x / 3, i = threadIdx.x % 3;
+    const double4_32a v = fint[(long long)e * 8 + a];
+    outF[(long long)k * 24 + threadIdx.x] = i == 0 ? v.x : (i == 1 ? v.y : v.z);
+  }
+}
+}  // namespace
+
+int launch_element_dump(Context* c, int first, int count, double* dKe, double* dfint) {
+  int s = residual_impl(c, 0);
+  if (s) return s;
+  s = launch_tangent(c, TG_FP64);
+  if (s) return s;
+  expand_ke_kernel<<<count, 256, 0, c->stream>>>(first, count, c->d_Ke64, c->d_fint, dKe, dfint);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "expand_ke_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_close_step(Context* c, int reset) {
+  if (!c->has_j2) return TG_OK;
+  j2_close_kernel<<<(c->nel + 255) / 256, 256, 0, c->stream>>>(c->nel, j2view(c), reset);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "j2_close_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+}  // namespace tg

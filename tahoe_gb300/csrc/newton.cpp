@@ -1,0 +1,437 @@
+// Tangent formation, Krylov entry points, history management and the Newton
+// driver of the tahoe_gb300 C ABI.  The Newton loop mirrors NLSolver::Solve
+// (tahoe/src/solvers/NLSolver.cpp:57-262) and its exit test
+// NLSolver::ExitIteration (:675-755); all vectors stay on the device and the
+// host reads back one residual norm per iteration plus the PCG flag per
+// graph chunk.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "tg_internal.h"
+
+namespace tg {
+
+int launch_gather_solution(Context* c, double* d_eq);
+
+namespace {
+
+int set_device(Context* c) { return ok(c, cudaSetDevice(c->device), "cudaSetDevice") ? TG_OK : TG_ERR_CUDA; }
+
+int check_status(Context* c) {
+  if (!ok(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "status") ||
+      !ok(c, cudaStreamSynchronize(c->stream), "sync"))
+    return TG_ERR_CUDA;
+  const int st = *c->h_status;
+  if (!st) return TG_OK;
+  cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+  cudaStreamSynchronize(c->stream);
+  if (st & kStatusBadJacobian) {
+    c->err = "non-positive Jacobian determinant";
+    return TG_ERR_BAD_JACOBIAN;
+  }
+  c->err = "non-finite value";
+  return TG_ERR_NAN;
+}
+
+// residual on the device; returns its norm
+int residual_norm(Context* c, double* norm) {
+  int s = launch_residual(c);
+  if (s) return s;
+  if (!ok(c, cudaMemcpyAsync(c->h_resid, c->d_resid, sizeof(ResidScalars), cudaMemcpyDeviceToHost, c->stream), "norm"))
+    return TG_ERR_CUDA;
+  s = check_status(c);
+  if (s) return s;
+  const double n2 = c->h_resid->norm2;
+  if (!std::isfinite(n2)) {
+    c->err = "non-finite residual";
+    return TG_ERR_NAN;
+  }
+  *norm = std::sqrt(n2);
+  return TG_OK;
+}
+
+struct PhaseTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  explicit PhaseTimer(bool on) {
+    if (on) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+    }
+  }
+  ~PhaseTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  void start(cudaStream_t s) {
+    if (a) cudaEventRecord(a, s);
+  }
+  double stop(cudaStream_t s) {
+    if (!a) return 0.0;
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+};
+
+}  // namespace
+
+int form_tangent(Context* c, int precision) {
+  const size_t keN = (size_t)c->nel * kKeStride;
+  if (precision == TG_MIXED) {
+    if (!c->d_Ke32 && !dalloc(c, &c->d_Ke32, keN)) return TG_ERR_OOM;
+    if (!c->d_vals32 && !dalloc(c, &c->d_vals32, (size_t)c->nnzb_pad * 9)) return TG_ERR_OOM;
+    if (!c->d_minv32 && !dalloc(c, &c->d_minv32, (size_t)c->nnd * 18)) return TG_ERR_OOM;
+  } else {
+    if (!c->d_Ke64 && !dalloc(c, &c->d_Ke64, keN)) return TG_ERR_OOM;
+    if (!c->d_vals64 && !dalloc(c, &c->d_vals64, (size_t)c->nnzb_pad * 9)) return TG_ERR_OOM;
+    if (!c->d_minv64 && !dalloc(c, &c->d_minv64, (size_t)c->nnd * 18)) return TG_ERR_OOM;
+  }
+  int s = launch_tangent(c, precision);
+  if (!s) s = launch_assemble(c, precision);
+  if (!s) s = check_status(c);
+  if (!s) c->tangent_precision = precision;
+  return s;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" {
+
+int tg_get_tangent_csr(tg_context* c, int upper_only, double* vals) {
+  if (!c || !vals || c->tangent_precision < 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  const size_t n = (size_t)c->nnzb_pad * 9;
+  std::vector<double> hv(n);
+  if (c->tangent_precision == TG_MIXED) {
+    std::vector<float> hf(n);
+    if (!ok(c, cudaMemcpy(hf.data(), c->d_vals32, sizeof(float) * n, cudaMemcpyDeviceToHost), "vals")) return TG_ERR_CUDA;
+    for (size_t k = 0; k < n; ++k) hv[k] = hf[k];
+  } else if (!ok(c, cudaMemcpy(hv.data(), c->d_vals64, sizeof(double) * n, cudaMemcpyDeviceToHost), "vals")) {
+    return TG_ERR_CUDA;
+  }
+  const int* eq = c->h_eqnos.data();
+  long long count = 0;
+  for (int I = 0; I < c->nnd; ++I)
+    for (int p = 0; p < 3; ++p) {
+      const int r = eq[I * 3 + p];
+      if (r <= 0) continue;
+      for (int k = c->h_rowptr[I]; k < c->h_rowptr[I + 1]; ++k) {
+        const int J = c->h_col[k];
+        for (int q = 0; q < 3; ++q) {
+          const int cc = eq[J * 3 + q];
+          if (cc <= 0 || (upper_only && cc < r)) continue;
+          vals[count++] = hv[(size_t)(p * 3 + q) * c->nnzb_pad + k];
+        }
+      }
+    }
+  return TG_OK;
+}
+
+int tg_element_dump(tg_context* c, int first, int count, double* Ke, double* fint) {
+  if (!c || first < 0 || count <= 0 || first + count > c->nel || !Ke || !fint) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (!c->d_Ke64 && !dalloc(c, &c->d_Ke64, (size_t)c->nel * kKeStride)) return TG_ERR_OOM;
+  double *dK = nullptr, *dF = nullptr;
+  if (!ok(c, cudaMalloc((void**)&dK, sizeof(double) * 576 * count), "alloc") ||
+      !ok(c, cudaMalloc((void**)&dF, sizeof(double) * 24 * count), "alloc")) {
+    cudaFree(dK);
+    return TG_ERR_OOM;
+  }
+  int s = launch_element_dump(c, first, count, dK, dF);
+  if (!s && (!ok(c, cudaMemcpyAsync(Ke, dK, sizeof(double) * 576 * count, cudaMemcpyDeviceToHost, c->stream), "K") ||
+             !ok(c, cudaMemcpyAsync(fint, dF, sizeof(double) * 24 * count, cudaMemcpyDeviceToHost, c->stream), "F")))
+    s = TG_ERR_CUDA;
+  if (!s) s = check_status(c);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(dK);
+  cudaFree(dF);
+  return s;
+}
+
+int tg_pcg_solve(tg_context* c, const double* rhs, double* du, double rel_tol, int max_it, int precond, int* iters,
+                 double* rel_res) {
+  if (!c || c->nnd <= 0 || max_it <= 0 || rel_tol <= 0.0) return TG_ERR_ARG;
+  if (precond != TG_PRECOND_JACOBI && precond != TG_PRECOND_BLOCK_JACOBI) return TG_ERR_ARG;
+  if (c->tangent_precision < 0) {
+    c->err = "tg_pcg_solve: form the tangent first";
+    return TG_ERR_ARG;
+  }
+  if (set_device(c)) return TG_ERR_CUDA;
+  const double4_32a* d_rhs = c->d_R;
+  double4_32a* tmp = nullptr;
+  double* d_eq = nullptr;
+  int s = TG_OK;
+  if (rhs || du) {
+    if (!ok(c, cudaMallocAsync((void**)&d_eq, sizeof(double) * std::max(c->neq, 1), c->stream), "alloc"))
+      return TG_ERR_OOM;
+  }
+  if (rhs) {
+    if (!ok(c, cudaMallocAsync((void**)&tmp, sizeof(double4_32a) * c->nnd, c->stream), "alloc") ||
+        !ok(c, cudaMemsetAsync(tmp, 0, sizeof(double4_32a) * c->nnd, c->stream), "memset") ||
+        !ok(c, cudaMemcpyAsync(d_eq, rhs, sizeof(double) * c->neq, cudaMemcpyHostToDevice, c->stream), "rhs"))
+      s = TG_ERR_CUDA;
+    if (!s) s = launch_scatter_eq(c, d_eq, tmp);
+    d_rhs = tmp;
+  }
+  if (!s) s = pcg_solve(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
+  int s2 = TG_OK;
+  if (du && (s == TG_OK || s == TG_ERR_NOT_CONVERGED)) {
+    s2 = launch_gather_solution(c, d_eq);
+    if (!s2 && !ok(c, cudaMemcpyAsync(du, d_eq, sizeof(double) * c->neq, cudaMemcpyDeviceToHost, c->stream), "du"))
+      s2 = TG_ERR_CUDA;
+  }
+  if (tmp) cudaFreeAsync(tmp, c->stream);
+  if (d_eq) cudaFreeAsync(d_eq, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return s ? s : s2;
+}
+
+int tg_apply_update(tg_context* c) {
+  if (!c || !c->have_du) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int s = launch_apply_update(c);
+  if (!s && !ok(c, cudaStreamSynchronize(c->stream), "sync")) s = TG_ERR_CUDA;
+  return s;
+}
+
+int tg_close_step(tg_context* c) {
+  if (!c) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int s = launch_close_step(c, 0);
+  if (!s && !ok(c, cudaStreamSynchronize(c->stream), "sync")) s = TG_ERR_CUDA;
+  return s;
+}
+
+int tg_reset_step(tg_context* c) {
+  if (!c) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int s = launch_close_step(c, 1);
+  if (!s && !ok(c, cudaStreamSynchronize(c->stream), "sync")) s = TG_ERR_CUDA;
+  return s;
+}
+
+int tg_get_active_set(tg_context* c, signed char* flags) {
+  if (!c || !flags || c->nel <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  return ok(c, cudaMemcpy(flags, c->d_j2_flags, (size_t)c->nel * 8, cudaMemcpyDeviceToHost), "flags") ? TG_OK
+                                                                                                      : TG_ERR_CUDA;
+}
+
+int tg_get_j2_state(tg_context* c, double* alpha, double* eps_p) {
+  if (!c || c->nel <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  const size_t nip = (size_t)c->nel * 8;
+  if (alpha && !ok(c, cudaMemcpy(alpha, c->d_j2_alpha, sizeof(double) * nip, cudaMemcpyDeviceToHost), "alpha"))
+    return TG_ERR_CUDA;
+  if (eps_p) {
+    std::vector<double> h(nip * 6);
+    if (!ok(c, cudaMemcpy(h.data(), c->d_j2_epsp, sizeof(double) * nip * 6, cudaMemcpyDeviceToHost), "epsp"))
+      return TG_ERR_CUDA;
+    for (size_t g = 0; g < nip; ++g)
+      for (int k = 0; k < 6; ++k) eps_p[g * 6 + k] = h[k * nip + g];
+  }
+  return TG_OK;
+}
+
+namespace {
+// NLSolver::Solve loop body: tangent, solve, update, residual (NLSolver.cpp:137-188)
+int newton_iteration(Context* c, const tg_newton_params* P, double* err, int* its, tg_newton_report* r,
+                     PhaseTimer* tm) {
+  if (tm) tm->start(c->stream);
+  int s = form_tangent(c, P->precision);
+  if (tm) r->ms_tangent += tm->stop(c->stream);
+  if (s) return s;
+  double rr = 0.0;
+  *its = 0;
+  if (tm) tm->start(c->stream);
+  s = pcg_solve(c, c->d_R, P->lin_rel_tol, P->lin_max_it, P->precond, its, &rr);
+  if (s == TG_ERR_NOT_CONVERGED) s = TG_OK;  // inexact Newton step; the outer test decides
+  if (!s) s = launch_apply_update(c);
+  if (tm) r->ms_solve += tm->stop(c->stream);
+  if (s) return s;
+  c->iteration += 1;
+  if (tm) tm->start(c->stream);
+  s = residual_norm(c, err);
+  if (tm) r->ms_residual += tm->stop(c->stream);
+  return s;
+}
+}  // namespace
+
+int tg_newton_iteration(tg_context* c, const tg_newton_params* P, double* norm, int* pcg_iterations) {
+  if (!c || !P || c->nnd <= 0) return TG_ERR_ARG;
+  if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  tg_newton_report r;
+  std::memset(&r, 0, sizeof(r));
+  double err = 0.0;
+  int its = 0;
+  int s = newton_iteration(c, P, &err, &its, &r, nullptr);
+  if (norm) *norm = err;
+  if (pcg_iterations) *pcg_iterations = its;
+  return s;
+}
+
+int tg_newton_solve(tg_context* c, const tg_newton_params* P, tg_newton_report* rep) {
+  if (!c || !P || c->nnd <= 0) return TG_ERR_ARG;
+  if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  tg_newton_report r;
+  std::memset(&r, 0, sizeof(r));
+  PhaseTimer tm(rep != nullptr);
+  // SolverT::InitStep: iteration -1 for the first residual
+  c->iteration = -1;
+  tm.start(c->stream);
+  double err0 = 0.0;
+  int s = residual_norm(c, &err0);
+  r.ms_residual += tm.stop(c->stream);
+  r.error0 = r.error = err0;
+  if (s) {
+    if (rep) *rep = r;
+    return s;
+  }
+  bool converged = err0 < P->abs_tol;  // "hit on first try"
+  while (!converged) {
+    double err = 0.0;
+    int its = 0;
+    s = newton_iteration(c, P, &err, &its, &r, rep ? &tm : nullptr);
+    r.pcg_iterations += its;
+    if (s) break;
+    ++r.iterations;
+    r.error = err;
+    const double rel = err / err0;
+    if (rel > P->div_tol) {
+      c->err = "diverging solution";
+      s = TG_ERR_DIVERGED;
+      break;
+    }
+    if (rel < P->rel_tol || err < P->abs_tol) {
+      converged = true;
+    } else if (c->iteration >= P->max_iterations) {
+      c->err = "max iterations hit";
+      s = TG_ERR_NOT_CONVERGED;
+      break;
+    }
+  }
+  if (rep) *rep = r;
+  return s;
+}
+
+int tg_predict_prescribed(tg_context* c, int n, const int* idx, const double* val, const tg_newton_params* P,
+                          int* pcg_iterations) {
+  if (!c || !P || n < 0 || (n > 0 && (!idx || !val)) || c->nnd <= 0) return TG_ERR_ARG;
+  if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
+  for (int k = 0; k < n; ++k)
+    if (idx[k] < 0 || idx[k] >= c->nnd * 3) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (pcg_iterations) *pcg_iterations = 0;
+  // R(u_old) without committing history, tangent at u_old
+  int s = launch_residual_nocommit(c);
+  if (!s) s = check_status(c);
+  if (!s) s = form_tangent(c, P->precision);
+  if (s) return s;
+  double4_32a *d_old = nullptr, *d_v = nullptr;
+  int* d_idx = nullptr;
+  double* d_val = nullptr;
+  const size_t nb = sizeof(double4_32a) * c->nnd;
+  if (!ok(c, cudaMallocAsync((void**)&d_old, nb, c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&d_v, nb, c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&d_idx, sizeof(int) * std::max(n, 1), c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&d_val, sizeof(double) * std::max(n, 1), c->stream), "alloc"))
+    return TG_ERR_OOM;
+  if (!ok(c, cudaMemcpyAsync(d_old, c->d_u, nb, cudaMemcpyDeviceToDevice, c->stream), "copy") ||
+      (n > 0 && (!ok(c, cudaMemcpyAsync(d_idx, idx, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream), "idx") ||
+                 !ok(c, cudaMemcpyAsync(d_val, val, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream), "val"))))
+    s = TG_ERR_CUDA;
+  if (!s) s = launch_set_prescribed(c, n, d_idx, d_val);  // u now carries the new prescribed values
+  if (!s) s = launch_diff(c, c->d_u, d_old, d_v);         // v = du_p (zero on free dofs)
+  if (!s) s = launch_lift_rhs(c, d_v, d_old);             // rhs = R - K v (d_old is free after the diff)
+  int its = 0;
+  double rr = 0.0;
+  if (!s) {
+    s = pcg_solve(c, d_old, P->lin_rel_tol, P->lin_max_it, P->precond, &its, &rr);
+    if (s == TG_ERR_NOT_CONVERGED) s = TG_OK;
+  }
+  if (!s) s = launch_apply_update(c);
+  cudaFreeAsync(d_old, c->stream);
+  cudaFreeAsync(d_v, c->stream);
+  cudaFreeAsync(d_idx, c->stream);
+  cudaFreeAsync(d_val, c->stream);
+  if (!ok(c, cudaStreamSynchronize(c->stream), "sync") && !s) s = TG_ERR_CUDA;
+  if (pcg_iterations) *pcg_iterations = its;
+  return s;
+}
+
+int tg_checkpoint(tg_context* c) {
+  if (!c || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (!c->d_u_ckpt && (!dalloc(c, &c->d_u_ckpt, (size_t)c->nnd) || !dalloc(c, &c->d_R_ckpt, (size_t)c->nnd)))
+    return TG_ERR_OOM;
+  const size_t n = sizeof(double4_32a) * c->nnd;
+  return ok(c, cudaMemcpyAsync(c->d_u_ckpt, c->d_u, n, cudaMemcpyDeviceToDevice, c->stream), "ckpt") &&
+                 ok(c, cudaMemcpyAsync(c->d_R_ckpt, c->d_R, n, cudaMemcpyDeviceToDevice, c->stream), "ckpt")
+             ? TG_OK
+             : TG_ERR_CUDA;
+}
+
+int tg_rollback(tg_context* c) {
+  if (!c || !c->d_u_ckpt) return TG_ERR_ARG;
+  const size_t n = sizeof(double4_32a) * c->nnd;
+  return ok(c, cudaMemcpyAsync(c->d_u, c->d_u_ckpt, n, cudaMemcpyDeviceToDevice, c->stream), "rollback") &&
+                 ok(c, cudaMemcpyAsync(c->d_R, c->d_R_ckpt, n, cudaMemcpyDeviceToDevice, c->stream), "rollback")
+             ? TG_OK
+             : TG_ERR_CUDA;
+}
+
+int tg_timer_start(tg_context* c) {
+  if (!c) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (!c->ev_a && (!ok(c, cudaEventCreate(&c->ev_a), "event") || !ok(c, cudaEventCreate(&c->ev_b), "event")))
+    return TG_ERR_CUDA;
+  return ok(c, cudaEventRecord(c->ev_a, c->stream), "event") ? TG_OK : TG_ERR_CUDA;
+}
+
+int tg_timer_stop(tg_context* c, double* ms) {
+  if (!c || !c->ev_a || !ms) return TG_ERR_ARG;
+  float e = 0.f;
+  if (!ok(c, cudaEventRecord(c->ev_b, c->stream), "event") || !ok(c, cudaEventSynchronize(c->ev_b), "event") ||
+      !ok(c, cudaEventElapsedTime(&e, c->ev_a, c->ev_b), "event"))
+    return TG_ERR_CUDA;
+  *ms = e;
+  return TG_OK;
+}
+
+int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
+  if (!c || reps <= 0 || !ms || which < 0 || which > 4) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (which <= 1) return time_pcg_kernel(c, which, reps, ms);
+  if ((which == 2 || which == 3) && c->tangent_precision < 0) return TG_ERR_ARG;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double total = 0.0;
+  int s = TG_OK;
+  for (int r = 0; r < reps && !s; ++r) {
+    cudaEventRecord(a, c->stream);
+    if (which == 2) s = launch_tangent(c, c->tangent_precision);
+    else if (which == 3) s = launch_assemble(c, c->tangent_precision);
+    else s = launch_residual(c);
+    cudaEventRecord(b, c->stream);
+    cudaEventSynchronize(b);
+    float e = 0.f;
+    cudaEventElapsedTime(&e, a, b);
+    total += e;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!s) s = check_status(c);
+  *ms = total / reps;
+  return s;
+}
+
+}  // extern "C"

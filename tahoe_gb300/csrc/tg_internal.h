@@ -1,0 +1,196 @@
+// Internal declarations shared by the host C++ and the CUDA translation units
+// of the tahoe_gb300 library.  Nothing here is part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tahoe_gb300.h"
+
+namespace tg {
+
+constexpr int kMaxBlocks = 4;      // material blocks per element group
+constexpr int kNumSMs = 152;       // GB300
+constexpr int kSlots = 36;         // upper-triangle node-pair blocks of a hex8 element
+constexpr int kKeBlock = 9;        // 3x3 block values
+constexpr int kKeStride = kSlots * kKeBlock;  // 324 values per element
+
+// Device status bits (set by kernels with atomicOr, never by trapping).
+enum : int { kStatusBadJacobian = 1, kStatusNaN = 2 };
+
+struct MatParams {
+  int kind;
+  int elastic_its;
+  double mu, kappa, lambda;
+  double hard_a, hard_b;
+  double C[36];  // row-major 6x6, engineering-shear Voigt
+};
+
+struct MatTable {
+  int nblocks;
+  int formulation;
+  MatParams m[kMaxBlocks];
+};
+
+// Scalars of one PCG solve, resident in device memory.
+struct PcgScalars {
+  double rz, rz_old, rr, rr0, pq, alpha, beta, tol2;
+  int done;       // 1 converged, 2 breakdown / non-finite
+  int iters;
+  int max_it;
+  unsigned int count_a, count_b;  // last-block-done counters
+  int fail;  // breakdown cause: 1 init non-finite, 2 p.q <= 0, 3 p.q non-finite, 4 update non-finite
+};
+
+// Scalars of the residual kernel.
+struct ResidScalars {
+  double norm2;
+  unsigned int count;
+  int pad;
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long launches = 0;
+
+  // mesh
+  int nnd = 0, nel = 0, neq = 0;
+  int formulation = TG_SMALL_STRAIN;
+  MatTable mats{};
+  bool have_blocks = false;
+  bool has_j2 = false;
+  std::vector<int> h_conn;       // nel*8
+  std::vector<int> h_eqnos;      // nnd*3
+  std::vector<double> h_coords;  // SoA 3*nnd
+  std::vector<int> h_eq_slot;    // neq -> node*4+dof
+
+  // device mesh
+  double* d_X = nullptr;        // SoA 3*nnd
+  int* d_conn = nullptr;        // nel*8
+  int8_t* d_block = nullptr;    // nel (optional)
+  uint8_t* d_mask = nullptr;    // nnd, active-dof bits
+  int* d_eq_slot = nullptr;     // neq
+  int* d_node_elem_ptr = nullptr;  // nnd+1
+  int* d_node_elem = nullptr;      // nel*8: e*8+a, sorted per node
+
+  // block CSR (3x3 node blocks)
+  long long nnzb = 0;
+  long long nnzb_pad = 0;       // SoA stride of the value arrays
+  int* d_rowptr = nullptr;      // nnd+1
+  int* d_col = nullptr;         // nnzb
+  int* d_contrib_ptr = nullptr; // nnzb+1
+  int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
+  std::vector<int> h_rowptr, h_col;
+  float* d_vals32 = nullptr;    // 9*nnzb_pad
+  double* d_vals64 = nullptr;
+  float* d_minv32 = nullptr;    // 18*nnd: Jacobi then block-Jacobi
+  double* d_minv64 = nullptr;
+  float* d_Ke32 = nullptr;      // nel*324
+  double* d_Ke64 = nullptr;
+  int tangent_precision = -1;   // precision of the last tangent
+  int tangent_precond = -1;
+
+  // nodal vectors (padded to 4 per node)
+  double4_32a* d_u = nullptr;
+  double4_32a* d_fext = nullptr;
+  double4_32a* d_R = nullptr;
+  double4_32a* d_fint = nullptr;   // nel*8
+  double load_factor = 1.0;
+  int iteration = 0;
+
+  // J2 history (structure of arrays over nel*8 integration points)
+  int8_t* d_j2_flags = nullptr;
+  int8_t* d_j2_alloc = nullptr;  // nel
+  double* d_j2_alpha = nullptr;
+  double* d_j2_dgamma = nullptr;
+  double* d_j2_norm = nullptr;
+  double* d_j2_epsp = nullptr;   // 6*nel*8 (component-major)
+  double* d_j2_nhat = nullptr;   // 6*nel*8
+
+  // PCG work
+  void* d_x = nullptr;  // float4 or double4_32a per node (solution du)
+  void* d_r = nullptr;
+  void* d_z = nullptr;
+  void* d_p = nullptr;
+  void* d_q = nullptr;
+  int pcg_vec_precision = -1;
+  PcgScalars* d_pcg = nullptr;
+  double* d_partials = nullptr;  // reduction partials
+  int partials_cap = 0;
+  ResidScalars* d_resid = nullptr;
+  int* d_status = nullptr;
+  PcgScalars* h_pcg = nullptr;       // pinned mirror
+  ResidScalars* h_resid = nullptr;   // pinned mirror
+  int* h_status = nullptr;           // pinned mirror
+  double4_32a* d_du_last = nullptr;      // FP64 update (nnd)
+  bool have_du = false;
+
+  // CUDA graph of a chunk of PCG iterations
+  cudaGraphExec_t pcg_graph = nullptr;
+  int pcg_graph_key = -1;  // precision*2 + precond
+
+  // step-start snapshot (tg_checkpoint / tg_rollback)
+  double4_32a* d_u_ckpt = nullptr;
+  double4_32a* d_R_ckpt = nullptr;
+  // caller timer (tg_timer_start / tg_timer_stop)
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+
+  std::vector<void*> allocations;
+};
+
+// ---- helpers ----
+bool ok(Context* c, cudaError_t e, const char* what);
+template <typename T>
+bool dalloc(Context* c, T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    c->err = std::string("cudaMalloc failed: ") + cudaGetErrorString(e);
+    *p = nullptr;
+    return false;
+  }
+  c->allocations.push_back((void*)*p);
+  return true;
+}
+void dfree(Context* c, void* p);
+
+// ---- host mesh utilities (mesh.cpp) ----
+void build_block_pattern(int nnd, int nel, const int* conn, std::vector<int>& rowptr, std::vector<int>& col);
+void build_contrib_map(int nnd, int nel, const int* conn, const std::vector<int>& rowptr,
+                       const std::vector<int>& col, std::vector<int>& cptr, std::vector<int>& contrib);
+void build_node_elem(int nnd, int nel, const int* conn, std::vector<int>& ptr, std::vector<int>& list);
+
+// ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----
+int launch_residual(Context* c);          // fint per element + gather + norm
+int launch_tangent(Context* c, int precision);   // Ke per element
+int launch_assemble(Context* c, int precision);
+int form_tangent(Context* c, int precision);
+int launch_element_dump(Context* c, int first, int count, double* dKe, double* dfint);
+int launch_close_step(Context* c, int reset);
+int launch_set_prescribed(Context* c, int n, const int* d_idx, const double* d_val);
+int launch_apply_update(Context* c);
+int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
+              double* rel_res);
+int time_pcg_kernel(Context* c, int which, int reps, double* ms);
+int launch_residual_nocommit(Context* c);
+// rhs = R - K v on active rows (v nodal, K the last tangent), FP64 accumulation
+int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs);
+int launch_diff(Context* c, const double4_32a* a, const double4_32a* b, double4_32a* out);
+int launch_gather_eq(Context* c, const double4_32a* d_nodal, double* d_eq);
+int launch_scatter_eq(Context* c, const double* d_eq, double4_32a* d_nodal);
+
+}  // namespace tg
+
+// The opaque handle of the C ABI is the context itself.
+struct tg_context : public tg::Context {};

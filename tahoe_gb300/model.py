@@ -1,0 +1,168 @@
+"""Host-side mirror of the reference's deck-level plugin surface.
+
+A ``SolidModel`` is what a Tahoe deck with a GPU element group and the GPU
+matrix/solver type describes: a hex8 element group (``small_strain`` or
+``total_lagrangian``), its material blocks, kinematic/force/traction boundary
+conditions with a load schedule, and a Newton solver over the device CSR
+matrix with (block-)Jacobi PCG.  ``run`` is the time loop of
+FEManagerT::Solve (tahoe/src/main/FEManagerT.cpp:138-262): per step it applies
+the prescribed values (FieldT::InitStep, FieldT.cpp:261), sets the schedule
+factor, calls the C++ Newton driver (tg_newton_solve) and closes the step
+(ContinuumElementT::CloseStep).
+"""
+import numpy as np
+
+from . import lib
+from .meshgen import equations
+
+# XML names registered by the reference factories (ElementListT.cpp:738,752;
+# SSSolidMatList3DT.cpp:199-207; FSSolidMatList3DT.cpp:409-415) and what the
+# GPU group runs for them.  updated_lagrangian converges to the same
+# displacement field as total_lagrangian for these hyperelastic materials.
+ELEMENT_GROUPS = {
+    "small_strain": lib.SMALL_STRAIN,
+    "total_lagrangian": lib.TOTAL_LAGRANGIAN,
+    "updated_lagrangian": lib.TOTAL_LAGRANGIAN,
+}
+MATERIALS = {
+    "small_strain_StVenant": lib.MAT_SS_HOOKEAN,
+    "small_strain_Hookean": lib.MAT_SS_HOOKEAN,
+    "small_strain_StVenant_J2": lib.MAT_SS_J2,
+    "Simo_isotropic": lib.MAT_FS_SIMO,
+    "large_strain_StVenant": lib.MAT_FS_STVENANT,
+}
+MATRIX_TYPES = {"GPU_CSR_matrix": (lib.FP64, lib.PRECOND_JACOBI),
+                "GPU_CSR_matrix_mixed": (lib.MIXED, lib.PRECOND_JACOBI)}
+
+
+def material_params(mat):
+    """(kind, params) from a material description dict."""
+    k = mat["kind"]
+    if k == "ss_hookean":
+        if "C" in mat:
+            return lib.MAT_SS_HOOKEAN, np.asarray(mat["C"], dtype=np.float64).reshape(36)
+        return lib.MAT_SS_HOOKEAN, np.array([mat["E"], mat["nu"]])
+    if k == "ss_j2":
+        return lib.MAT_SS_J2, np.array([mat["E"], mat["nu"], mat["a"], mat["b"], mat.get("elastic_iterations", 0)])
+    if k == "fs_simo":
+        return lib.MAT_FS_SIMO, np.array([mat["mu"], mat["kappa"]])
+    if k == "fs_stvenant":
+        return lib.MAT_FS_STVENANT, np.array([mat["E"], mat["nu"]])
+    raise ValueError("unknown material kind %r" % k)
+
+
+def schedule_value(pts, t):
+    """PiecewiseLinearT::function (toolbox/src/C1functions/PiecewiseLinearT.cpp:179)"""
+    if pts is None or len(pts) == 0:
+        return 1.0
+    xs = [p[0] for p in pts]
+    ys = [p[1] for p in pts]
+    if t <= xs[0]:
+        return ys[0]
+    for i in range(1, len(xs)):
+        if t < xs[i]:
+            return ys[i - 1] + (t - xs[i - 1]) * (ys[i] - ys[i - 1]) / (xs[i] - xs[i - 1])
+    return ys[-1]
+
+
+class SolidModel:
+    def __init__(self, X, conn, formulation, materials, blocks=None, device=0):
+        self.X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 8)
+        self.formulation = ELEMENT_GROUPS.get(formulation, formulation)
+        if isinstance(materials, dict):
+            materials = [materials]
+        self.materials = materials
+        self.blocks = None if blocks is None else np.ascontiguousarray(blocks, dtype=np.int32)
+        self.schedule = None
+        self.kbc = []       # (node, dof, value, scheduled)
+        self.forces = []    # (node, dof, value)
+        self.tractions = []  # (elem, facet, t3)
+        self.device = device
+        self.ctx = None
+
+    # boundary conditions -------------------------------------------------
+    def set_schedule(self, pts):
+        self.schedule = [tuple(p) for p in pts]
+
+    def add_kbc(self, node, dof, value=0.0, scheduled=False):
+        self.kbc.append((int(node), int(dof), float(value), bool(scheduled)))
+
+    def add_force(self, node, dof, value):
+        self.forces.append((int(node), int(dof), float(value)))
+
+    def add_traction(self, elem, facet, t):
+        self.tractions.append((int(elem), int(facet), [float(x) for x in t]))
+
+    def equations(self):
+        idx = [n * 3 + d for (n, d, _, _) in self.kbc]
+        return equations(self.X.shape[0], idx)
+
+    # set-up ----------------------------------------------------------------
+    def setup(self):
+        eq = self.equations()
+        c = lib.Context(self.device)
+        c.upload(self.X, self.conn, eq)
+        c.set_formulation(self.formulation)
+        for b, m in enumerate(self.materials):
+            kind, p = material_params(m)
+            c.set_material(b, kind, p)
+        if self.blocks is not None:
+            c.set_blocks(self.blocks)
+        f = np.zeros((self.X.shape[0], 3))
+        for n, d, v in self.forces:
+            f[n, d] += v
+        if self.tractions:
+            e = [t[0] for t in self.tractions]
+            fc = [t[1] for t in self.tractions]
+            tr = [t[2] for t in self.tractions]
+            f += lib.traction_forces(self.X, self.conn, e, fc, tr)
+        c.set_fext(f)
+        self.ctx = c
+        self.eqnos = eq
+        self._kbc_idx = np.array([n * 3 + d for (n, d, _, _) in self.kbc], dtype=np.int32)
+        self._kbc_val = np.array([v for (_, _, v, _) in self.kbc])
+        self._kbc_sch = np.array([s for (_, _, _, s) in self.kbc], dtype=bool)
+        return c
+
+    def apply_step(self, t, predictor=None):
+        """Prescribed values and load factor of the step at time t.  With
+        predictor=(precision, precond, lin_rel_tol) the prescribed increment
+        is applied through tg_predict_prescribed instead of directly."""
+        sc = schedule_value(self.schedule, t)
+        self.ctx.set_load_factor(sc)
+        vals = np.where(self._kbc_sch, sc * self._kbc_val, 0.0)
+        if predictor is not None:
+            prec, pc, tol = predictor
+            return self.ctx.predict_prescribed(self._kbc_idx, vals, precision=prec, precond=pc, lin_rel_tol=tol)
+        if len(self._kbc_idx):
+            self.ctx.set_prescribed(self._kbc_idx, vals)
+        return 0
+
+    def run(self, nsteps, dt, rel_tol=1e-12, abs_tol=1e-10, max_iterations=10, div_tol=10.0, precision=lib.FP64,
+            precond=lib.PRECOND_JACOBI, lin_rel_tol=1e-12, lin_max_it=20000, on_step=None, predictor=False):
+        if self.ctx is None:
+            self.setup()
+        c = self.ctx
+        hist, reports = [], []
+        for step in range(1, nsteps + 1):
+            self.apply_step(step * dt, (precision, precond, lin_rel_tol) if predictor else None)
+            rc, rep = c.newton(rel_tol, abs_tol, div_tol, max_iterations, precision, precond, lin_rel_tol, lin_max_it)
+            if on_step is not None:
+                on_step(step, c)
+            c.close_step()
+            hist.append(c.get_u())
+            reports.append(rep)
+        return np.array(hist), reports
+
+
+def model_from_fixture(fx, device=0):
+    m = SolidModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], device=device)
+    m.set_schedule(fx["schedule"])
+    for n, d, v, s in fx["kbc"]:
+        m.add_kbc(n, d, v, s)
+    for n, d, v in fx.get("forces", []):
+        m.add_force(n, d, v)
+    for row in fx.get("tractions", []):
+        m.add_traction(row[0], row[1], row[2:5])
+    return m

@@ -1,0 +1,59 @@
+"""Shared builders for the parity tests (oracle and GPU driven from the same
+inputs)."""
+import json
+import os
+
+import numpy as np
+
+from oracle.pyoracle import OracleModel
+from tahoe_gb300.meshgen import BoxMesh
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN_NAMES = ["mat08_j2_cube", "mat24_hookean_cube", "mat05_simo_cube", "traction_a_cube",
+                "beam_newton_totlag", "beam_newton_updlag"]
+
+
+def load_fixture(name):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        return json.load(f)
+
+
+def golden_displacements(fx):
+    """{step index (0-based): (nnd,3) displacements} from the golden outputs"""
+    out = {}
+    for o in fx["outputs"]:
+        step = int(round(o["time"] / fx["dt"])) - 1
+        out[step] = np.array(o["rows"])[:, :3]
+    return out
+
+
+def msr_to_upper_csr(bindx, n):
+    """MSR (diagonal implicit) -> list of sorted upper columns per row incl. diag"""
+    rows = []
+    for r in range(n):
+        rows.append(np.concatenate([[r], bindx[bindx[r]:bindx[r + 1]]]))
+    return rows
+
+
+def cube_case(n=4, jitter=0.0, seed=0, fix="z0"):
+    """small box with z=0 fully fixed (and optionally more) for parity"""
+    m = BoxMesh(n, n, n, jitter=jitter, seed=seed)
+    fixed = []
+    for node in m.face_nodes(2, 0):
+        for d in range(3):
+            fixed.append((int(node), d))
+    return m, fixed
+
+
+def oracle_for(mesh, formulation, material, fixed, blocks=None, threads=1):
+    o = OracleModel(mesh.X, mesh.conn, formulation, material, blocks=blocks, threads=threads)
+    for node, d in fixed:
+        o.add_kbc(node, d, 0.0, False)
+    return o
+
+
+def rel_err(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    s = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / s)
