@@ -322,6 +322,27 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+KERNELS = {"spmv": 0, "update": 1, "tangent": 2, "assembly": 3, "residual": 4}
+
+
+def run_kernel_only(args):
+    """Standalone launches of one hot kernel on the C2 state (for ncu): the
+    step's prescribed values applied directly, residual, tangent, then
+    --launches launches of the chosen kernel timed with CUDA events."""
+    from tahoe_gb300 import lib, workloads
+    prec = lib.MIXED if args.precision == "mixed" else lib.FP64
+    mesh, model, _ = workloads.c2(n=args.n)
+    model.setup()
+    model.apply_step(1.0)
+    ctx = model.ctx
+    ctx.set_iteration(-1)
+    ctx.residual(want_vector=False)
+    ctx.tangent(prec)
+    ms = ctx.time_kernel(KERNELS[args.kernel], args.launches)
+    print(json.dumps({"kernel": args.kernel, "n": args.n, "precision": args.precision, "launches": args.launches,
+                      "ms_per_launch": ms, "block_nnz": ctx.block_nnz, "nodes": mesh.nnd, "elements": mesh.nel}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,8 +353,13 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the full load-step comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--ref-pcg-iters", type=int, default=600)
+    ap.add_argument("--kernel", choices=sorted(KERNELS), help="time standalone launches of one kernel only")
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--n", type=int, default=64, help="mesh size per side for --kernel")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.kernel:
+        run_kernel_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -208,7 +208,13 @@ int tg_rollback(tg_context* ctx);
  * as in SolverT::InitStep.  Does not close the step. */
 int tg_newton_solve(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report);
 
-/* ---- measurement helpers (no reference counterpart) --------------------- */
+/* ---- measurement and tuning helpers (no reference counterpart) ---------- */
+
+/* Shape of the streamed PCG matrix product: row tiles of at most tile_blocks
+ * block nonzeros (the unit of the tile-contiguous matrix storage) staged
+ * through a ring of `stages` (2 or 3) shared-memory buffers.  Defaults
+ * 640 / 2.  Changing the tile size drops the assembled tangent. */
+int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
 
 /* CUDA events on the context stream around caller-defined work */
 int tg_timer_start(tg_context* ctx);

@@ -163,11 +163,12 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
   c->pcg_vec_precision = -1;
   c->pcg_graph_key = -1;
   c->tangent_precision = -1;
-  c->d_x = c->d_r = c->d_z = c->d_p = c->d_q = nullptr;
+  c->d_x = c->d_r = c->d_z = c->d_p = c->d_p1 = c->d_q = nullptr;
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
-  c->d_vals32 = nullptr;
-  c->d_vals64 = nullptr;
+  c->d_blob32 = c->d_blob64 = nullptr;
+  c->d_blob_off32 = c->d_blob_off64 = nullptr;
+  c->d_row_tile = nullptr;
   c->d_minv32 = nullptr;
   c->d_minv64 = nullptr;
   c->d_block = nullptr;
@@ -203,12 +204,12 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
   build_node_elem(nnd, nel, conn, nptr, nlist);
   c->nnzb = c->h_rowptr[nnd];
   c->nnzb_pad = (c->nnzb + 31) / 32 * 32;
-
   const size_t nip = (size_t)nel * 8;
   bool good = dalloc(c, &c->d_X, (size_t)nnd * 3) && dalloc(c, &c->d_conn, (size_t)nel * 8) &&
               dalloc(c, &c->d_mask, (size_t)nnd) && dalloc(c, &c->d_eq_slot, (size_t)std::max(neq, 1)) &&
               dalloc(c, &c->d_node_elem_ptr, (size_t)nnd + 1) && dalloc(c, &c->d_node_elem, nip) &&
-              dalloc(c, &c->d_rowptr, (size_t)nnd + 1) && dalloc(c, &c->d_col, (size_t)c->nnzb) &&
+              dalloc(c, &c->d_rowptr, (size_t)(nnd + 1 + 3) / 4 * 4 + 4) && dalloc(c, &c->d_col, (size_t)c->nnzb_pad) &&
+
               dalloc(c, &c->d_contrib_ptr, (size_t)c->nnzb + 1) && dalloc(c, &c->d_contrib, (size_t)nel * 64) &&
               dalloc(c, &c->d_u, (size_t)nnd) && dalloc(c, &c->d_fext, (size_t)nnd) && dalloc(c, &c->d_R, (size_t)nnd) &&
               dalloc(c, &c->d_fint, nip) && dalloc(c, &c->d_status, 1) && dalloc(c, &c->d_resid, 1) &&
@@ -226,8 +227,11 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
          ok(c, cudaMemcpyAsync(c->d_eq_slot, c->h_eq_slot.data(), sizeof(int) * neq, cudaMemcpyHostToDevice, s), "slot") &&
          ok(c, cudaMemcpyAsync(c->d_node_elem_ptr, nptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, s), "np") &&
          ok(c, cudaMemcpyAsync(c->d_node_elem, nlist.data(), sizeof(int) * nip, cudaMemcpyHostToDevice, s), "nl") &&
+         ok(c, cudaMemsetAsync(c->d_rowptr, 0, sizeof(int) * ((size_t)(nnd + 1 + 3) / 4 * 4 + 4), s), "rp") &&
          ok(c, cudaMemcpyAsync(c->d_rowptr, c->h_rowptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, s), "rp") &&
+         ok(c, cudaMemsetAsync(c->d_col, 0, sizeof(int) * c->nnzb_pad, s), "col") &&
          ok(c, cudaMemcpyAsync(c->d_col, c->h_col.data(), sizeof(int) * c->nnzb, cudaMemcpyHostToDevice, s), "col") &&
+
          ok(c, cudaMemcpyAsync(c->d_contrib_ptr, cptr.data(), sizeof(int) * (c->nnzb + 1), cudaMemcpyHostToDevice, s), "cp") &&
          ok(c, cudaMemcpyAsync(c->d_contrib, contrib.data(), sizeof(int) * (size_t)nel * 64, cudaMemcpyHostToDevice, s), "ct") &&
          ok(c, cudaMemsetAsync(c->d_u, 0, sizeof(double4_32a) * nnd, s), "u") &&
@@ -244,7 +248,103 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
          ok(c, cudaMemsetAsync(c->d_j2_epsp, 0, sizeof(double) * nip * 6, s), "ep") &&
          ok(c, cudaMemsetAsync(c->d_j2_nhat, 0, sizeof(double) * nip * 6, s), "nh") &&
          ok(c, cudaStreamSynchronize(s), "upload sync");
-  return good ? TG_OK : TG_ERR_CUDA;
+  if (!good) return TG_ERR_CUDA;
+  c->d_tile_row = nullptr;
+  return build_tiles(c, c->spmv_tile_blocks);
+}
+
+}  // extern "C"
+
+namespace tg {
+// Row tiles of the streamed SpMV: consecutive rows holding at most
+// tile_blocks block nonzeros (a longer row is a tile of its own), and the
+// byte offsets of every tile in the tile-contiguous matrix storage of each
+// precision.  Any existing matrix storage is dropped (its layout changes).
+int build_tiles(Context* c, int tile_blocks) {
+  std::vector<int> tiles(1, 0);
+  for (int r = 0; r < c->nnd; ++r)
+    if (r > tiles.back() && c->h_rowptr[r + 1] - c->h_rowptr[tiles.back()] > tile_blocks) tiles.push_back(r);
+  tiles.push_back(c->nnd);
+  const int nt = (int)tiles.size() - 1;
+  std::vector<int> row_tile(c->nnd);
+  c->h_blob_off32.assign(nt + 1, 0);
+  c->h_blob_off64.assign(nt + 1, 0);
+  c->blob_cap32 = c->blob_cap64 = 0;
+  for (int t = 0; t < nt; ++t) {
+    const int nrows = tiles[t + 1] - tiles[t];
+    const int nb = c->h_rowptr[tiles[t + 1]] - c->h_rowptr[tiles[t]];
+    for (int r = tiles[t]; r < tiles[t + 1]; ++r) row_tile[r] = t;
+    const long long b32 = blob_tile_bytes(nrows, nb, 4), b64 = blob_tile_bytes(nrows, nb, 8);
+    c->h_blob_off32[t + 1] = c->h_blob_off32[t] + b32;
+    c->h_blob_off64[t + 1] = c->h_blob_off64[t] + b64;
+    c->blob_cap32 = std::max(c->blob_cap32, b32);
+    c->blob_cap64 = std::max(c->blob_cap64, b64);
+  }
+  for (void** p : {(void**)&c->d_tile_row, (void**)&c->d_row_tile, (void**)&c->d_blob_off32,
+                   (void**)&c->d_blob_off64, (void**)&c->d_blob32, (void**)&c->d_blob64}) {
+    if (*p) dfree(c, *p);
+    *p = nullptr;
+  }
+  c->tangent_precision = -1;  // values must be assembled into the new layout
+  c->ntiles = nt;
+  c->h_tile_row = tiles;
+  c->spmv_tile_blocks = tile_blocks;
+  if (!dalloc(c, &c->d_tile_row, tiles.size()) || !dalloc(c, &c->d_row_tile, (size_t)c->nnd) ||
+      !dalloc(c, &c->d_blob_off32, (size_t)nt + 1) || !dalloc(c, &c->d_blob_off64, (size_t)nt + 1))
+    return TG_ERR_OOM;
+  if (!ok(c, cudaMemcpy(c->d_tile_row, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice), "tiles") ||
+      !ok(c, cudaMemcpy(c->d_row_tile, row_tile.data(), sizeof(int) * c->nnd, cudaMemcpyHostToDevice), "rows") ||
+      !ok(c, cudaMemcpy(c->d_blob_off32, c->h_blob_off32.data(), sizeof(long long) * (nt + 1), cudaMemcpyHostToDevice),
+          "off") ||
+      !ok(c, cudaMemcpy(c->d_blob_off64, c->h_blob_off64.data(), sizeof(long long) * (nt + 1), cudaMemcpyHostToDevice),
+          "off"))
+    return TG_ERR_CUDA;
+  // the captured PCG chunk bakes in the launch shape
+  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
+  c->pcg_graph = nullptr;
+  c->pcg_graph_key = -1;
+  return TG_OK;
+}
+
+// Allocates the matrix storage of one precision and writes its structure
+// (headers, local row pointers, column indices); the value planes are filled
+// by the assembly.
+int ensure_blob(Context* c, int precision) {
+  unsigned char** blob = precision == TG_MIXED ? &c->d_blob32 : &c->d_blob64;
+  if (*blob) return TG_OK;
+  const std::vector<long long>& off = precision == TG_MIXED ? c->h_blob_off32 : c->h_blob_off64;
+  const int elem = precision == TG_MIXED ? 4 : 8;
+  const long long total = off[c->ntiles];
+  std::vector<unsigned char> h((size_t)total, 0);
+  for (int t = 0; t < c->ntiles; ++t) {
+    const int r0 = c->h_tile_row[t], r1 = c->h_tile_row[t + 1];
+    const int b0 = c->h_rowptr[r0], nb = c->h_rowptr[r1] - b0, nrows = r1 - r0;
+    int* hdr = reinterpret_cast<int*>(h.data() + off[t]);
+    hdr[0] = r0;
+    hdr[1] = nrows;
+    hdr[2] = nb;
+    hdr[3] = (int)((((long long)nb * elem + 15) / 16 * 16) / elem);
+    int* rp = hdr + 4;
+    for (int i = 0; i <= nrows; ++i) rp[i] = c->h_rowptr[r0 + i] - b0;
+    int* cl = rp + ceil4(nrows + 1);
+    for (int j = 0; j < nb; ++j) cl[j] = c->h_col[b0 + j];
+  }
+  if (!dalloc(c, blob, (size_t)total)) return TG_ERR_OOM;
+  return ok(c, cudaMemcpy(*blob, h.data(), (size_t)total, cudaMemcpyHostToDevice), "blob") ? TG_OK : TG_ERR_CUDA;
+}
+}  // namespace tg
+
+extern "C" {
+
+int tg_spmv_config(tg_context* c, int tile_blocks, int stages) {
+  if (!c || tile_blocks < 32 || tile_blocks > 16384 || stages < 2 || stages > 3) return TG_ERR_ARG;
+  c->spmv_stages = stages;
+  if (c->nnd <= 0) {
+    c->spmv_tile_blocks = tile_blocks;
+    return TG_OK;
+  }
+  if (cudaSetDevice(c->device) != cudaSuccess) return TG_ERR_CUDA;
+  return build_tiles(c, tile_blocks);
 }
 
 int tg_element_set(tg_context* c, int formulation) {

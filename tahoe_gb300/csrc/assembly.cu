@@ -1,8 +1,10 @@
 // Deterministic, atomic-free global assembly on sm_103a.
 //
-// The global tangent is CSR over 3x3 node blocks (rows = nodes), values kept
-// as nine structure-of-arrays planes vals[k*stride + blk] so a warp reading
-// consecutive blocks of a row issues unit-stride loads.  Every block gathers
+// The global tangent is CSR over 3x3 node blocks (rows = nodes).  Values live
+// in tile-contiguous storage: each row tile of the streamed product holds its
+// row pointers, column indices and nine value planes (entry k of every block)
+// in one contiguous range, so a warp writing consecutive blocks of a row
+// issues unit-stride stores and the product streams the matrix sequentially.  Every block gathers
 // its element contributions through the destination-sorted map built on the
 // host (ascending element order), so the sum order is fixed and the result is
 // bitwise repeatable.  Rows of prescribed dofs are zeroed; restricted to the
@@ -24,13 +26,20 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
                                                        const int* __restrict__ col,
                                                        const int* __restrict__ cptr,
                                                        const int* __restrict__ contrib, const T* __restrict__ Ke,
-                                                       const uint8_t* __restrict__ mask, T* __restrict__ vals,
-                                                       long long stride, T* __restrict__ minv) {
+                                                       const uint8_t* __restrict__ mask, unsigned char* __restrict__ blob,
+                                                       const long long* __restrict__ blob_off,
+                                                       const int* __restrict__ row_tile, T* __restrict__ minv) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nnd; I += warps) {
     const uint8_t mI = mask[I];
     const int r0 = rowptr[I], r1 = rowptr[I + 1];
+    // this row's value planes in its tile of the tile-contiguous storage
+    unsigned char* base = blob + blob_off[row_tile[I]];
+    const int* hdr = reinterpret_cast<const int*>(base);
+    const int trow0 = hdr[0], tnrows = hdr[1], tnb = hdr[2], ps = hdr[3];
+    T* planes = reinterpret_cast<T*>(base + 16 + 4 * ceil4(tnrows + 1) + 4 * ceil4(tnb));
+    const int tb0 = rowptr[trow0];
     for (int j = r0 + lane; j < r1; j += 32) {
       T acc[9];
 #pragma unroll
@@ -62,7 +71,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
 #pragma unroll
           for (int q = 0; q < 3; ++q) acc[p * 3 + q] = T(0);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) vals[k * stride + j] = acc[k];
+      for (int k = 0; k < 9; ++k) planes[(long long)k * ps + (j - tb0)] = acc[k];
       if (J == I) {
         // (block-)Jacobi inverse of the diagonal block; inactive dofs get
         // identity in the inverse's input and zero in its output.
@@ -118,15 +127,18 @@ __global__ void set_prescribed_kernel(int n, const int* __restrict__ idx, const 
   p[d] = val[k];
 }
 
+// u += du / scale (the PCG ran on a scaled right-hand side)
 template <typename V>
-__global__ void apply_update_kernel(int nnd, const V* __restrict__ du, double4_32a* __restrict__ u) {
+__global__ void apply_update_kernel(int nnd, const V* __restrict__ du, const PcgScalars* __restrict__ sc,
+                                    double4_32a* __restrict__ u) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nnd) return;
+  const double us = sc->unscale;
   const V d = du[n];
   double4_32a x = u[n];
-  x.x += (double)d.x;
-  x.y += (double)d.y;
-  x.z += (double)d.z;
+  x.x += us * (double)d.x;
+  x.y += us * (double)d.y;
+  x.z += us * (double)d.z;
   u[n] = x;
 }
 
@@ -153,12 +165,12 @@ int launch_assemble(Context* c, int precision) {
   grid = std::min(grid, kNumSMs * 16);
   if (precision == TG_MIXED)
     assemble_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_contrib_ptr,
-                                                        c->d_contrib, c->d_Ke32, c->d_mask, c->d_vals32,
-                                                        c->nnzb_pad, c->d_minv32);
+                                                        c->d_contrib, c->d_Ke32, c->d_mask, c->d_blob32,
+                                                        c->d_blob_off32, c->d_row_tile, c->d_minv32);
   else
     assemble_kernel<double><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_contrib_ptr,
-                                                         c->d_contrib, c->d_Ke64, c->d_mask, c->d_vals64,
-                                                         c->nnzb_pad, c->d_minv64);
+                                                         c->d_contrib, c->d_Ke64, c->d_mask, c->d_blob64,
+                                                         c->d_blob_off64, c->d_row_tile, c->d_minv64);
   c->launches++;
   return ok(c, cudaGetLastError(), "assemble_kernel") ? TG_OK : TG_ERR_CUDA;
 }
@@ -173,9 +185,9 @@ int launch_set_prescribed(Context* c, int n, const int* d_idx, const double* d_v
 int launch_apply_update(Context* c) {
   const int grid = (c->nnd + 255) / 256;
   if (c->pcg_vec_precision == TG_MIXED)
-    apply_update_kernel<float4><<<grid, 256, 0, c->stream>>>(c->nnd, (const float4*)c->d_x, c->d_u);
+    apply_update_kernel<float4><<<grid, 256, 0, c->stream>>>(c->nnd, (const float4*)c->d_x, c->d_pcg, c->d_u);
   else
-    apply_update_kernel<double4_32a><<<grid, 256, 0, c->stream>>>(c->nnd, (const double4_32a*)c->d_x, c->d_u);
+    apply_update_kernel<double4_32a><<<grid, 256, 0, c->stream>>>(c->nnd, (const double4_32a*)c->d_x, c->d_pcg, c->d_u);
   c->launches++;
   return ok(c, cudaGetLastError(), "apply_update_kernel") ? TG_OK : TG_ERR_CUDA;
 }

@@ -1,10 +1,12 @@
 // (Block-)Jacobi preconditioned CG on the node-block CSR matrix, sm_103a.
 //
 // Each iteration is two kernels:
-//   pcg_spmv_kernel   w = A z; q = w + beta q; p = z + beta p; partial p.q
-//                     (uses A p = A z + beta A p_old, so the product runs on z,
-//                     which is complete when the kernel starts)
-//   pcg_update_kernel x += alpha p; r -= alpha q; z = M^-1 r; partial r.z, r.r
+//   pcg_spmv_kernel   p_new = z + beta p_old formed on the fly at every
+//                     gathered node, q = A p_new, partial p_new.q (the
+//                     product is exact each iteration; p is double-buffered
+//                     and the buffers alternate between iterations)
+//   pcg_update_kernel x += alpha p_new; r -= alpha q; z = M^-1 r; partial
+//                     r.z, r.r
 // Both end in a last-block-done reduction of their FP64 partial sums in a
 // fixed order (bitwise repeatable, no floating-point atomics) that also
 // computes alpha / beta and the convergence flag on the device.  Iterations
@@ -42,57 +44,101 @@ __device__ __forceinline__ V mk(T x, T y, T z) {
   return v;
 }
 
-// block-wide sum of `nv` doubles; results valid in thread 0
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double* sh /* NV*32 */) {
+// Dot-product accumulators.  GB300 issues an FP64 warp instruction at a
+// small fraction of the FP32 rate, so in the FP32 form the per-element
+// products are accumulated as compensated FP32 pairs (hi + lo, error-free
+// two-product and two-sum, about 48 significant bits) and only the per-block
+// totals are converted to FP64 for the cross-block sum.  The FP64 form
+// accumulates in FP64 throughout.
+template <typename T>
+struct Acc;
+
+template <>
+struct Acc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float b) {  // Knuth two-sum, error into lo
+    const float s = __fadd_rn(hi, b);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+  }
+  __device__ __forceinline__ void add_prod(float x, float y) {  // exact product p + pe
+    const float p = __fmul_rn(x, y);
+    const float pe = __fmaf_rn(x, y, -p);
+    add(p);
+    lo = __fadd_rn(lo, pe);
+  }
+  __device__ __forceinline__ void merge(float ohi, float olo) {
+    add(ohi);
+    lo = __fadd_rn(lo, olo);
+  }
+  __device__ __forceinline__ void shfl_merge(int o) {
+    const float ohi = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float olo = __shfl_xor_sync(0xffffffffu, lo, o);
+    merge(ohi, olo);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double b) { s += b; }
+  __device__ __forceinline__ void add_prod(double x, double y) { s = fma(x, y, s); }
+  __device__ __forceinline__ void merge(double o, double) { s += o; }
+  __device__ __forceinline__ void shfl_merge(int o) { s += __shfl_xor_sync(0xffffffffu, s, o); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+// Block total of NV accumulators (fixed order), FP64 value on thread 0.
+template <typename T, int NV>
+__device__ __forceinline__ void block_total(Acc<T> (&v)[NV], double (&out)[NV]) {
+  __shared__ double sh[NV][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    for (int o = 16; o > 0; o >>= 1) v[k].shfl_merge(o);
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < NV; ++k) sh[k * 32 + w] = v[k];
+    for (int k = 0; k < NV; ++k) sh[k][w] = v[k].value();
   __syncthreads();
   if (w == 0) {
     const int nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      double x = lane < nw ? sh[k * 32 + lane] : 0.0;
+      double x = lane < nw ? sh[k][lane] : 0.0;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      v[k] = x;
+      out[k] = x;
     }
   }
+  __syncthreads();
 }
 
-// last-block reduction of per-block partials (layout partials[k*gridDim + b]);
-// returns true in the last block, with totals in `tot` on thread 0
-template <int NV>
-__device__ __forceinline__ bool last_block_total(double (&v)[NV], double* partials, unsigned int* counter,
+// Last-block reduction of per-block partials (partials[k*gridDim + b]) in
+// FP64 and a fixed order; true in the last block, totals on thread 0.
+template <typename T, int NV>
+__device__ __forceinline__ bool last_block_total(Acc<T> (&v)[NV], double* partials, unsigned int* counter,
                                                  double (&tot)[NV]) {
-  __shared__ double sh[NV * 32];
   __shared__ bool last;
-  block_sum<NV>(v, sh);
+  double bt[NV];
+  block_total<T, NV>(v, bt);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+    for (int k = 0; k < NV; ++k) partials[k * gridDim.x + blockIdx.x] = bt[k];
     __threadfence();
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  double acc[NV];
+  Acc<double> acc[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    acc[k] = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc[k] += ((volatile double*)partials)[k * gridDim.x + b];
-  }
-  __syncthreads();
-  block_sum<NV>(acc, sh);
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = acc[k];
+  for (int k = 0; k < NV; ++k)
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc[k].add(((volatile double*)partials)[k * gridDim.x + b]);
+  block_total<double, NV>(acc, tot);
   if (threadIdx.x == 0) *counter = 0u;
   return true;
 }
@@ -105,31 +151,66 @@ __device__ __forceinline__ void apply_minv(const T* __restrict__ minv, int n, T 
   zz = B[6] * rx + B[7] * ry + B[8] * rz;
 }
 
+// FP64 pre-pass: s = b.M^-1.b over active dofs; the solve then runs on
+// b/sqrt(s) so the FP32 iterates stay O(1) whatever the residual magnitude
+// (late Newton residuals sit at FP64 round-off, far below FP32 range when
+// squared).
+template <typename T>
+__global__ void __launch_bounds__(256) pcg_scale_kernel(int nnd, const double4_32a* __restrict__ rhs,
+                                                        const uint8_t* __restrict__ mask, const T* __restrict__ minv,
+                                                        double* partials, PcgScalars* sc) {
+  Acc<double> v[1];
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gridDim.x * blockDim.x) {
+    const double4_32a b = rhs[n];
+    const uint8_t m = mask[n];
+    const double bx = (m & 1) ? b.x : 0.0, by = (m & 2) ? b.y : 0.0, bz = (m & 4) ? b.z : 0.0;
+    const T* B = minv + (long long)n * 9;
+    const double zx = (double)B[0] * bx + (double)B[1] * by + (double)B[2] * bz;
+    const double zy = (double)B[3] * bx + (double)B[4] * by + (double)B[5] * bz;
+    const double zz = (double)B[6] * bx + (double)B[7] * by + (double)B[8] * bz;
+    v[0].add(bx * zx + by * zy + bz * zz);
+  }
+  double tot[1];
+  if (last_block_total<double, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
+    const double s = tot[0];
+    const double sc_ = (s > 0.0 && isfinite(s)) ? 1.0 / sqrt(s) : 1.0;
+    sc->scale = sc_;
+    sc->unscale = 1.0 / sc_;
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32a* __restrict__ rhs,
                                                        const uint8_t* __restrict__ mask, const T* __restrict__ minv,
                                                        typename Vec4<T>::type* x, typename Vec4<T>::type* r,
                                                        typename Vec4<T>::type* z, typename Vec4<T>::type* p,
-                                                       typename Vec4<T>::type* q, double* partials, PcgScalars* sc,
-                                                       double tol, int max_it) {
+                                                       typename Vec4<T>::type* p1, typename Vec4<T>::type* q,
+                                                       double* partials, PcgScalars* sc, double tol, int max_it) {
   using V = typename Vec4<T>::type;
-  double v[2] = {0.0, 0.0};
+  Acc<T> v[2];
+  const double scale = sc->scale;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gridDim.x * blockDim.x) {
     const double4_32a b = rhs[n];
     const uint8_t mk_ = mask[n];
-    const T rx = (mk_ & 1) ? T(b.x) : T(0), ry = (mk_ & 2) ? T(b.y) : T(0), rz = (mk_ & 4) ? T(b.z) : T(0);
+    const T rx = (mk_ & 1) ? T(b.x * scale) : T(0), ry = (mk_ & 2) ? T(b.y * scale) : T(0),
+            rz = (mk_ & 4) ? T(b.z * scale) : T(0);
     T zx, zy, zz;
     apply_minv<T>(minv, n, rx, ry, rz, zx, zy, zz);
     x[n] = mk<V, T>(T(0), T(0), T(0));
     r[n] = mk<V, T>(rx, ry, rz);
     z[n] = mk<V, T>(zx, zy, zz);
     p[n] = mk<V, T>(T(0), T(0), T(0));
+    p1[n] = mk<V, T>(T(0), T(0), T(0));
     q[n] = mk<V, T>(T(0), T(0), T(0));
-    v[0] += (double)rx * zx + (double)ry * zy + (double)rz * zz;
-    v[1] += (double)rx * rx + (double)ry * ry + (double)rz * rz;
+    v[0].add_prod(rx, zx);
+    v[0].add_prod(ry, zy);
+    v[0].add_prod(rz, zz);
+    v[1].add_prod(rx, rx);
+    v[1].add_prod(ry, ry);
+    v[1].add_prod(rz, rz);
   }
   double tot[2];
-  if (last_block_total<2>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
+  if (last_block_total<T, 2>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
     sc->rz = tot[0];
     sc->rr = tot[1];
     sc->rr0 = tot[1];
@@ -145,46 +226,165 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) pcg_spmv_kernel(int nnd, const int* __restrict__ rowptr,
-                                                       const int* __restrict__ col, const T* __restrict__ vals,
-                                                       long long stride, const typename Vec4<T>::type* __restrict__ z,
-                                                       typename Vec4<T>::type* __restrict__ p,
+// ---- bulk-copy (TMA) staging of the streamed matrix ----------------------
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ready;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ready)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ready != 0;
+}
+// Bounded wait: gives up after `limit` polls (the caller records the timeout).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_copy(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst_smem)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+constexpr int kWaitLimit = 1 << 18;  // polls before a staged tile is declared lost
+
+// q = A p_new with p_new = z + beta p_old formed at every gathered node, on a
+// persistent grid.  Each CTA streams its row tiles through a ring of NST
+// shared-memory stages: one bulk copy per tile (the tile-contiguous storage
+// makes a tile one range), completing on the stage's mbarrier, is issued
+// NST-1 tiles ahead while the CTA's warps compute the current tile: 8 lanes
+// per row, 4 rows per warp at a time, each lane over every 8th block.  Every
+// wait is bounded; a timeout sets an error flag, drains the copies in flight
+// (bounded) and marks the solve broken down.
+template <typename T, int NST>
+__global__ void __launch_bounds__(256) pcg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off,
+                                                       const unsigned char* __restrict__ blob, int cap,
+                                                       const typename Vec4<T>::type* __restrict__ z,
+                                                       const typename Vec4<T>::type* __restrict__ pold,
+                                                       typename Vec4<T>::type* __restrict__ pnew,
                                                        typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                       PcgScalars* sc) {
+                                                       PcgScalars* sc, int* status) {
   using V = typename Vec4<T>::type;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[NST];
+  __shared__ int abort_flag;
   if (((volatile PcgScalars*)sc)->done) return;
   const T beta = T(sc->beta);
-  const int lane = threadIdx.x & 31;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  double v[1] = {0.0};
-  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nnd; I += warps) {
-    T a0 = T(0), a1 = T(0), a2 = T(0);
-    const int r1 = rowptr[I + 1];
-    for (int j = rowptr[I] + lane; j < r1; j += 32) {
-      const V zj = z[col[j]];
-      a0 += vals[0 * stride + j] * zj.x + vals[1 * stride + j] * zj.y + vals[2 * stride + j] * zj.z;
-      a1 += vals[3 * stride + j] * zj.x + vals[4 * stride + j] * zj.y + vals[5 * stride + j] * zj.z;
-      a2 += vals[6 * stride + j] * zj.x + vals[7 * stride + j] * zj.y + vals[8 * stride + j] * zj.z;
-    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    for (int k = 0; k < NST; ++k) mbar_init(&bars[k], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  Acc<T> v[1];
+  const int t0 = blockIdx.x, G = gridDim.x;
+  auto issue = [&](int t, int stage) {
+    const long long o0 = blob_off[t], o1 = blob_off[t + 1];
+    const unsigned bytes = (unsigned)(o1 - o0);
+    mbar_expect_tx(&bars[stage], bytes);
+    bulk_copy(smem + (size_t)stage * cap, blob + o0, bytes, &bars[stage]);
+  };
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NST - 1; ++k)
+      if (t0 + k * G < ntiles) issue(t0 + k * G, k);
+  unsigned phases = 0u;  // bit k: parity of stage k's next completion
+  int stuck = -1;
+  int it = 0;
+  const int sub = lane & 7;
+  for (int t = t0; t < ntiles; ++it, t += G) {
+    const int s = it % NST;
+    const int tn = t + (NST - 1) * G;
+    if (threadIdx.x == 0 && tn < ntiles) {
+      fence_async_smem();  // the stage was last read through generic loads
+      issue(tn, (it + NST - 1) % NST);
     }
-    if (lane == 0) {
-      const V zi = z[I], pi = p[I], qi = q[I];
-      const V qn = mk<V, T>(a0 + beta * qi.x, a1 + beta * qi.y, a2 + beta * qi.z);
-      const V pn = mk<V, T>(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z);
-      q[I] = qn;
-      p[I] = pn;
-      v[0] += (double)pn.x * qn.x + (double)pn.y * qn.y + (double)pn.z * qn.z;
+    if (!mbar_wait(&bars[s], (phases >> s) & 1u, kWaitLimit)) {
+      if (lane == 0) atomicOr(&abort_flag, 1);
     }
+    phases ^= 1u << s;
+    __syncthreads();
+    if (abort_flag) {
+      stuck = s;
+      break;
+    }
+    const unsigned char* base = smem + (size_t)s * cap;
+    const int* hdr = reinterpret_cast<const int*>(base);
+    const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
+    const int* rp = hdr + 4;
+    const int* cl = rp + ceil4(nrows + 1);
+    const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
+    for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
+      const bool live = li < nrows;
+      const int I = r0 + li;
+      V zi, pi;
+      if (live && sub == 0) {
+        zi = z[I];
+        pi = pold[I];
+      }
+      T a0 = T(0), a1 = T(0), a2 = T(0);
+      const int e0 = live ? rp[li] : 0;
+      const int e1 = live ? rp[li + 1] : 0;
+#pragma unroll 4
+      for (int j = e0 + sub; j < e1; j += 8) {
+        const int J = cl[j];
+        const T* vv = pl + j;
+        const V zj = z[J], pj = pold[J];
+        const T x = zj.x + beta * pj.x, y = zj.y + beta * pj.y, w = zj.z + beta * pj.z;
+        a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
+        a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
+        a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
+      }
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      }
+      if (live && sub == 0) {
+        const V pn = mk<V, T>(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z);
+        q[I] = mk<V, T>(a0, a1, a2);
+        pnew[I] = pn;
+        v[0].add_prod(pn.x, a0);
+        v[0].add_prod(pn.y, a1);
+        v[0].add_prod(pn.z, a2);
+      }
+    }
+    __syncthreads();  // stage s is free for the copy issued next iteration
+  }
+  if (stuck >= 0 && threadIdx.x == 0) {
+    // a staged tile never completed: record it, drain the copies still in
+    // flight (bounded waits) and leave the solve flagged as broken down
+    atomicOr(status, kStatusWaitTimeout);
+    for (int k = 0; k < NST; ++k) {
+      const unsigned parity = ((phases >> k) & 1u) ^ (k == stuck ? 1u : 0u);
+      mbar_wait(&bars[k], parity, kWaitLimit);  // bounded even when nothing is pending
+    }
+    sc->done = 2;
+    sc->fail = 5;
   }
   double tot[1];
-  if (last_block_total<1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
+  if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
+    if (sc->done == 2) return;
     if (!(tot[0] > 0.0) || !isfinite(tot[0])) {
       sc->done = 2;
       sc->fail = isfinite(tot[0]) ? 2 : 3;
@@ -205,7 +405,7 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __res
   using V = typename Vec4<T>::type;
   if (((volatile PcgScalars*)sc)->done) return;
   const T alpha = T(sc->alpha);
-  double v[2] = {0.0, 0.0};
+  Acc<T> v[2];
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gridDim.x * blockDim.x) {
     const V pn = p[n], qn = q[n];
     V xn = x[n], rn = r[n];
@@ -220,11 +420,15 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __res
     x[n] = xn;
     r[n] = rn;
     z[n] = mk<V, T>(zx, zy, zz);
-    v[0] += (double)rn.x * zx + (double)rn.y * zy + (double)rn.z * zz;
-    v[1] += (double)rn.x * rn.x + (double)rn.y * rn.y + (double)rn.z * rn.z;
+    v[0].add_prod(rn.x, zx);
+    v[0].add_prod(rn.y, zy);
+    v[0].add_prod(rn.z, zz);
+    v[1].add_prod(rn.x, rn.x);
+    v[1].add_prod(rn.y, rn.y);
+    v[1].add_prod(rn.z, rn.z);
   }
   double tot[2];
-  if (last_block_total<2>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
+  if (last_block_total<T, 2>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
     const int it = sc->iters + 1;
     sc->iters = it;
     sc->beta = tot[0] / sc->rz;
@@ -241,26 +445,89 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __res
 
 struct Grids {
   int spmv, vec;
+  size_t spmv_smem;
+  int stages;
 };
+
+// persistent grid for the streamed SpMV: as many CTAs as fit (shared memory
+// bound), at most one per tile
+template <typename T>
+int blob_cap(const Context* c) {
+  return (int)(((std::is_same<T, float>::value ? c->blob_cap32 : c->blob_cap64) + 127) / 128 * 128);
+}
+template <typename T, int NST>
+int spmv_config_n(Context* c, Grids& g) {
+  g.spmv_smem = (size_t)NST * blob_cap<T>(c);
+  int optin = 0;
+  if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
+    return TG_ERR_CUDA;
+  if (g.spmv_smem + 1024 > (size_t)optin) {
+    c->err = "SpMV tile ring does not fit in shared memory (reduce tile_blocks or stages)";
+    return TG_ERR_CAPACITY;
+  }
+  if (!ok(c, cudaFuncSetAttribute(pcg_spmv_kernel<T, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)g.spmv_smem), "smem attribute"))
+    return TG_ERR_CUDA;
+  int per_sm = 0;
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_spmv_kernel<T, NST>, 256, g.spmv_smem),
+          "occupancy"))
+    return TG_ERR_CUDA;
+  if (per_sm < 1) {
+    c->err = "SpMV tile does not fit in shared memory";
+    return TG_ERR_CAPACITY;
+  }
+  g.spmv = std::max(1, std::min(c->ntiles, kNumSMs * per_sm));
+  return TG_OK;
+}
+template <typename T>
+int spmv_config(Context* c, Grids& g) {
+  // the configured ring depth, or 8 stages when 16 do not fit (FP64 tiles)
+  int optin = 0;
+  if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
+    return TG_ERR_CUDA;
+  g.stages = c->spmv_stages;
+  if (g.stages == 3 && 3 * (size_t)blob_cap<T>(c) + 1024 > (size_t)optin) g.stages = 2;
+  return g.stages == 3 ? spmv_config_n<T, 3>(c, g) : spmv_config_n<T, 2>(c, g);
+}
+template <typename T>
+void launch_spmv(Context* c, const Grids& g, const void* z, const void* pold, void* pnew) {
+  using V = typename Vec4<T>::type;
+  const bool f32 = std::is_same<T, float>::value;
+  const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
+  const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
+  const int cap = blob_cap<T>(c);
+  if (g.stages == 3)
+    pcg_spmv_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, (const V*)z,
+                                                                   (const V*)pold, (V*)pnew, (V*)c->d_q,
+                                                                   c->d_partials, c->d_pcg, c->d_status);
+  else
+    pcg_spmv_kernel<T, 2><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, (const V*)z,
+                                                                   (const V*)pold, (V*)pnew, (V*)c->d_q,
+                                                                   c->d_partials, c->d_pcg, c->d_status);
+}
 Grids grids(const Context* c) {
   Grids g;
-  g.spmv = std::min((c->nnd + 7) / 8, kNumSMs * 8);
-  g.vec = std::min((c->nnd + 255) / 256, kNumSMs * 8);
+  g.spmv = 0;
+  g.spmv_smem = 0;
+  g.stages = 8;
+  g.vec = std::min((c->nnd + 255) / 256, kNumSMs * 2);
   return g;
 }
 
 template <typename T>
 int capture_chunk(Context* c, const T* minv) {
   using V = typename Vec4<T>::type;
-  const Grids g = grids(c);
-  const T* vals = std::is_same<T, float>::value ? (const T*)c->d_vals32 : (const T*)c->d_vals64;
+  Grids g = grids(c);
+  if (spmv_config<T>(c, g)) return TG_ERR_CUDA;
   cudaGraph_t graph;
   if (!ok(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return TG_ERR_CUDA;
+  static_assert(kChunk % 2 == 0, "p buffers alternate within a chunk");
   for (int k = 0; k < kChunk; ++k) {
-    pcg_spmv_kernel<T><<<g.spmv, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, vals, c->nnzb_pad,
-                                                     (const V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials, c->d_pcg);
-    pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z,
-                                                      (const V*)c->d_p, (const V*)c->d_q, c->d_partials, c->d_pcg);
+    V* pold = (V*)(k % 2 == 0 ? c->d_p : c->d_p1);
+    V* pnew = (V*)(k % 2 == 0 ? c->d_p1 : c->d_p);
+    launch_spmv<T>(c, g, c->d_z, pold, pnew);
+    pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z, pnew,
+                                                      (const V*)c->d_q, c->d_partials, c->d_pcg);
   }
   if (!ok(c, cudaStreamEndCapture(c->stream, &graph), "end capture")) return TG_ERR_CUDA;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
@@ -274,7 +541,7 @@ template <typename T>
 int ensure_vectors(Context* c, int precision) {
   using V = typename Vec4<T>::type;
   if (c->pcg_vec_precision == precision) return TG_OK;
-  for (void** pp : {&c->d_x, &c->d_r, &c->d_z, &c->d_p, &c->d_q}) {
+  for (void** pp : {&c->d_x, &c->d_r, &c->d_z, &c->d_p, &c->d_p1, &c->d_q}) {
     if (*pp) dfree(c, *pp);
     V* v = nullptr;
     if (!dalloc(c, &v, (size_t)c->nnd)) return TG_ERR_OOM;
@@ -300,9 +567,11 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
   const T* minv = minv_base + (precond == TG_PRECOND_BLOCK_JACOBI ? (long long)c->nnd * 9 : 0);
   const int key = precision * 2 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0);
   const Grids g = grids(c);
+  pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, d_rhs, c->d_mask, minv, c->d_partials, c->d_pcg);
+  c->launches++;
   pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, d_rhs, c->d_mask, minv, (V*)c->d_x, (V*)c->d_r,
-                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials, c->d_pcg,
-                                                  rel_tol, max_it);
+                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_p1, (V*)c->d_q, c->d_partials,
+                                                  c->d_pcg, rel_tol, max_it);
   c->launches++;
   if (!ok(c, cudaGetLastError(), "pcg_init_kernel")) return TG_ERR_CUDA;
   if (c->pcg_graph_key != key || !c->pcg_graph) {
@@ -326,8 +595,8 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
   if (h.done == 1) return TG_OK;
   if (h.done == 2) {
     static const char* why[] = {"", "non-finite initial residual", "p.Ap <= 0 (indefinite operator)",
-                                "non-finite p.Ap", "non-finite r.z or r.r"};
-    c->err = std::string("PCG breakdown: ") + why[h.fail >= 1 && h.fail <= 4 ? h.fail : 0] + " at iteration " +
+                                "non-finite p.Ap", "non-finite r.z or r.r", "staged tile wait timed out"};
+    c->err = std::string("PCG breakdown: ") + why[h.fail >= 1 && h.fail <= 5 ? h.fail : 0] + " at iteration " +
              std::to_string(h.iters);
     return TG_ERR_NAN;
   }
@@ -339,19 +608,28 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
 // in R), accumulated in FP64 whatever the matrix precision
 template <typename T>
 __global__ void __launch_bounds__(256) lift_rhs_kernel(int nnd, const int* __restrict__ rowptr,
-                                                       const int* __restrict__ col, const T* __restrict__ vals,
-                                                       long long stride, const double4_32a* __restrict__ v,
+                                                       const int* __restrict__ row_tile,
+                                                       const long long* __restrict__ blob_off,
+                                                       const unsigned char* __restrict__ blob,
+                                                       const double4_32a* __restrict__ v,
                                                        const double4_32a* __restrict__ R, double4_32a* __restrict__ rhs) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nnd; I += warps) {
+    const unsigned char* base = blob + blob_off[row_tile[I]];
+    const int* hdr = reinterpret_cast<const int*>(base);
+    const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
+    const int* rp = hdr + 4;
+    const int* cl = rp + ceil4(nrows + 1);
+    const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    const int r1 = rowptr[I + 1];
-    for (int j = rowptr[I] + lane; j < r1; j += 32) {
-      const double4_32a vj = v[col[j]];
-      a0 += (double)vals[0 * stride + j] * vj.x + (double)vals[1 * stride + j] * vj.y + (double)vals[2 * stride + j] * vj.z;
-      a1 += (double)vals[3 * stride + j] * vj.x + (double)vals[4 * stride + j] * vj.y + (double)vals[5 * stride + j] * vj.z;
-      a2 += (double)vals[6 * stride + j] * vj.x + (double)vals[7 * stride + j] * vj.y + (double)vals[8 * stride + j] * vj.z;
+    const int e1 = rp[I - r0 + 1];
+    for (int j = rp[I - r0] + lane; j < e1; j += 32) {
+      const double4_32a vj = v[cl[j]];
+      const T* vv = pl + j;
+      a0 += (double)vv[0 * ps] * vj.x + (double)vv[1 * ps] * vj.y + (double)vv[2 * ps] * vj.z;
+      a1 += (double)vv[3 * ps] * vj.x + (double)vv[4 * ps] * vj.y + (double)vv[5 * ps] * vj.z;
+      a2 += (double)vv[6 * ps] * vj.x + (double)vv[7 * ps] * vj.y + (double)vv[8 * ps] * vj.z;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -376,25 +654,26 @@ __global__ void diff_kernel(int nnd, const double4_32a* __restrict__ a, const do
 
 template <typename V>
 __global__ void gather_solution_kernel(int neq, const int* __restrict__ slot, const V* __restrict__ x,
-                                       double* __restrict__ eq) {
+                                       const PcgScalars* __restrict__ sc, double* __restrict__ eq) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= neq) return;
   const int s = slot[k];
   const V v = x[s >> 2];
   const int d = s & 3;
-  eq[k] = (double)(d == 0 ? v.x : (d == 1 ? v.y : v.z));
+  eq[k] = sc->unscale * (double)(d == 0 ? v.x : (d == 1 ? v.y : v.z));
 }
 
 }  // namespace
 
 int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs) {
-  const Grids g = grids(c);
+  Grids g = grids(c);
+  g.spmv = std::min((c->nnd + 7) / 8, kNumSMs * 8);
   if (c->tangent_precision == TG_MIXED)
-    lift_rhs_kernel<float><<<g.spmv, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_vals32, c->nnzb_pad,
-                                                         d_v, c->d_R, d_rhs);
+    lift_rhs_kernel<float><<<g.spmv, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_row_tile, c->d_blob_off32,
+                                                         c->d_blob32, d_v, c->d_R, d_rhs);
   else
-    lift_rhs_kernel<double><<<g.spmv, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_vals64, c->nnzb_pad,
-                                                          d_v, c->d_R, d_rhs);
+    lift_rhs_kernel<double><<<g.spmv, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_row_tile, c->d_blob_off64,
+                                                          c->d_blob64, d_v, c->d_R, d_rhs);
   c->launches++;
   return ok(c, cudaGetLastError(), "lift_rhs_kernel") ? TG_OK : TG_ERR_CUDA;
 }
@@ -409,9 +688,10 @@ int launch_gather_solution(Context* c, double* d_eq) {
   if (c->neq == 0) return TG_OK;
   const int grid = (c->neq + 255) / 256;
   if (c->pcg_vec_precision == TG_MIXED)
-    gather_solution_kernel<float4><<<grid, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, (const float4*)c->d_x, d_eq);
+    gather_solution_kernel<float4><<<grid, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, (const float4*)c->d_x, c->d_pcg, d_eq);
   else
-    gather_solution_kernel<double4_32a><<<grid, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, (const double4_32a*)c->d_x, d_eq);
+    gather_solution_kernel<double4_32a><<<grid, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, (const double4_32a*)c->d_x, c->d_pcg,
+                                                                      d_eq);
   c->launches++;
   return ok(c, cudaGetLastError(), "gather_solution_kernel") ? TG_OK : TG_ERR_CUDA;
 }
@@ -426,11 +706,13 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
   int s = ensure_vectors<T>(c, precision);
   if (s) return s;
   const T* minv = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
-  const T* vals = std::is_same<T, float>::value ? (const T*)c->d_vals32 : (const T*)c->d_vals64;
-  const Grids g = grids(c);
+  Grids g = grids(c);
+  if (spmv_config<T>(c, g)) return TG_ERR_CUDA;
+  pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, c->d_R, c->d_mask, minv, c->d_partials, c->d_pcg);
+  c->launches++;
   pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, c->d_R, c->d_mask, minv, (V*)c->d_x, (V*)c->d_r,
-                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials, c->d_pcg,
-                                                  1e-30, 1 << 30);
+                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_p1, (V*)c->d_q, c->d_partials,
+                                                  c->d_pcg, 1e-30, 1 << 30);
   c->launches++;
   PcgScalars t;
   std::memset(&t, 0, sizeof(t));
@@ -444,12 +726,11 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
     cudaMemcpyAsync(c->d_pcg, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream);
     cudaEventRecord(a, c->stream);
     if (which == 0)
-      pcg_spmv_kernel<T><<<g.spmv, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, vals, c->nnzb_pad,
-                                                       (const V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials,
-                                                       c->d_pcg);
+      launch_spmv<T>(c, g, c->d_z, c->d_p, c->d_p1);
     else
       pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z,
-                                                        (const V*)c->d_p, (const V*)c->d_q, c->d_partials, c->d_pcg);
+                                                        (const V*)c->d_p1, (const V*)c->d_q, c->d_partials,
+                                                        c->d_pcg);
     cudaEventRecord(b, c->stream);
     c->launches++;
     cudaEventSynchronize(b);

@@ -83,12 +83,14 @@ int form_tangent(Context* c, int precision) {
   const size_t keN = (size_t)c->nel * kKeStride;
   if (precision == TG_MIXED) {
     if (!c->d_Ke32 && !dalloc(c, &c->d_Ke32, keN)) return TG_ERR_OOM;
-    if (!c->d_vals32 && !dalloc(c, &c->d_vals32, (size_t)c->nnzb_pad * 9)) return TG_ERR_OOM;
     if (!c->d_minv32 && !dalloc(c, &c->d_minv32, (size_t)c->nnd * 18)) return TG_ERR_OOM;
   } else {
     if (!c->d_Ke64 && !dalloc(c, &c->d_Ke64, keN)) return TG_ERR_OOM;
-    if (!c->d_vals64 && !dalloc(c, &c->d_vals64, (size_t)c->nnzb_pad * 9)) return TG_ERR_OOM;
     if (!c->d_minv64 && !dalloc(c, &c->d_minv64, (size_t)c->nnd * 18)) return TG_ERR_OOM;
+  }
+  {
+    const int sb = ensure_blob(c, precision);
+    if (sb) return sb;
   }
   int s = launch_tangent(c, precision);
   if (!s) s = launch_assemble(c, precision);
@@ -106,15 +108,26 @@ extern "C" {
 int tg_get_tangent_csr(tg_context* c, int upper_only, double* vals) {
   if (!c || !vals || c->tangent_precision < 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
-  const size_t n = (size_t)c->nnzb_pad * 9;
-  std::vector<double> hv(n);
-  if (c->tangent_precision == TG_MIXED) {
-    std::vector<float> hf(n);
-    if (!ok(c, cudaMemcpy(hf.data(), c->d_vals32, sizeof(float) * n, cudaMemcpyDeviceToHost), "vals")) return TG_ERR_CUDA;
-    for (size_t k = 0; k < n; ++k) hv[k] = hf[k];
-  } else if (!ok(c, cudaMemcpy(hv.data(), c->d_vals64, sizeof(double) * n, cudaMemcpyDeviceToHost), "vals")) {
+  // decode the tile-contiguous storage: tile t, local block jl, plane k
+  const bool f32 = c->tangent_precision == TG_MIXED;
+  const std::vector<long long>& off = f32 ? c->h_blob_off32 : c->h_blob_off64;
+  std::vector<unsigned char> h((size_t)off[c->ntiles]);
+  if (!ok(c, cudaMemcpy(h.data(), f32 ? c->d_blob32 : c->d_blob64, h.size(), cudaMemcpyDeviceToHost), "blob"))
     return TG_ERR_CUDA;
-  }
+  auto value = [&](int I, int k, int pq) -> double {
+    int t = 0;
+    {
+      const auto& tr = c->h_tile_row;
+      t = (int)(std::upper_bound(tr.begin(), tr.end(), I) - tr.begin()) - 1;
+    }
+    const unsigned char* base = h.data() + off[t];
+    const int* hdr = reinterpret_cast<const int*>(base);
+    const int nrows = hdr[1], nb = hdr[2], ps = hdr[3];
+    const int jl = k - c->h_rowptr[hdr[0]];
+    const unsigned char* planes = base + 16 + 4 * ceil4(nrows + 1) + 4 * ceil4(nb);
+    return f32 ? (double)reinterpret_cast<const float*>(planes)[(size_t)pq * ps + jl]
+               : reinterpret_cast<const double*>(planes)[(size_t)pq * ps + jl];
+  };
   const int* eq = c->h_eqnos.data();
   long long count = 0;
   for (int I = 0; I < c->nnd; ++I)
@@ -126,7 +139,7 @@ int tg_get_tangent_csr(tg_context* c, int upper_only, double* vals) {
         for (int q = 0; q < 3; ++q) {
           const int cc = eq[J * 3 + q];
           if (cc <= 0 || (upper_only && cc < r)) continue;
-          vals[count++] = hv[(size_t)(p * 3 + q) * c->nnzb_pad + k];
+          vals[count++] = value(I, k, p * 3 + q);
         }
       }
     }

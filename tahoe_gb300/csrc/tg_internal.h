@@ -19,7 +19,8 @@ constexpr int kKeBlock = 9;        // 3x3 block values
 constexpr int kKeStride = kSlots * kKeBlock;  // 324 values per element
 
 // Device status bits (set by kernels with atomicOr, never by trapping).
-enum : int { kStatusBadJacobian = 1, kStatusNaN = 2 };
+enum : int { kStatusBadJacobian = 1, kStatusNaN = 2, kStatusWaitTimeout = 4 };
+constexpr int kTileBlocks = 640;   // block nonzeros per streamed SpMV tile
 
 struct MatParams {
   int kind;
@@ -38,6 +39,8 @@ struct MatTable {
 // Scalars of one PCG solve, resident in device memory.
 struct PcgScalars {
   double rz, rz_old, rr, rr0, pq, alpha, beta, tol2;
+  double scale;    // rhs scaling applied before the solve (b.M^-1.b -> 1)
+  double unscale;  // 1/scale, applied to the solution
   int done;       // 1 converged, 2 breakdown / non-finite
   int iters;
   int max_it;
@@ -87,13 +90,30 @@ struct Context {
   // block CSR (3x3 node blocks)
   long long nnzb = 0;
   long long nnzb_pad = 0;       // SoA stride of the value arrays
-  int* d_rowptr = nullptr;      // nnd+1
-  int* d_col = nullptr;         // nnzb
+  int* d_rowptr = nullptr;      // nnd+1, padded to a multiple of 4 plus 4 (bulk copies)
+  int* d_col = nullptr;         // nnzb_pad (tail zero: bulk copies round up to 16 B)
+  // row tiles of the streamed SpMV: tile t covers rows [tile_row[t], tile_row[t+1])
+  int ntiles = 0;
+  int* d_tile_row = nullptr;
+  int spmv_tile_blocks = kTileBlocks;
+  int spmv_stages = 2;
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
   std::vector<int> h_rowptr, h_col;
-  float* d_vals32 = nullptr;    // 9*nnzb_pad
-  double* d_vals64 = nullptr;
+  // Tile-contiguous matrix storage ("blob", one per precision): tile t
+  // occupies bytes [blob_off[t], blob_off[t+1]) and holds a 16-byte header
+  // {first row, rows, blocks, plane stride}, the local row pointers, the
+  // column indices and the nine value planes, each part 16-byte aligned, so
+  // one bulk copy moves a whole tile and the product streams the matrix as
+  // one sequential range.
+  unsigned char* d_blob32 = nullptr;
+  unsigned char* d_blob64 = nullptr;
+  long long* d_blob_off32 = nullptr;  // ntiles+1
+  long long* d_blob_off64 = nullptr;
+  std::vector<long long> h_blob_off32, h_blob_off64;
+  long long blob_cap32 = 0, blob_cap64 = 0;  // largest tile, bytes
+  int* d_row_tile = nullptr;   // nnd: tile of each row
+  std::vector<int> h_tile_row;
   float* d_minv32 = nullptr;    // 18*nnd: Jacobi then block-Jacobi
   double* d_minv64 = nullptr;
   float* d_Ke32 = nullptr;      // nel*324
@@ -122,7 +142,8 @@ struct Context {
   void* d_x = nullptr;  // float4 or double4_32a per node (solution du)
   void* d_r = nullptr;
   void* d_z = nullptr;
-  void* d_p = nullptr;
+  void* d_p = nullptr;   // search direction, double-buffered with d_p1
+  void* d_p1 = nullptr;
   void* d_q = nullptr;
   int pcg_vec_precision = -1;
   PcgScalars* d_pcg = nullptr;
@@ -169,6 +190,15 @@ void dfree(Context* c, void* p);
 void build_block_pattern(int nnd, int nel, const int* conn, std::vector<int>& rowptr, std::vector<int>& col);
 void build_contrib_map(int nnd, int nel, const int* conn, const std::vector<int>& rowptr,
                        const std::vector<int>& col, std::vector<int>& cptr, std::vector<int>& contrib);
+int build_tiles(Context* c, int tile_blocks);
+int ensure_blob(Context* c, int precision);
+
+// blob geometry shared by host and device code
+__host__ __device__ inline int ceil4(int n) { return (n + 3) & ~3; }
+__host__ __device__ inline long long blob_tile_bytes(int nrows, int nb, int elem) {
+  const long long pstride = ((long long)nb * elem + 15) / 16 * 16 / elem;
+  return 16 + 4LL * ceil4(nrows + 1) + 4LL * ceil4(nb) + 9LL * pstride * elem;
+}
 void build_node_elem(int nnd, int nel, const int* conn, std::vector<int>& ptr, std::vector<int>& list);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----

@@ -76,6 +76,7 @@ _SIGS = {
     "tg_timer_start": (ctypes.c_int, [_vp]),
     "tg_timer_stop": (ctypes.c_int, [_vp, _dp]),
     "tg_time_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    "tg_spmv_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
 }
 
 _lib = None
@@ -305,6 +306,9 @@ class Context:
         ms = ctypes.c_double(0)
         self._chk(self.L.tg_timer_stop(self.h, ctypes.byref(ms)), "tg_timer_stop")
         return ms.value
+
+    def spmv_config(self, tile_blocks, stages):
+        self._chk(self.L.tg_spmv_config(self.h, int(tile_blocks), int(stages)), "tg_spmv_config")
 
     def time_kernel(self, which, reps):
         ms = ctypes.c_double(0)

@@ -65,9 +65,10 @@ def c3(nx=96, ny=96, nz=48, nsteps=40, add=None):
 def spmv_bytes(nnzb, nnd, s_val):
     """Algorithmic bytes of one fused PCG SpMV launch on the node-block CSR:
     nine values + one column index per block, row pointers, the gathered z
-    vector once, and p, q read + written (vectors padded to 4 lanes)."""
+    and p_old vectors once each, p_new and q written (vectors padded to 4
+    lanes)."""
     s_vec = 4 * s_val
-    return nnzb * (9 * s_val + 4) + (nnd + 1) * 4 + nnd * s_vec + 4 * nnd * s_vec
+    return nnzb * (9 * s_val + 4) + (nnd + 1) * 4 + 2 * nnd * s_vec + 2 * nnd * s_vec
 
 
 def assembly_bytes(nel, nnzb, nnd, s_val):
