@@ -42,6 +42,22 @@ NEWTON_TOL = 1e-8       # outer relative tolerance on the FP64 residual
 C2_PCG_ITERS_FP64 = None  # filled from the run when available
 
 
+def profiled_traffic(precision_mixed):
+    """DRAM bytes per SpMV launch from the committed ncu summary of this
+    workload (profiles/pcg_spmv_c2_64cubed.md), or None."""
+    if not precision_mixed:
+        return None
+    path = os.path.join(ROOT, "profiles", "pcg_spmv_c2_64cubed.md")
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    return int(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -274,7 +290,8 @@ def run_ours(args):
                       "assembly": round(t_asm, 4), "residual": round(t_res, 4)},
         "roofline": {"kernel": "pcg_spmv_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "algorithmic_bytes": int(bytes_spmv), "traffic": None},
+                     "algorithmic_bytes": int(bytes_spmv), "traffic": profiled_traffic(prec == lib.MIXED),
+                     "traffic_source": "ncu dram__bytes_read.sum+dram__bytes_write.sum, profiles/pcg_spmv_c2_64cubed.md"},
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/Newton iteration", "h2d_bytes_per_step": nnd * 32,
                 "d2h_bytes_per_step": nnd * 32},
         "gpu_launches": int(launches),
