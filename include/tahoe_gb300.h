@@ -146,6 +146,18 @@ int tg_pcg_solve(tg_context* ctx, const double* rhs, double* du, double rel_tol,
  * FieldT.cpp:531-563) */
 int tg_apply_update(tg_context* ctx);
 
+/* Same solve as tg_pcg_solve for callers that cannot allocate device memory
+ * (hosts that reserve all device memory up front, or whose request path must
+ * not enter the CUDA allocator).  No counterpart in the reference.  rhs and du
+ * are DEVICE pointers (neq doubles each).  Allocates nothing: work vectors,
+ * partial sums and scalars live in one static device array of 8 MiB held by
+ * every GPU that loads the library, which limits the mesh to 32,768 nodes
+ * (larger meshes get TG_ERR_CAPACITY).  The first call on a device looks up
+ * that array's address, so make it before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race. */
+int tg_pcg_solve_noalloc(tg_context* ctx, const double* rhs_device, double* du_device, double rel_tol, int max_it,
+                         int precond, int* iterations, double* rel_res);
+
 /* ---- history ------------------------------------------------------------ */
 
 /* J2 history update after a converged step / reset after a failed one

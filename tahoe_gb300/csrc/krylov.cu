@@ -751,6 +751,99 @@ int time_pcg_kernel(Context* c, int which, int reps, double* ms) {
   return TG_ERR_ARG;
 }
 
+// ---- PCG on caller-provided scratch (used by tg_pcg_solve_noalloc) ------
+namespace {
+
+template <typename T>
+int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
+                    int max_it, int precond, int* iters, double* rel_res) {
+  using V = typename Vec4<T>::type;
+  // scratch layout: scalars | partials | rhs (nodal FP64) | x r z p p1 q
+  unsigned char* cur = scratch;
+  PcgScalars* sc = reinterpret_cast<PcgScalars*>(cur);
+  cur += kScratchScalarBytes;
+  double* partials = reinterpret_cast<double*>(cur);
+  cur += kScratchPartialBytes;
+  double4_32a* rhs = reinterpret_cast<double4_32a*>(cur);
+  cur += sizeof(double4_32a) * (size_t)c->nnd;
+  V* vec[6];
+  for (int k = 0; k < 6; ++k) {
+    vec[k] = reinterpret_cast<V*>(cur);
+    cur += sizeof(V) * (size_t)c->nnd;
+  }
+  V *x = vec[0], *r = vec[1], *z = vec[2], *p = vec[3], *p1 = vec[4], *q = vec[5];
+  // what must start at zero: the scalars (last-block counters) and the nodal
+  // right-hand side (prescribed slots are never written by the scatter)
+  if (!ok(c, cudaMemsetAsync(sc, 0, sizeof(PcgScalars), c->stream), "memset") ||
+      !ok(c, cudaMemsetAsync(rhs, 0, sizeof(double4_32a) * (size_t)c->nnd, c->stream), "memset"))
+    return TG_ERR_CUDA;
+  int s = launch_scatter_eq(c, d_rhs_eq, rhs);
+  if (s) return s;
+  Grids g = grids(c);
+  s = spmv_config<T>(c, g);
+  if (s) return s;
+  const T* minv_base = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
+  const T* minv = minv_base + (precond == TG_PRECOND_BLOCK_JACOBI ? (long long)c->nnd * 9 : 0);
+  const bool f32 = std::is_same<T, float>::value;
+  const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
+  const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
+  const int cap = blob_cap<T>(c);
+  pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, rhs, c->d_mask, minv, partials, sc);
+  pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, rhs, c->d_mask, minv, x, r, z, p, p1, q, partials, sc,
+                                                  rel_tol, max_it);
+  c->launches += 2;
+  if (!ok(c, cudaGetLastError(), "pcg init")) return TG_ERR_CUDA;
+  const int max_chunks = max_it / kChunk + 2;
+  for (int ch = 0; ch < max_chunks; ++ch) {
+    for (int k = 0; k < kChunk; ++k) {
+      V* pold = k % 2 == 0 ? p : p1;
+      V* pnew = k % 2 == 0 ? p1 : p;
+      if (g.stages == 3)
+        pcg_spmv_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, z, pold, pnew, q,
+                                                                       partials, sc, c->d_status);
+      else
+        pcg_spmv_kernel<T, 2><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, z, pold, pnew, q,
+                                                                       partials, sc, c->d_status);
+      pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, x, r, z, pnew, q, partials, sc);
+    }
+    c->launches += 2 * kChunk;
+    if (!ok(c, cudaGetLastError(), "pcg chunk") ||
+        !ok(c, cudaMemcpyAsync(c->h_pcg, sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c->stream), "copy") ||
+        !ok(c, cudaStreamSynchronize(c->stream), "pcg sync"))
+      return TG_ERR_CUDA;
+    if (c->h_pcg->done) break;
+  }
+  const PcgScalars h = *c->h_pcg;
+  if (iters) *iters = h.iters;
+  if (rel_res) *rel_res = h.rr0 > 0 ? std::sqrt(h.rr / h.rr0) : 0.0;
+  if (h.done == 2) {
+    c->err = "PCG breakdown";
+    return TG_ERR_NAN;
+  }
+  if (c->neq > 0) {
+    gather_solution_kernel<V><<<(c->neq + 255) / 256, 256, 0, c->stream>>>(c->neq, c->d_eq_slot, x, sc, d_du_eq);
+    c->launches++;
+  }
+  if (!ok(c, cudaGetLastError(), "gather") || !ok(c, cudaStreamSynchronize(c->stream), "sync")) return TG_ERR_CUDA;
+  if (h.done == 1) return TG_OK;
+  c->err = "PCG iteration limit reached";
+  return TG_ERR_NOT_CONVERGED;
+}
+
+}  // namespace
+
+size_t pcg_scratch_bytes(const Context* c) {
+  const size_t v = c->tangent_precision == TG_MIXED ? sizeof(float4) : sizeof(double4_32a);
+  return kScratchScalarBytes + kScratchPartialBytes + (sizeof(double4_32a) + 6 * v) * (size_t)c->nnd;
+}
+
+int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
+                      int max_it, int precond, int* iters, double* rel_res) {
+  if (c->tangent_precision == TG_MIXED)
+    return solve_scratch_t<float>(c, d_rhs_eq, d_du_eq, scratch, rel_tol, max_it, precond, iters, rel_res);
+  return solve_scratch_t<double>(c, d_rhs_eq, d_du_eq, scratch, rel_tol, max_it, precond, iters, rel_res);
+}
+
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
               double* rel_res) {
   if (c->tangent_precision == TG_MIXED) return solve_t<float>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);

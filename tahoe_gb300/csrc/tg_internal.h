@@ -213,6 +213,12 @@ int launch_apply_update(Context* c);
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
               double* rel_res);
 int time_pcg_kernel(Context* c, int which, int reps, double* ms);
+// PCG with every work vector, partial sum and scalar in caller scratch
+constexpr size_t kScratchScalarBytes = 256;
+constexpr size_t kScratchPartialBytes = 32768;
+size_t pcg_scratch_bytes(const Context* c);
+int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
+                      int max_it, int precond, int* iters, double* rel_res);
 int launch_residual_nocommit(Context* c);
 // rhs = R - K v on active rows (v nodal, K the last tangent), FP64 accumulation
 int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs);

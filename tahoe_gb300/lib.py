@@ -63,6 +63,8 @@ _SIGS = {
     "tg_get_tangent_csr": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "tg_element_dump": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "tg_pcg_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, _ip, _dp]),
+    "tg_pcg_solve_noalloc": (ctypes.c_int, [_vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                            ctypes.c_int, _ip, _dp]),
     "tg_apply_update": (ctypes.c_int, [_vp]),
     "tg_close_step": (ctypes.c_int, [_vp]),
     "tg_reset_step": (ctypes.c_int, [_vp]),
@@ -244,6 +246,18 @@ class Context:
         if rc not in (TG_OK, -6):
             self._chk(rc, "tg_pcg_solve")
         return du, its.value, rr.value, rc
+
+    def pcg_noalloc(self, rhs_device_ptr, du_device_ptr, rel_tol=1e-10, max_it=10000, precond=PRECOND_JACOBI):
+        """tg_pcg_solve_noalloc on caller-owned device buffers (raw pointers);
+        returns (iterations, relative residual, status)."""
+        its = ctypes.c_int(0)
+        rr = ctypes.c_double(0)
+        rc = self.L.tg_pcg_solve_noalloc(self.h, ctypes.c_void_p(rhs_device_ptr), ctypes.c_void_p(du_device_ptr),
+                                         float(rel_tol), int(max_it), int(precond), ctypes.byref(its),
+                                         ctypes.byref(rr))
+        if rc not in (TG_OK, -6):
+            self._chk(rc, "tg_pcg_solve_noalloc")
+        return its.value, rr.value, rc
 
     def apply_update(self):
         self._chk(self.L.tg_apply_update(self.h), "tg_apply_update")
