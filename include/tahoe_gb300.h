@@ -220,6 +220,28 @@ int tg_rollback(tg_context* ctx);
  * as in SolverT::InitStep.  Does not close the step. */
 int tg_newton_solve(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report);
 
+/* ---- batched FE^2 micro-solves ------------------------------------------ */
+
+/* A batch of independent RVEs uploaded as one disconnected mesh: RVE r owns
+ * nodes [node_off[r], node_off[r+1]) and elements [elem_off[r],
+ * elem_off[r+1]) (nseg+1 entries each, host arrays).  No reference
+ * counterpart: the reference has no FE^2 driver; each RVE is an ordinary
+ * element group with affine prescribed boundary displacement
+ * (MappedPeriodicT / kinematic_BC). */
+int tg_set_segments(tg_context* ctx, int nseg, const int* node_off, const int* elem_off);
+/* ||R_r||_2 of the last residual restricted to each RVE (nseg doubles) */
+int tg_segment_residual_norms(tg_context* ctx, double* norms);
+/* volume-averaged first Piola stress of each RVE from the last residual
+ * evaluation: P_r = (1/V0_r) sum over its element nodes of fint (x) X, equal
+ * at equilibrium to the reaction sum sum_{boundary a} f_a (x) X_a; P is
+ * nseg*9 row-major (P_iJ), vol0 the reference volumes (NULL: no division) */
+int tg_segment_average_stress(tg_context* ctx, const double* vol0, double* P);
+/* Newton over the whole batch with NLSolver's exit test applied to every RVE
+ * (relative to that RVE's first residual); iterates until all converge.
+ * seg_rel (nseg, may be NULL) receives each RVE's final relative residual. */
+int tg_newton_solve_segmented(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report,
+                              double* seg_rel);
+
 /* ---- measurement and tuning helpers (no reference counterpart) ---------- */
 
 /* Shape of the streamed PCG matrix product: row tiles of at most tile_blocks

@@ -167,6 +167,9 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
   c->d_blob32 = c->d_blob64 = nullptr;
+  c->nseg = 0;
+  c->d_seg_node = c->d_seg_elem = nullptr;
+  c->d_seg_out = nullptr;
   c->d_blob_off32 = c->d_blob_off64 = nullptr;
   c->d_row_tile = nullptr;
   c->d_minv32 = nullptr;
@@ -313,24 +316,10 @@ int ensure_blob(Context* c, int precision) {
   unsigned char** blob = precision == TG_MIXED ? &c->d_blob32 : &c->d_blob64;
   if (*blob) return TG_OK;
   const std::vector<long long>& off = precision == TG_MIXED ? c->h_blob_off32 : c->h_blob_off64;
-  const int elem = precision == TG_MIXED ? 4 : 8;
   const long long total = off[c->ntiles];
-  std::vector<unsigned char> h((size_t)total, 0);
-  for (int t = 0; t < c->ntiles; ++t) {
-    const int r0 = c->h_tile_row[t], r1 = c->h_tile_row[t + 1];
-    const int b0 = c->h_rowptr[r0], nb = c->h_rowptr[r1] - b0, nrows = r1 - r0;
-    int* hdr = reinterpret_cast<int*>(h.data() + off[t]);
-    hdr[0] = r0;
-    hdr[1] = nrows;
-    hdr[2] = nb;
-    hdr[3] = (int)((((long long)nb * elem + 15) / 16 * 16) / elem);
-    int* rp = hdr + 4;
-    for (int i = 0; i <= nrows; ++i) rp[i] = c->h_rowptr[r0 + i] - b0;
-    int* cl = rp + ceil4(nrows + 1);
-    for (int j = 0; j < nb; ++j) cl[j] = c->h_col[b0 + j];
-  }
   if (!dalloc(c, blob, (size_t)total)) return TG_ERR_OOM;
-  return ok(c, cudaMemcpy(*blob, h.data(), (size_t)total, cudaMemcpyHostToDevice), "blob") ? TG_OK : TG_ERR_CUDA;
+  if (!ok(c, cudaMemsetAsync(*blob, 0, (size_t)total, c->stream), "blob")) return TG_ERR_CUDA;
+  return launch_blob_structure(c, precision);
 }
 }  // namespace tg
 

@@ -157,7 +157,39 @@ __global__ void scatter_eq_kernel(int neq, const int* __restrict__ slot, const d
   reinterpret_cast<double*>(nodal)[slot[k]] = eq[k];
 }
 
+// Structure part of the tile-contiguous storage: one CTA per tile writes the
+// header, the local row pointers and the column indices from the global CSR.
+__global__ void blob_structure_kernel(int ntiles, const int* __restrict__ tile_row, const int* __restrict__ rowptr,
+                                      const int* __restrict__ col, const long long* __restrict__ off, int elem,
+                                      unsigned char* __restrict__ blob) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int r0 = tile_row[t], r1 = tile_row[t + 1];
+    const int b0 = rowptr[r0], nb = rowptr[r1] - b0, nrows = r1 - r0;
+    int* hdr = reinterpret_cast<int*>(blob + off[t]);
+    if (threadIdx.x == 0) {
+      hdr[0] = r0;
+      hdr[1] = nrows;
+      hdr[2] = nb;
+      hdr[3] = (int)((((long long)nb * elem + 15) / 16 * 16) / elem);
+    }
+    int* rp = hdr + 4;
+    for (int i = threadIdx.x; i <= nrows; i += blockDim.x) rp[i] = rowptr[r0 + i] - b0;
+    int* cl = rp + ceil4(nrows + 1);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) cl[j] = col[b0 + j];
+  }
+}
+
 }  // namespace
+
+int launch_blob_structure(Context* c, int precision) {
+  const bool f32 = precision == TG_MIXED;
+  const int grid = std::min(c->ntiles, kNumSMs * 16);
+  blob_structure_kernel<<<std::max(grid, 1), 128, 0, c->stream>>>(c->ntiles, c->d_tile_row, c->d_rowptr, c->d_col,
+                                                                  f32 ? c->d_blob_off32 : c->d_blob_off64,
+                                                                  f32 ? 4 : 8, f32 ? c->d_blob32 : c->d_blob64);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "blob_structure_kernel") ? TG_OK : TG_ERR_CUDA;
+}
 
 int launch_assemble(Context* c, int precision) {
   const int warps_per_block = 8;

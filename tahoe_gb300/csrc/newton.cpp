@@ -5,6 +5,7 @@
 // host reads back one residual norm per iteration plus the PCG flag per
 // graph chunk.
 #include <algorithm>
+#include <string>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -377,6 +378,117 @@ int tg_predict_prescribed(tg_context* c, int n, const int* idx, const double* va
   cudaFreeAsync(d_val, c->stream);
   if (!ok(c, cudaStreamSynchronize(c->stream), "sync") && !s) s = TG_ERR_CUDA;
   if (pcg_iterations) *pcg_iterations = its;
+  return s;
+}
+
+int tg_set_segments(tg_context* c, int nseg, const int* node_off, const int* elem_off) {
+  if (!c || nseg <= 0 || !node_off || !elem_off || c->nnd <= 0) return TG_ERR_ARG;
+  if (node_off[0] != 0 || node_off[nseg] != c->nnd || elem_off[0] != 0 || elem_off[nseg] != c->nel) return TG_ERR_ARG;
+  for (int s = 0; s < nseg; ++s)
+    if (node_off[s + 1] < node_off[s] || elem_off[s + 1] < elem_off[s]) return TG_ERR_ARG;
+  // elements of RVE s may only reference nodes of RVE s
+  for (int s = 0; s < nseg; ++s)
+    for (long long k = (long long)elem_off[s] * 8; k < (long long)elem_off[s + 1] * 8; ++k)
+      if (c->h_conn[k] < node_off[s] || c->h_conn[k] >= node_off[s + 1]) {
+        c->err = "element of RVE " + std::to_string(s) + " references a node outside it";
+        return TG_ERR_ARG;
+      }
+  if (set_device(c)) return TG_ERR_CUDA;
+  for (void** p : {(void**)&c->d_seg_node, (void**)&c->d_seg_elem, (void**)&c->d_seg_out}) {
+    if (*p) dfree(c, *p);
+    *p = nullptr;
+  }
+  c->nseg = nseg;
+  c->h_seg_node.assign(node_off, node_off + nseg + 1);
+  c->h_seg_elem.assign(elem_off, elem_off + nseg + 1);
+  if (!dalloc(c, &c->d_seg_node, (size_t)nseg + 1) || !dalloc(c, &c->d_seg_elem, (size_t)nseg + 1) ||
+      !dalloc(c, &c->d_seg_out, (size_t)nseg * 9))
+    return TG_ERR_OOM;
+  return ok(c, cudaMemcpy(c->d_seg_node, node_off, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice), "seg") &&
+                 ok(c, cudaMemcpy(c->d_seg_elem, elem_off, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice), "seg")
+             ? TG_OK
+             : TG_ERR_CUDA;
+}
+
+int tg_segment_residual_norms(tg_context* c, double* norms) {
+  if (!c || !norms || c->nseg <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int s = launch_segment_norms(c, c->nseg, c->d_seg_node, c->d_seg_out);
+  if (!s && (!ok(c, cudaMemcpyAsync(norms, c->d_seg_out, sizeof(double) * c->nseg, cudaMemcpyDeviceToHost, c->stream),
+                 "norms") ||
+             !ok(c, cudaStreamSynchronize(c->stream), "sync")))
+    s = TG_ERR_CUDA;
+  if (!s)
+    for (int i = 0; i < c->nseg; ++i) norms[i] = std::sqrt(norms[i]);
+  return s;
+}
+
+int tg_segment_average_stress(tg_context* c, const double* vol0, double* P) {
+  if (!c || !P || c->nseg <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  int s = launch_segment_stress(c, c->nseg, c->d_seg_elem, c->d_seg_out);
+  if (!s &&
+      (!ok(c, cudaMemcpyAsync(P, c->d_seg_out, sizeof(double) * 9 * c->nseg, cudaMemcpyDeviceToHost, c->stream), "P") ||
+       !ok(c, cudaStreamSynchronize(c->stream), "sync")))
+    s = TG_ERR_CUDA;
+  if (!s && vol0)
+    for (int i = 0; i < c->nseg; ++i)
+      for (int k = 0; k < 9; ++k) P[i * 9 + k] /= vol0[i];
+  return s;
+}
+
+int tg_newton_solve_segmented(tg_context* c, const tg_newton_params* P, tg_newton_report* rep, double* seg_rel) {
+  if (!c || !P || c->nseg <= 0) return TG_ERR_ARG;
+  if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  tg_newton_report r;
+  std::memset(&r, 0, sizeof(r));
+  PhaseTimer tm(rep != nullptr);
+  c->iteration = -1;
+  std::vector<double> n0(c->nseg), nk(c->nseg);
+  double err0 = 0.0;
+  tm.start(c->stream);
+  int s = residual_norm(c, &err0);
+  if (!s) s = tg_segment_residual_norms(c, n0.data());
+  r.ms_residual += tm.stop(c->stream);
+  r.error0 = r.error = err0;
+  // NLSolver::ExitIteration per RVE: converged when rel < rel_tol or the
+  // absolute norm < abs_tol; the batch iterates until every RVE has
+  auto all_converged = [&](const std::vector<double>& nv, double* worst) {
+    bool okk = true;
+    double w = 0.0;
+    for (int i = 0; i < c->nseg; ++i) {
+      const double rel = n0[i] > 0.0 ? nv[i] / n0[i] : 0.0;
+      if (!(rel < P->rel_tol || nv[i] < P->abs_tol)) okk = false;
+      w = std::max(w, n0[i] > 0.0 ? rel : 0.0);
+    }
+    *worst = w;
+    return okk;
+  };
+  double worst = 0.0;
+  bool converged = !s && all_converged(n0, &worst);
+  while (!s && !converged) {
+    double err = 0.0;
+    int its = 0;
+    s = newton_iteration(c, P, &err, &its, &r, rep ? &tm : nullptr);
+    r.pcg_iterations += its;
+    if (s) break;
+    ++r.iterations;
+    r.error = err;
+    s = tg_segment_residual_norms(c, nk.data());
+    if (s) break;
+    converged = all_converged(nk, &worst);
+    if (!converged && worst > P->div_tol) {
+      c->err = "diverging RVE";
+      s = TG_ERR_DIVERGED;
+    } else if (!converged && c->iteration >= P->max_iterations) {
+      c->err = "max iterations hit";
+      s = TG_ERR_NOT_CONVERGED;
+    }
+  }
+  if (seg_rel)
+    for (int i = 0; i < c->nseg; ++i) seg_rel[i] = n0[i] > 0.0 ? (r.iterations ? nk[i] : n0[i]) / n0[i] : 0.0;
+  if (rep) *rep = r;
   return s;
 }
 

@@ -161,6 +161,13 @@ struct Context {
   cudaGraphExec_t pcg_graph = nullptr;
   int pcg_graph_key = -1;  // precision*2 + precond
 
+  // RVE partition of a batch mesh (tg_set_segments)
+  int nseg = 0;
+  int* d_seg_node = nullptr;   // nseg+1
+  int* d_seg_elem = nullptr;   // nseg+1
+  double* d_seg_out = nullptr; // nseg*9 scratch for segmented results
+  std::vector<int> h_seg_node, h_seg_elem;
+
   // step-start snapshot (tg_checkpoint / tg_rollback)
   double4_32a* d_u_ckpt = nullptr;
   double4_32a* d_R_ckpt = nullptr;
@@ -205,6 +212,10 @@ void build_node_elem(int nnd, int nel, const int* conn, std::vector<int>& ptr, s
 int launch_residual(Context* c);          // fint per element + gather + norm
 int launch_tangent(Context* c, int precision);   // Ke per element
 int launch_assemble(Context* c, int precision);
+int launch_blob_structure(Context* c, int precision);
+// segmented (per-RVE) reductions over node / element ranges
+int launch_segment_norms(Context* c, int nseg, const int* d_node_off, double* d_out);
+int launch_segment_stress(Context* c, int nseg, const int* d_elem_off, double* d_out);
 int form_tangent(Context* c, int precision);
 int launch_element_dump(Context* c, int first, int count, double* dKe, double* dfint);
 int launch_close_step(Context* c, int reset);

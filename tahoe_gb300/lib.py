@@ -79,6 +79,11 @@ _SIGS = {
     "tg_timer_stop": (ctypes.c_int, [_vp, _dp]),
     "tg_time_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     "tg_spmv_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
+    "tg_segment_residual_norms": (ctypes.c_int, [_vp, _dp]),
+    "tg_segment_average_stress": (ctypes.c_int, [_vp, _dp, _dp]),
+    "tg_newton_solve_segmented": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), ctypes.POINTER(NewtonReport),
+                                                 _dp]),
 }
 
 _lib = None
@@ -320,6 +325,33 @@ class Context:
         ms = ctypes.c_double(0)
         self._chk(self.L.tg_timer_stop(self.h, ctypes.byref(ms)), "tg_timer_stop")
         return ms.value
+
+    def set_segments(self, node_off, elem_off):
+        no = np.ascontiguousarray(node_off, dtype=np.int32)
+        eo = np.ascontiguousarray(elem_off, dtype=np.int32)
+        self._chk(self.L.tg_set_segments(self.h, len(no) - 1, _i(no), _i(eo)), "tg_set_segments")
+        self.nseg = len(no) - 1
+
+    def segment_norms(self):
+        out = np.zeros(self.nseg)
+        self._chk(self.L.tg_segment_residual_norms(self.h, _d(out)), "tg_segment_residual_norms")
+        return out
+
+    def segment_stress(self, vol0=None):
+        P = np.zeros(self.nseg * 9)
+        v = None if vol0 is None else np.ascontiguousarray(vol0, dtype=np.float64)
+        self._chk(self.L.tg_segment_average_stress(self.h, _d(v), _d(P)), "tg_segment_average_stress")
+        return P.reshape(-1, 3, 3)
+
+    def newton_segmented(self, rel_tol=1e-8, abs_tol=0.0, div_tol=1e3, max_iterations=20, precision=MIXED,
+                         precond=PRECOND_JACOBI, lin_rel_tol=1e-4, lin_max_it=20000, check=True):
+        P = NewtonParams(rel_tol, abs_tol, div_tol, max_iterations, precision, precond, lin_rel_tol, lin_max_it)
+        R = NewtonReport()
+        rel = np.zeros(self.nseg)
+        rc = self.L.tg_newton_solve_segmented(self.h, ctypes.byref(P), ctypes.byref(R), _d(rel))
+        if check:
+            self._chk(rc, "tg_newton_solve_segmented")
+        return rc, R, rel
 
     def spmv_config(self, tile_blocks, stages):
         self._chk(self.L.tg_spmv_config(self.h, int(tile_blocks), int(stages)), "tg_spmv_config")

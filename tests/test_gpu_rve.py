@@ -1,0 +1,78 @@
+"""Batched FE^2 RVE solves on the GPU against the oracle, per RVE.
+
+Displacements within 1e-8 of the oracle's direct solve, the volume-averaged
+first Piola stress within 1e-7 of the oracle's reaction sum
+(1/V0) sum_{boundary a} f_a (x) X_a, the mixed form within 1e-6 of FP64, and
+an RVE solved alone equal (1e-6) to the same RVE solved inside a batch.
+"""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import OracleModel
+from tahoe_gb300 import lib, rve
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_rve(n, F):
+    t = rve.template(n)
+    o = OracleModel(t.X, t.conn, "total_lagrangian", [rve.MATRIX, rve.INCLUSION], blocks=t.blocks)
+    o.set_schedule([(0.0, 1.0)])
+    U = t.X @ (F - np.eye(3)).T
+    for a in t.boundary:
+        for d in range(3):
+            o.add_kbc(int(a), d, float(U[a, d]), True)
+    st, uh, its = o.run(1, 1.0, 1e-12, 1e-15, 20, 1e3, 0)
+    assert st == 0
+    u = uh[-1]
+    f = o.nodal_internal_force(u)
+    P = sum(np.outer(f[a], t.X[a]) for a in t.boundary) / t.vol
+    return u, P
+
+
+@pytest.fixture(scope="module")
+def batch():
+    ns = np.array([4, 5, 4, 6, 5])
+    rng = np.random.default_rng(11)
+    Fs = np.stack([rve.sample_F(rng) for _ in ns])
+    return ns, Fs
+
+
+def test_batch_matches_oracle_per_rve(batch):
+    ns, Fs = batch
+    b = rve.RVEBatch(ns, Fs)
+    b.setup()
+    rc, rep, rel, P = b.solve(precision=lib.FP64, rel_tol=1e-10, lin_rel_tol=1e-12)
+    assert rc == 0 and rel.max() < 1e-10
+    u = b.ctx.get_u()
+    for r, (n, F) in enumerate(zip(ns, Fs)):
+        uo, Po = oracle_rve(int(n), F)
+        assert rel_err(b.rve_displacement(r, u), uo) < 1e-8, r
+        assert rel_err(P[r], Po) < 1e-7, r
+
+
+def test_mixed_batch_within_1e6_of_fp64(batch):
+    ns, Fs = batch
+    res = {}
+    for prec in (lib.FP64, lib.MIXED):
+        b = rve.RVEBatch(ns, Fs)
+        b.setup()
+        rc, rep, rel, P = b.solve(precision=prec, rel_tol=1e-8, lin_rel_tol=1e-4)
+        assert rc == 0 and rel.max() < 1e-8
+        res[prec] = P
+    assert rel_err(res[lib.MIXED], res[lib.FP64]) < 1e-6
+
+
+def test_rve_alone_equals_rve_in_batch(batch):
+    ns, Fs = batch
+    b = rve.RVEBatch(ns, Fs)
+    b.setup()
+    rc, rep, rel, P = b.solve(precision=lib.MIXED, rel_tol=1e-8)
+    assert rc == 0
+    for r in (1, 3):
+        one = rve.RVEBatch(ns[r:r + 1], Fs[r:r + 1])
+        one.setup()
+        rc1, rep1, rel1, P1 = one.solve(precision=lib.MIXED, rel_tol=1e-8)
+        assert rc1 == 0
+        assert rel_err(P1[0], P[r]) < 1e-6, r
