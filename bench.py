@@ -390,7 +390,7 @@ def run_c4(args):
         "higher_is_better": True, "n_gpus": 1,
         "config": {"workload": "C4: %d independent RVEs, n x n x n hex8 unit cubes, n ~ U{4..16} (seed 0), two-phase "
                                "Simo neo-Hookean (mu 1/10, kappa 10/100, inclusion r=0.3 by centroid), affine BC from "
-                               "F = I + 0.05 S, Newton to 1e-8 per RVE from the affine field" % len(ns),
+                               "F = I + 0.05 S, linear predictor then Newton to 1e-8 per RVE" % len(ns),
                    "elements": int(b.nel), "nodes": int(b.nnd), "dofs": int(3 * b.nnd), "equations": int(c.neq),
                    "block_nnz": int(c.block_nnz)},
         "batch_ms": {k: round(v["ms"], 2) for k, v in out.items()},
@@ -412,6 +412,57 @@ def run_c4(args):
                                 "sample": "oracle (Newton + Jacobi-PCG 1e-4, FP64) on one RVE per size n=4..16, "
                                           "single-threaded; batch rate = pool of %d independent processes at the "
                                           "size-weighted mean %.3f s per RVE" % (threads, mean)}
+    print(json.dumps(line))
+
+
+def run_c5(args):
+    """Configuration 5: a Poisson stream of RVE requests served with
+    continuous batching over several lanes (mixed precision), beside the plain
+    one-at-a-time FP64 GPU solve of the same requests."""
+    from tahoe_gb300 import lib, serve
+    rates = [float(r) for r in args.rates.split(",")]
+    import torch
+    free, _ = torch.cuda.mem_get_info(0)
+    budget = 0.5 * free
+    srv = serve.Server(serve.gpu_batch_solver(lib.MIXED), lanes=args.lanes, max_batch=args.max_batch,
+                       hbm_budget=budget)
+    plain = serve.Server(serve.gpu_batch_solver(lib.FP64), lanes=1, max_batch=1, hbm_budget=budget,
+                         precision=lib.FP64)
+    # warm-up: contexts, memory pools, one graph capture per lane
+    wa, wn, wF = serve.sample_requests(4 * args.lanes, 1e5, seed=99, nmin=4, nmax=8)
+    srv.run(wa, wn, wF)
+    plain.run(wa[:2], wn[:2], wF[:2])
+    sweep = []
+    for i, rate in enumerate(rates):
+        arr, ns, Fs = serve.sample_requests(args.requests, rate, seed=i)
+        res = srv.run(arr, ns, Fs)
+        k = min(args.plain_requests, len(ns))
+        ref = plain.run(arr[:k], ns[:k], Fs[:k])
+        both = (res["status"][:k] == 0) & (ref["status"] == 0)
+        d = np.abs(res["P"][:k] - ref["P"]).reshape(k, -1).max(axis=1) / \
+            np.abs(ref["P"]).reshape(k, -1).max(axis=1)
+        sweep.append({
+            "rate_per_s": rate, "requests": len(ns), "completed": res["completed"],
+            "solves_per_s": round(res["solves_per_s"], 1), "p50_ms": round(res["p50_ms"], 2),
+            "p99_ms": round(res["p99_ms"], 2), "mean_batch": round(res["mean_batch"], 1),
+            "batches": len(res["batches"]), "max_concurrent_lanes": res["max_concurrent_lanes"],
+            "plain_fp64": {"requests": k, "completed": ref["completed"], "solves_per_s": round(ref["solves_per_s"], 1),
+                           "p50_ms": round(ref["p50_ms"], 2), "p99_ms": round(ref["p99_ms"], 2)},
+            "P_rel_err_vs_plain_fp64_worst": float(d[both].max()) if both.any() else None,
+        })
+    srv.close()
+    plain.close()
+    top = max(sweep, key=lambda r: r["solves_per_s"])
+    line = {
+        "metric": "served RVE solves/s", "value": top["solves_per_s"], "unit": "RVE/s", "higher_is_better": True,
+        "n_gpus": 1,
+        "config": {"workload": "C5: Poisson stream of RVE requests, n log-uniform in {4..24}, two-phase Simo "
+                               "neo-Hookean RVE as in C4, F = I + 0.05 S; %d lanes (one CUDA stream each), "
+                               "continuous batching up to %d RVEs per batch, admission by half of free HBM, "
+                               "mixed precision, Newton to 1e-8 per RVE" % (args.lanes, args.max_batch),
+                   "hbm_budget_bytes": int(budget)},
+        "sweep": sweep,
+    }
     print(json.dumps(line))
 
 
@@ -446,11 +497,18 @@ def main():
     ap.add_argument("--kernel", choices=sorted(KERNELS), help="time standalone launches of one kernel only")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--n", type=int, default=64, help="mesh size per side for --kernel")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"])
     ap.add_argument("--rves", type=int, default=4096)
+    ap.add_argument("--rates", default="1000,5000,20000,50000", help="C5 arrival rates per second")
+    ap.add_argument("--requests", type=int, default=2000, help="C5 requests per rate")
+    ap.add_argument("--plain-requests", type=int, default=200, help="C5 requests for the one-at-a-time arm")
+    ap.add_argument("--lanes", type=int, default=4)
+    ap.add_argument("--max-batch", type=int, default=1024)
     args = ap.parse_args()
     if args.workload == "c4" and args.impl == "ours":
         run_c4(args)
+    elif args.workload == "c5" and args.impl == "ours":
+        run_c5(args)
     elif args.kernel:
         run_kernel_only(args)
     elif args.impl == "reference":

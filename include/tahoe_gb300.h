@@ -242,6 +242,30 @@ int tg_segment_average_stress(tg_context* ctx, const double* vol0, double* P);
 int tg_newton_solve_segmented(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report,
                               double* seg_rel);
 
+/* ---- resident templates and composed batch meshes ----------------------
+ * No reference counterpart (serving side of the FE^2 batch): a mesh used
+ * over and over (one RVE size) is registered once; its pattern, contribution
+ * map and tiles stay on the device.  A batch mesh is then composed on the
+ * device as the disjoint union of instances, instance i becoming segment i,
+ * with the same structure tg_mesh_upload would build for the concatenated
+ * mesh.  Templates live until tg_destroy; the context's materials and
+ * formulation apply to composed meshes as to uploaded ones. */
+/* template: coordinates SoA, 0-based connectivity, equation numbers as for
+ * tg_mesh_upload (ascending node-major from 1, prescribed <= 0), element
+ * blocks (NULL: all 0); returns its id */
+int tg_template_add(tg_context* ctx, int nnd, const double* coords_soa, int nel, const int* conn, const int* eqnos,
+                    const int* block_of_element, int* template_id);
+/* replaces the mesh by count instances (template ids in order; <= 65535);
+ * state (displacement, loads, history) starts at zero */
+int tg_mesh_compose(tg_context* ctx, int count, const int* template_ids);
+/* every prescribed dof of segment s set to the affine field (F_s - I) X
+ * (F: nseg row-major 3x3): the per-node kinematic_BC values an affine
+ * (MappedPeriodicT-style) boundary condition would give */
+int tg_set_affine_prescribed(tg_context* ctx, const double* F);
+/* tg_predict_prescribed with the affine field of tg_set_affine_prescribed as
+ * the new prescribed values */
+int tg_predict_affine(tg_context* ctx, const double* F, const tg_newton_params* params, int* pcg_iterations);
+
 /* ---- measurement and tuning helpers (no reference counterpart) ---------- */
 
 /* Shape of the streamed PCG matrix product: row tiles of at most tile_blocks

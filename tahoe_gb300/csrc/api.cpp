@@ -20,12 +20,26 @@ bool ok(Context* c, cudaError_t e, const char* what) {
 
 void dfree(Context* c, void* p) {
   if (!p) return;
-  cudaFree(p);
+  cudaFreeAsync(p, c->stream);
   auto it = std::find(c->allocations.begin(), c->allocations.end(), p);
   if (it != c->allocations.end()) c->allocations.erase(it);
 }
 
 namespace {
+
+// Device buffers go back to the stream-ordered pool; pinned host buffers are
+// released only with the context (freeing pinned memory can synchronise the
+// device).
+void free_device(Context* c) {
+  if (c->ev_a) cudaEventDestroy(c->ev_a);
+  if (c->ev_b) cudaEventDestroy(c->ev_b);
+  c->ev_a = c->ev_b = nullptr;
+  c->d_u_ckpt = c->d_R_ckpt = nullptr;
+  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
+  c->pcg_graph = nullptr;
+  for (void* p : c->allocations) cudaFreeAsync(p, c->stream);
+  c->allocations.clear();
+}
 
 void free_all(Context* c) {
   if (c->ev_a) cudaEventDestroy(c->ev_a);
@@ -34,8 +48,10 @@ void free_all(Context* c) {
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
-  for (void* p : c->allocations) cudaFree(p);
+  for (void* p : c->allocations) cudaFreeAsync(p, c->stream);
   c->allocations.clear();
+  free_templates(c);
+  if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->h_pcg) cudaFreeHost(c->h_pcg);
   if (c->h_resid) cudaFreeHost(c->h_resid);
   if (c->h_status) cudaFreeHost(c->h_status);
@@ -103,6 +119,103 @@ bool valid_material(int kind, const double* p, int np, MatParams& m) {
 }
 
 }  // namespace
+
+// Active-dof bits per node and the node*4+dof slot of every equation; the
+// equation numbers must be 1..neq in node-major / dof-minor order (prescribed
+// dofs <= 0).  Returns neq, or -1 with the context error set.
+int equation_slots(Context* c, int nnd, const int* eqnos, std::vector<uint8_t>& mask, std::vector<int>& slot) {
+  int neq = 0;
+  mask.assign(nnd, 0);
+  slot.clear();
+  for (int n = 0; n < nnd; ++n)
+    for (int d = 0; d < 3; ++d) {
+      const int q = eqnos[n * 3 + d];
+      if (q > 0) {
+        if (q != neq + 1) {
+          c->err = "equation numbers must be ascending node-major from 1";
+          return -1;
+        }
+        ++neq;
+        mask[n] |= (uint8_t)(1u << d);
+        slot.push_back(n * 4 + d);
+      }
+    }
+  return neq;
+}
+
+// Releases the current mesh (buffers back to the pool) and allocates every
+// per-mesh device array for the given sizes, with the state zeroed: nodal
+// vectors, status words, J2 history (flags unallocated), padded index tails.
+int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
+  cudaStreamSynchronize(c->stream);
+  free_device(c);
+  c->pcg_vec_precision = -1;
+  c->pcg_graph_key = -1;
+  c->tangent_precision = -1;
+  c->d_x = c->d_r = c->d_z = c->d_p = c->d_p1 = c->d_q = nullptr;
+  c->d_Ke32 = nullptr;
+  c->d_Ke64 = nullptr;
+  c->d_blob32 = c->d_blob64 = nullptr;
+  c->nseg = 0;
+  c->d_seg_node = c->d_seg_elem = nullptr;
+  c->d_seg_out = nullptr;
+  c->h_seg_node.clear();
+  c->h_seg_elem.clear();
+  c->d_blob_off32 = c->d_blob_off64 = nullptr;
+  c->d_row_tile = nullptr;
+  c->d_tile_row = nullptr;
+  c->d_minv32 = nullptr;
+  c->d_minv64 = nullptr;
+  c->d_block = nullptr;
+  c->have_blocks = false;
+  c->have_du = false;
+  c->composed = false;
+  c->h_conn.clear();
+  c->h_eqnos.clear();
+  c->h_coords.clear();
+  c->h_eq_slot.clear();
+  c->h_rowptr.clear();
+  c->h_col.clear();
+  c->nnd = nnd;
+  c->nel = nel;
+  c->neq = neq;
+  c->nnzb = nnzb;
+  c->nnzb_pad = (nnzb + 31) / 32 * 32;
+  const size_t nip = (size_t)nel * 8;
+  const size_t rp_len = (size_t)(nnd + 1 + 3) / 4 * 4 + 4;
+  bool good = dalloc(c, &c->d_X, (size_t)nnd * 3) && dalloc(c, &c->d_conn, nip) &&
+              dalloc(c, &c->d_mask, (size_t)nnd) && dalloc(c, &c->d_eq_slot, (size_t)std::max(neq, 1)) &&
+              dalloc(c, &c->d_node_elem_ptr, (size_t)nnd + 1) && dalloc(c, &c->d_node_elem, nip) &&
+              dalloc(c, &c->d_rowptr, rp_len) && dalloc(c, &c->d_col, (size_t)c->nnzb_pad) &&
+              dalloc(c, &c->d_contrib_ptr, (size_t)nnzb + 1) && dalloc(c, &c->d_contrib, nip * 8) &&
+              dalloc(c, &c->d_u, (size_t)nnd) && dalloc(c, &c->d_fext, (size_t)nnd) && dalloc(c, &c->d_R, (size_t)nnd) &&
+              dalloc(c, &c->d_fint, nip) && dalloc(c, &c->d_status, 1) && dalloc(c, &c->d_resid, 1) &&
+              dalloc(c, &c->d_pcg, 1);
+  c->partials_cap = 4096;
+  good = good && dalloc(c, &c->d_partials, (size_t)c->partials_cap * 2);
+  good = good && dalloc(c, &c->d_j2_flags, nip) && dalloc(c, &c->d_j2_alloc, (size_t)nel) &&
+         dalloc(c, &c->d_j2_alpha, nip) && dalloc(c, &c->d_j2_dgamma, nip) && dalloc(c, &c->d_j2_norm, nip) &&
+         dalloc(c, &c->d_j2_epsp, nip * 6) && dalloc(c, &c->d_j2_nhat, nip * 6);
+  if (!good) return TG_ERR_OOM;
+  cudaStream_t s = c->stream;
+  good = ok(c, cudaMemsetAsync(c->d_rowptr, 0, sizeof(int) * rp_len, s), "rp") &&
+         ok(c, cudaMemsetAsync(c->d_col, 0, sizeof(int) * c->nnzb_pad, s), "col") &&
+         ok(c, cudaMemsetAsync(c->d_u, 0, sizeof(double4_32a) * nnd, s), "u") &&
+         ok(c, cudaMemsetAsync(c->d_fext, 0, sizeof(double4_32a) * nnd, s), "f") &&
+         ok(c, cudaMemsetAsync(c->d_R, 0, sizeof(double4_32a) * nnd, s), "R") &&
+         ok(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s), "st") &&
+         ok(c, cudaMemsetAsync(c->d_resid, 0, sizeof(ResidScalars), s), "rs") &&
+         ok(c, cudaMemsetAsync(c->d_pcg, 0, sizeof(PcgScalars), s), "pcg") &&
+         ok(c, cudaMemsetAsync(c->d_j2_flags, TG_J2_UNALLOCATED, nip, s), "fl") &&
+         ok(c, cudaMemsetAsync(c->d_j2_alloc, 0, nel, s), "al") &&
+         ok(c, cudaMemsetAsync(c->d_j2_alpha, 0, sizeof(double) * nip, s), "a") &&
+         ok(c, cudaMemsetAsync(c->d_j2_dgamma, 0, sizeof(double) * nip, s), "dg") &&
+         ok(c, cudaMemsetAsync(c->d_j2_norm, 0, sizeof(double) * nip, s), "nr") &&
+         ok(c, cudaMemsetAsync(c->d_j2_epsp, 0, sizeof(double) * nip * 6, s), "ep") &&
+         ok(c, cudaMemsetAsync(c->d_j2_nhat, 0, sizeof(double) * nip * 6, s), "nh");
+  return good ? TG_OK : TG_ERR_CUDA;
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -117,6 +230,15 @@ int tg_create(tg_context** out, int device) {
   c->device = device;
   c->mats.nblocks = 1;
   c->mats.formulation = TG_SMALL_STRAIN;
+  // keep freed device memory in the stream-ordered pool for reuse
+  if (!set_device(c)) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      unsigned long long keep = ~0ULL;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   if (set_device(c) || !ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
       !ok(c, cudaMallocHost((void**)&c->h_pcg, sizeof(PcgScalars)), "pinned") ||
       !ok(c, cudaMallocHost((void**)&c->h_resid, sizeof(ResidScalars)), "pinned") ||
@@ -153,106 +275,38 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
       c->err = "connectivity out of range";
       return TG_ERR_ARG;
     }
+  std::vector<uint8_t> mask;
+  std::vector<int> slot;
+  const int neq = equation_slots(c, nnd, eqnos, mask, slot);
+  if (neq < 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
-  cudaStreamSynchronize(c->stream);
-  free_all(c);
-  if (!ok(c, cudaMallocHost((void**)&c->h_pcg, sizeof(PcgScalars)), "pinned") ||
-      !ok(c, cudaMallocHost((void**)&c->h_resid, sizeof(ResidScalars)), "pinned") ||
-      !ok(c, cudaMallocHost((void**)&c->h_status, sizeof(int)), "pinned"))
-    return TG_ERR_CUDA;
-  c->pcg_vec_precision = -1;
-  c->pcg_graph_key = -1;
-  c->tangent_precision = -1;
-  c->d_x = c->d_r = c->d_z = c->d_p = c->d_p1 = c->d_q = nullptr;
-  c->d_Ke32 = nullptr;
-  c->d_Ke64 = nullptr;
-  c->d_blob32 = c->d_blob64 = nullptr;
-  c->nseg = 0;
-  c->d_seg_node = c->d_seg_elem = nullptr;
-  c->d_seg_out = nullptr;
-  c->d_blob_off32 = c->d_blob_off64 = nullptr;
-  c->d_row_tile = nullptr;
-  c->d_minv32 = nullptr;
-  c->d_minv64 = nullptr;
-  c->d_block = nullptr;
-  c->have_blocks = false;
-  c->have_du = false;
-  c->nnd = nnd;
-  c->nel = nel;
+  std::vector<int> rowptr, col, cptr, contrib, nptr, nlist;
+  build_block_pattern(nnd, nel, conn, rowptr, col);
+  build_contrib_map(nnd, nel, conn, rowptr, col, cptr, contrib);
+  build_node_elem(nnd, nel, conn, nptr, nlist);
+  int s = alloc_mesh(c, nnd, nel, neq, rowptr[nnd]);
+  if (s) return s;
   c->h_conn.assign(conn, conn + (size_t)nel * 8);
   c->h_eqnos.assign(eqnos, eqnos + (size_t)nnd * 3);
   c->h_coords.assign(coords, coords + (size_t)nnd * 3);
-  // active equations must be 1..neq in node-major / dof-minor order
-  int neq = 0;
-  std::vector<uint8_t> mask(nnd, 0);
-  c->h_eq_slot.clear();
-  for (int n = 0; n < nnd; ++n)
-    for (int d = 0; d < 3; ++d) {
-      const int q = eqnos[n * 3 + d];
-      if (q > 0) {
-        if (q != neq + 1) {
-          c->err = "equation numbers must be ascending node-major from 1";
-          return TG_ERR_ARG;
-        }
-        ++neq;
-        mask[n] |= (uint8_t)(1u << d);
-        c->h_eq_slot.push_back(n * 4 + d);
-      }
-    }
-  c->neq = neq;
-
-  build_block_pattern(nnd, nel, conn, c->h_rowptr, c->h_col);
-  std::vector<int> cptr, contrib, nptr, nlist;
-  build_contrib_map(nnd, nel, conn, c->h_rowptr, c->h_col, cptr, contrib);
-  build_node_elem(nnd, nel, conn, nptr, nlist);
-  c->nnzb = c->h_rowptr[nnd];
-  c->nnzb_pad = (c->nnzb + 31) / 32 * 32;
+  c->h_eq_slot = slot;
+  c->h_rowptr.swap(rowptr);
+  c->h_col.swap(col);
   const size_t nip = (size_t)nel * 8;
-  bool good = dalloc(c, &c->d_X, (size_t)nnd * 3) && dalloc(c, &c->d_conn, (size_t)nel * 8) &&
-              dalloc(c, &c->d_mask, (size_t)nnd) && dalloc(c, &c->d_eq_slot, (size_t)std::max(neq, 1)) &&
-              dalloc(c, &c->d_node_elem_ptr, (size_t)nnd + 1) && dalloc(c, &c->d_node_elem, nip) &&
-              dalloc(c, &c->d_rowptr, (size_t)(nnd + 1 + 3) / 4 * 4 + 4) && dalloc(c, &c->d_col, (size_t)c->nnzb_pad) &&
-
-              dalloc(c, &c->d_contrib_ptr, (size_t)c->nnzb + 1) && dalloc(c, &c->d_contrib, (size_t)nel * 64) &&
-              dalloc(c, &c->d_u, (size_t)nnd) && dalloc(c, &c->d_fext, (size_t)nnd) && dalloc(c, &c->d_R, (size_t)nnd) &&
-              dalloc(c, &c->d_fint, nip) && dalloc(c, &c->d_status, 1) && dalloc(c, &c->d_resid, 1) &&
-              dalloc(c, &c->d_pcg, 1);
-  c->partials_cap = 4096;
-  good = good && dalloc(c, &c->d_partials, (size_t)c->partials_cap * 2);
-  good = good && dalloc(c, &c->d_j2_flags, nip) && dalloc(c, &c->d_j2_alloc, (size_t)nel) &&
-         dalloc(c, &c->d_j2_alpha, nip) && dalloc(c, &c->d_j2_dgamma, nip) && dalloc(c, &c->d_j2_norm, nip) &&
-         dalloc(c, &c->d_j2_epsp, nip * 6) && dalloc(c, &c->d_j2_nhat, nip * 6);
-  if (!good) return TG_ERR_OOM;
-  cudaStream_t s = c->stream;
-  good = ok(c, cudaMemcpyAsync(c->d_X, coords, sizeof(double) * nnd * 3, cudaMemcpyHostToDevice, s), "X") &&
-         ok(c, cudaMemcpyAsync(c->d_conn, conn, sizeof(int) * nel * 8, cudaMemcpyHostToDevice, s), "conn") &&
-         ok(c, cudaMemcpyAsync(c->d_mask, mask.data(), nnd, cudaMemcpyHostToDevice, s), "mask") &&
-         ok(c, cudaMemcpyAsync(c->d_eq_slot, c->h_eq_slot.data(), sizeof(int) * neq, cudaMemcpyHostToDevice, s), "slot") &&
-         ok(c, cudaMemcpyAsync(c->d_node_elem_ptr, nptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, s), "np") &&
-         ok(c, cudaMemcpyAsync(c->d_node_elem, nlist.data(), sizeof(int) * nip, cudaMemcpyHostToDevice, s), "nl") &&
-         ok(c, cudaMemsetAsync(c->d_rowptr, 0, sizeof(int) * ((size_t)(nnd + 1 + 3) / 4 * 4 + 4), s), "rp") &&
-         ok(c, cudaMemcpyAsync(c->d_rowptr, c->h_rowptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, s), "rp") &&
-         ok(c, cudaMemsetAsync(c->d_col, 0, sizeof(int) * c->nnzb_pad, s), "col") &&
-         ok(c, cudaMemcpyAsync(c->d_col, c->h_col.data(), sizeof(int) * c->nnzb, cudaMemcpyHostToDevice, s), "col") &&
-
-         ok(c, cudaMemcpyAsync(c->d_contrib_ptr, cptr.data(), sizeof(int) * (c->nnzb + 1), cudaMemcpyHostToDevice, s), "cp") &&
-         ok(c, cudaMemcpyAsync(c->d_contrib, contrib.data(), sizeof(int) * (size_t)nel * 64, cudaMemcpyHostToDevice, s), "ct") &&
-         ok(c, cudaMemsetAsync(c->d_u, 0, sizeof(double4_32a) * nnd, s), "u") &&
-         ok(c, cudaMemsetAsync(c->d_fext, 0, sizeof(double4_32a) * nnd, s), "f") &&
-         ok(c, cudaMemsetAsync(c->d_R, 0, sizeof(double4_32a) * nnd, s), "R") &&
-         ok(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s), "st") &&
-         ok(c, cudaMemsetAsync(c->d_resid, 0, sizeof(ResidScalars), s), "rs") &&
-         ok(c, cudaMemsetAsync(c->d_pcg, 0, sizeof(PcgScalars), s), "pcg") &&
-         ok(c, cudaMemsetAsync(c->d_j2_flags, TG_J2_UNALLOCATED, nip, s), "fl") &&
-         ok(c, cudaMemsetAsync(c->d_j2_alloc, 0, nel, s), "al") &&
-         ok(c, cudaMemsetAsync(c->d_j2_alpha, 0, sizeof(double) * nip, s), "a") &&
-         ok(c, cudaMemsetAsync(c->d_j2_dgamma, 0, sizeof(double) * nip, s), "dg") &&
-         ok(c, cudaMemsetAsync(c->d_j2_norm, 0, sizeof(double) * nip, s), "nr") &&
-         ok(c, cudaMemsetAsync(c->d_j2_epsp, 0, sizeof(double) * nip * 6, s), "ep") &&
-         ok(c, cudaMemsetAsync(c->d_j2_nhat, 0, sizeof(double) * nip * 6, s), "nh") &&
-         ok(c, cudaStreamSynchronize(s), "upload sync");
+  cudaStream_t st = c->stream;
+  const bool good =
+      ok(c, cudaMemcpyAsync(c->d_X, coords, sizeof(double) * nnd * 3, cudaMemcpyHostToDevice, st), "X") &&
+      ok(c, cudaMemcpyAsync(c->d_conn, conn, sizeof(int) * nip, cudaMemcpyHostToDevice, st), "conn") &&
+      ok(c, cudaMemcpyAsync(c->d_mask, mask.data(), nnd, cudaMemcpyHostToDevice, st), "mask") &&
+      ok(c, cudaMemcpyAsync(c->d_eq_slot, slot.data(), sizeof(int) * neq, cudaMemcpyHostToDevice, st), "slot") &&
+      ok(c, cudaMemcpyAsync(c->d_node_elem_ptr, nptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, st), "np") &&
+      ok(c, cudaMemcpyAsync(c->d_node_elem, nlist.data(), sizeof(int) * nip, cudaMemcpyHostToDevice, st), "nl") &&
+      ok(c, cudaMemcpyAsync(c->d_rowptr, c->h_rowptr.data(), sizeof(int) * (nnd + 1), cudaMemcpyHostToDevice, st), "rp") &&
+      ok(c, cudaMemcpyAsync(c->d_col, c->h_col.data(), sizeof(int) * c->nnzb, cudaMemcpyHostToDevice, st), "col") &&
+      ok(c, cudaMemcpyAsync(c->d_contrib_ptr, cptr.data(), sizeof(int) * (c->nnzb + 1), cudaMemcpyHostToDevice, st), "cp") &&
+      ok(c, cudaMemcpyAsync(c->d_contrib, contrib.data(), sizeof(int) * nip * 8, cudaMemcpyHostToDevice, st), "ct") &&
+      ok(c, cudaStreamSynchronize(st), "upload sync");
   if (!good) return TG_ERR_CUDA;
-  c->d_tile_row = nullptr;
   return build_tiles(c, c->spmv_tile_blocks);
 }
 
@@ -264,6 +318,7 @@ namespace tg {
 // byte offsets of every tile in the tile-contiguous matrix storage of each
 // precision.  Any existing matrix storage is dropped (its layout changes).
 int build_tiles(Context* c, int tile_blocks) {
+  if (ensure_host_mesh(c)) return TG_ERR_CUDA;
   std::vector<int> tiles(1, 0);
   for (int r = 0; r < c->nnd; ++r)
     if (r > tiles.back() && c->h_rowptr[r + 1] - c->h_rowptr[tiles.back()] > tile_blocks) tiles.push_back(r);
@@ -380,6 +435,7 @@ int tg_sizes(const tg_context* c, int* neq, long long* nnzb) {
 // Scalar expansion of the block pattern over active equations.
 int tg_pattern_build(tg_context* c, int upper_only, int* row_ptr, int* col_idx, long long* nnz) {
   if (!c || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c) || ensure_host_mesh(c)) return TG_ERR_CUDA;
   const int* eq = c->h_eqnos.data();
   long long count = 0;
   if (row_ptr) row_ptr[0] = 0;

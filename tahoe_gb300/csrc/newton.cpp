@@ -108,7 +108,7 @@ extern "C" {
 
 int tg_get_tangent_csr(tg_context* c, int upper_only, double* vals) {
   if (!c || !vals || c->tangent_precision < 0) return TG_ERR_ARG;
-  if (set_device(c)) return TG_ERR_CUDA;
+  if (set_device(c) || ensure_host_mesh(c)) return TG_ERR_CUDA;
   // decode the tile-contiguous storage: tile t, local block jl, plane k
   const bool f32 = c->tangent_precision == TG_MIXED;
   const std::vector<long long>& off = f32 ? c->h_blob_off32 : c->h_blob_off64;
@@ -152,9 +152,9 @@ int tg_element_dump(tg_context* c, int first, int count, double* Ke, double* fin
   if (set_device(c)) return TG_ERR_CUDA;
   if (!c->d_Ke64 && !dalloc(c, &c->d_Ke64, (size_t)c->nel * kKeStride)) return TG_ERR_OOM;
   double *dK = nullptr, *dF = nullptr;
-  if (!ok(c, cudaMalloc((void**)&dK, sizeof(double) * 576 * count), "alloc") ||
-      !ok(c, cudaMalloc((void**)&dF, sizeof(double) * 24 * count), "alloc")) {
-    cudaFree(dK);
+  if (!ok(c, cudaMallocAsync((void**)&dK, sizeof(double) * 576 * count, c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&dF, sizeof(double) * 24 * count, c->stream), "alloc")) {
+    if (dK) cudaFreeAsync(dK, c->stream);
     return TG_ERR_OOM;
   }
   int s = launch_element_dump(c, first, count, dK, dF);
@@ -162,9 +162,9 @@ int tg_element_dump(tg_context* c, int first, int count, double* Ke, double* fin
              !ok(c, cudaMemcpyAsync(fint, dF, sizeof(double) * 24 * count, cudaMemcpyDeviceToHost, c->stream), "F")))
     s = TG_ERR_CUDA;
   if (!s) s = check_status(c);
+  cudaFreeAsync(dK, c->stream);
+  cudaFreeAsync(dF, c->stream);
   cudaStreamSynchronize(c->stream);
-  cudaFree(dK);
-  cudaFree(dF);
   return s;
 }
 
@@ -290,6 +290,14 @@ int tg_newton_iteration(tg_context* c, const tg_newton_params* P, double* norm, 
   if (pcg_iterations) *pcg_iterations = its;
   return s;
 }
+}  // extern "C"
+
+namespace {
+int predict(tg_context* c, int n, const int* idx, const double* val, const double* F, const tg_newton_params* P,
+            int* pcg_iterations);
+}  // namespace
+
+extern "C" {
 
 int tg_newton_solve(tg_context* c, const tg_newton_params* P, tg_newton_report* rep) {
   if (!c || !P || c->nnd <= 0) return TG_ERR_ARG;
@@ -342,6 +350,23 @@ int tg_predict_prescribed(tg_context* c, int n, const int* idx, const double* va
   if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
   for (int k = 0; k < n; ++k)
     if (idx[k] < 0 || idx[k] >= c->nnd * 3) return TG_ERR_ARG;
+  return predict(c, n, idx, val, nullptr, P, pcg_iterations);
+}
+
+int tg_predict_affine(tg_context* c, const double* F, const tg_newton_params* P, int* pcg_iterations) {
+  if (!c || !P || !F || c->nnd <= 0 || c->nseg <= 0) return TG_ERR_ARG;
+  if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
+  return predict(c, 0, nullptr, nullptr, F, P, pcg_iterations);
+}
+
+}  // extern "C"
+
+namespace {
+// The prescribed-increment predictor: the new prescribed values are either
+// n (dof, value) pairs or, with F given, the affine field (F_s - I) X of every
+// segment on its prescribed dofs.
+int predict(tg_context* c, int n, const int* idx, const double* val, const double* F, const tg_newton_params* P,
+            int* pcg_iterations) {
   if (set_device(c)) return TG_ERR_CUDA;
   if (pcg_iterations) *pcg_iterations = 0;
   // R(u_old) without committing history, tangent at u_old
@@ -353,16 +378,19 @@ int tg_predict_prescribed(tg_context* c, int n, const int* idx, const double* va
   int* d_idx = nullptr;
   double* d_val = nullptr;
   const size_t nb = sizeof(double4_32a) * c->nnd;
+  const size_t nval = F ? (size_t)9 * c->nseg : (size_t)std::max(n, 1);
   if (!ok(c, cudaMallocAsync((void**)&d_old, nb, c->stream), "alloc") ||
       !ok(c, cudaMallocAsync((void**)&d_v, nb, c->stream), "alloc") ||
       !ok(c, cudaMallocAsync((void**)&d_idx, sizeof(int) * std::max(n, 1), c->stream), "alloc") ||
-      !ok(c, cudaMallocAsync((void**)&d_val, sizeof(double) * std::max(n, 1), c->stream), "alloc"))
+      !ok(c, cudaMallocAsync((void**)&d_val, sizeof(double) * nval, c->stream), "alloc"))
     return TG_ERR_OOM;
   if (!ok(c, cudaMemcpyAsync(d_old, c->d_u, nb, cudaMemcpyDeviceToDevice, c->stream), "copy") ||
       (n > 0 && (!ok(c, cudaMemcpyAsync(d_idx, idx, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream), "idx") ||
-                 !ok(c, cudaMemcpyAsync(d_val, val, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream), "val"))))
+                 !ok(c, cudaMemcpyAsync(d_val, val, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream), "val"))) ||
+      (F && !ok(c, cudaMemcpyAsync(d_val, F, sizeof(double) * nval, cudaMemcpyHostToDevice, c->stream), "F")))
     s = TG_ERR_CUDA;
-  if (!s) s = launch_set_prescribed(c, n, d_idx, d_val);  // u now carries the new prescribed values
+  // u now carries the new prescribed values
+  if (!s) s = F ? launch_affine_prescribed(c, d_val) : launch_set_prescribed(c, n, d_idx, d_val);
   if (!s) s = launch_diff(c, c->d_u, d_old, d_v);         // v = du_p (zero on free dofs)
   if (!s) s = launch_lift_rhs(c, d_v, d_old);             // rhs = R - K v (d_old is free after the diff)
   int its = 0;
@@ -380,12 +408,16 @@ int tg_predict_prescribed(tg_context* c, int n, const int* idx, const double* va
   if (pcg_iterations) *pcg_iterations = its;
   return s;
 }
+}  // namespace
+
+extern "C" {
 
 int tg_set_segments(tg_context* c, int nseg, const int* node_off, const int* elem_off) {
   if (!c || nseg <= 0 || !node_off || !elem_off || c->nnd <= 0) return TG_ERR_ARG;
   if (node_off[0] != 0 || node_off[nseg] != c->nnd || elem_off[0] != 0 || elem_off[nseg] != c->nel) return TG_ERR_ARG;
   for (int s = 0; s < nseg; ++s)
     if (node_off[s + 1] < node_off[s] || elem_off[s + 1] < elem_off[s]) return TG_ERR_ARG;
+  if (set_device(c) || ensure_host_mesh(c)) return TG_ERR_CUDA;
   // elements of RVE s may only reference nodes of RVE s
   for (int s = 0; s < nseg; ++s)
     for (long long k = (long long)elem_off[s] * 8; k < (long long)elem_off[s + 1] * 8; ++k)

@@ -55,6 +55,8 @@ struct ResidScalars {
   int pad;
 };
 
+struct MeshTemplate;  // a resident template mesh (compose.cu)
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
@@ -174,6 +176,11 @@ struct Context {
   // caller timer (tg_timer_start / tg_timer_stop)
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
 
+  // resident mesh templates (tg_template_add) and the composed mesh
+  std::vector<MeshTemplate*> templates;
+  bool composed = false;           // mesh built by tg_mesh_compose (host copies on demand)
+  std::vector<int> h_inst_tpl;     // template of every instance of the composed mesh
+
   std::vector<void*> allocations;
 };
 
@@ -182,9 +189,14 @@ bool ok(Context* c, cudaError_t e, const char* what);
 template <typename T>
 bool dalloc(Context* c, T** p, size_t n) {
   if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  // stream-ordered: no device-wide synchronisation, so contexts on other
+  // streams keep running while this one (re)allocates
+  cudaError_t e = cudaMallocAsync((void**)p, n * sizeof(T), c->stream);
+  // the buffer is then valid for any stream and for synchronous copies
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
-    c->err = std::string("cudaMalloc failed: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    c->err = std::string("cudaMallocAsync failed: ") + cudaGetErrorString(e);
     *p = nullptr;
     return false;
   }
@@ -192,6 +204,13 @@ bool dalloc(Context* c, T** p, size_t n) {
   return true;
 }
 void dfree(Context* c, void* p);
+
+int equation_slots(Context* c, int nnd, const int* eqnos, std::vector<uint8_t>& mask, std::vector<int>& slot);
+int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb);
+// host copies of the mesh structure of a composed mesh, fetched on demand
+int ensure_host_mesh(Context* c);
+void free_templates(Context* c);
+int launch_affine_prescribed(Context* c, const double* d_F);
 
 // ---- host mesh utilities (mesh.cpp) ----
 void build_block_pattern(int nnd, int nel, const int* conn, std::vector<int>& rowptr, std::vector<int>& col);

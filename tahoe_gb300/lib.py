@@ -84,6 +84,10 @@ _SIGS = {
     "tg_segment_average_stress": (ctypes.c_int, [_vp, _dp, _dp]),
     "tg_newton_solve_segmented": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), ctypes.POINTER(NewtonReport),
                                                  _dp]),
+    "tg_template_add": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, _ip]),
+    "tg_mesh_compose": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
+    "tg_set_affine_prescribed": (ctypes.c_int, [_vp, _dp]),
+    "tg_predict_affine": (ctypes.c_int, [_vp, _dp, ctypes.POINTER(NewtonParams), _ip]),
 }
 
 _lib = None
@@ -311,6 +315,47 @@ class Context:
         self._chk(self.L.tg_predict_prescribed(self.h, len(idx), _i(idx), _d(vals), ctypes.byref(P),
                                                ctypes.byref(its)), "tg_predict_prescribed")
         return its.value
+
+    def predict_affine(self, F, precision=MIXED, precond=PRECOND_JACOBI, lin_rel_tol=1e-6, lin_max_it=20000):
+        F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1)
+        if F.size != 9 * self.nseg:
+            raise ValueError("need one 3x3 F per segment")
+        P = NewtonParams(0.0, 0.0, 1e30, 1 << 30, precision, precond, lin_rel_tol, lin_max_it)
+        its = ctypes.c_int(0)
+        self._chk(self.L.tg_predict_affine(self.h, _d(F), ctypes.byref(P), ctypes.byref(its)), "tg_predict_affine")
+        return its.value
+
+    # ---- resident templates ----
+    def template_add(self, X, conn, eqnos, blocks=None):
+        X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+        coords = np.ascontiguousarray(X.T).reshape(-1)
+        conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 8)
+        eq = np.ascontiguousarray(eqnos, dtype=np.int32).reshape(-1)
+        b = None if blocks is None else np.ascontiguousarray(blocks, dtype=np.int32)
+        tid = ctypes.c_int(-1)
+        self._chk(self.L.tg_template_add(self.h, X.shape[0], _d(coords), conn.shape[0], _i(conn), _i(eq), _i(b),
+                                         ctypes.byref(tid)), "tg_template_add")
+        if not hasattr(self, "_tpl_sizes"):
+            self._tpl_sizes = []
+        self._tpl_sizes.append((X.shape[0], conn.shape[0]))
+        return tid.value
+
+    def compose(self, template_ids):
+        ids = np.ascontiguousarray(template_ids, dtype=np.int32)
+        self._chk(self.L.tg_mesh_compose(self.h, len(ids), _i(ids)), "tg_mesh_compose")
+        sizes = np.asarray(self._tpl_sizes, dtype=np.int64)[ids]
+        self.nnd, self.nel = int(sizes[:, 0].sum()), int(sizes[:, 1].sum())
+        n = ctypes.c_int(0)
+        nb = ctypes.c_longlong(0)
+        self.L.tg_sizes(self.h, ctypes.byref(n), ctypes.byref(nb))
+        self.neq, self.block_nnz = n.value, nb.value
+        self.nseg = len(ids)
+
+    def set_affine(self, F):
+        F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1)
+        if F.size != 9 * self.nseg:
+            raise ValueError("need one 3x3 F per segment")
+        self._chk(self.L.tg_set_affine_prescribed(self.h, _d(F)), "tg_set_affine_prescribed")
 
     def checkpoint(self):
         self._chk(self.L.tg_checkpoint(self.h), "tg_checkpoint")

@@ -114,9 +114,11 @@ class RVEBatch:
     def nel(self):
         return self.conn.shape[0]
 
-    def setup(self, device=0):
+    def setup(self, device=0, ctx=None):
+        """Uploads the batch; an existing context (a serving lane's) is
+        reused, its previous mesh released into the stream's memory pool."""
         eq = equations(self.nnd, self.prescribed_idx)
-        c = lib.Context(device)
+        c = ctx if ctx is not None else lib.Context(device)
         c.upload(self.X, self.conn, eq)
         c.set_formulation(lib.TOTAL_LAGRANGIAN)
         for b, m in enumerate((MATRIX, INCLUSION)):
@@ -147,3 +149,44 @@ class RVEBatch:
     def rve_displacement(self, r, u=None):
         u = self.ctx.get_u() if u is None else u
         return u[self.node_off[r]:self.node_off[r + 1]]
+
+
+class ResidentRVEs:
+    """RVE templates resident on one context: every side length is registered
+    once (pattern, contribution map, tiles built one time), and each batch
+    mesh is composed on the device from them (tg_mesh_compose), so preparing
+    a batch costs O(batch) host work."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.ids = {}
+        ctx.set_formulation(lib.TOTAL_LAGRANGIAN)
+        for b, m in enumerate((MATRIX, INCLUSION)):
+            kind, p = material_params(m)
+            ctx.set_material(b, kind, p)
+
+    def template_id(self, n):
+        n = int(n)
+        if n not in self.ids:
+            t = template(n)
+            pidx = (t.boundary[:, None] * 3 + np.arange(3)[None, :]).reshape(-1)
+            self.ids[n] = self.ctx.template_add(t.X, t.conn, equations(t.nnd, pidx), t.blocks)
+        return self.ids[n]
+
+    def compose(self, ns):
+        self.ctx.compose([self.template_id(n) for n in ns])
+
+    def solve(self, ns, Fs, precision=lib.MIXED, rel_tol=1e-8, lin_rel_tol=1e-4, max_iterations=20,
+              precond=lib.PRECOND_JACOBI):
+        """Composes the batch, runs the affine predictor from the undeformed
+        state and Newton to rel_tol per RVE; same returns as RVEBatch.solve."""
+        c = self.ctx
+        self.compose(ns)
+        Fs = np.asarray(Fs, dtype=np.float64).reshape(-1, 3, 3)
+        pred_its = c.predict_affine(Fs, precision=precision, precond=precond, lin_rel_tol=lin_rel_tol)
+        rc, rep, rel = c.newton_segmented(rel_tol=rel_tol, abs_tol=0.0, max_iterations=max_iterations,
+                                          precision=precision, precond=precond, lin_rel_tol=lin_rel_tol,
+                                          check=False)
+        rep.pcg_iterations += pred_its
+        P = c.segment_stress(np.array([template(int(n)).vol for n in ns]))
+        return rc, rep, rel, P
