@@ -367,21 +367,27 @@ def rve_cpu_sample(sizes_all, threads, seed=0):
 
 
 def run_c4(args):
-    """Configuration 4: a batch of independent RVEs solved together."""
+    """Configuration 4: a batch of independent RVEs solved together.  The
+    timed batch covers composing the batch mesh from the resident templates,
+    the affine predictor, Newton to 1e-8 per RVE and the averaged stresses."""
     from tahoe_gb300 import lib, rve
     ns, Fs = rve.sample_batch(args.rves, seed=0)
     t0 = time.perf_counter()
-    b = rve.RVEBatch(ns, Fs)
-    c = b.setup()
+    c = lib.Context(0)
+    res = rve.ResidentRVEs(c)
+    for n in np.unique(ns):
+        res.template_id(n)
     t_setup = time.perf_counter() - t0
+    precond = lib.PRECOND_BLOCK_JACOBI if args.precond == "block" else lib.PRECOND_JACOBI
     out = {}
     for name, prec in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
-        b.solve(precision=prec)  # warm-up: buffers, graphs
+        res.solve(ns, Fs, precision=prec, precond=precond)  # warm-up: pools, graphs
         c.timer_start()
-        rc, rep, rel, P = b.solve(precision=prec)
+        rc, rep, rel, P = res.solve(ns, Fs, precision=prec, precond=precond)
         ms = c.timer_stop()
         out[name] = dict(ms=ms, rc=rc, newton=rep.iterations, pcg=rep.pcg_iterations, worst_rel=float(rel.max()),
                          P=P, ms_tangent=rep.ms_tangent, ms_solve=rep.ms_solve, ms_residual=rep.ms_residual)
+    b = argparse.Namespace(nel=c.nel, nnd=c.nnd)
     Pm, Pf = out["mixed"]["P"], out["fp64"]["P"]
     err = float(np.abs(Pm - Pf).max() / np.abs(Pf).max())
     per_rve = np.abs(Pm - Pf).reshape(len(ns), -1).max(axis=1) / np.abs(Pf).reshape(len(ns), -1).max(axis=1)
@@ -403,7 +409,8 @@ def run_c4(args):
         "status": {k: v["rc"] for k, v in out.items()},
         "P_rel_err_mixed_vs_fp64": err,
         "P_rel_err_mixed_vs_fp64_worst_rve": float(per_rve.max()),
-        "setup_s": round(t_setup, 2),
+        "template_setup_s": round(t_setup, 3),
+        "precond": args.precond,
     }
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -450,6 +457,13 @@ def run_c5(args):
                            "p50_ms": round(ref["p50_ms"], 2), "p99_ms": round(ref["p99_ms"], 2)},
             "P_rel_err_vs_plain_fp64_worst": float(d[both].max()) if both.any() else None,
         })
+        if res["retried"]:
+            sweep[-1]["retried_alone"] = res["retried"]
+            sweep[-1]["batch_failures"] = [[f[0], f[1][:120], f[2][:12], f[3]] for f in res["failures"][:3]]
+        if res["completed"] < len(ns):
+            codes, counts = np.unique(res["status"][res["status"] != 0], return_counts=True)
+            sweep[-1]["failed"] = {int(k): int(v) for k, v in zip(codes, counts)}
+            sweep[-1]["errors"] = [e[2][:200] for e in res["errors"][:3]]
     srv.close()
     plain.close()
     top = max(sweep, key=lambda r: r["solves_per_s"])
@@ -504,6 +518,7 @@ def main():
     ap.add_argument("--plain-requests", type=int, default=200, help="C5 requests for the one-at-a-time arm")
     ap.add_argument("--lanes", type=int, default=4)
     ap.add_argument("--max-batch", type=int, default=1024)
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "block"])
     args = ap.parse_args()
     if args.workload == "c4" and args.impl == "ours":
         run_c4(args)

@@ -31,9 +31,8 @@ namespace {
 // released only with the context (freeing pinned memory can synchronise the
 // device).
 void free_device(Context* c) {
-  if (c->ev_a) cudaEventDestroy(c->ev_a);
-  if (c->ev_b) cudaEventDestroy(c->ev_b);
-  c->ev_a = c->ev_b = nullptr;
+  // the caller's timer events outlive mesh changes (a timed region may
+  // cover composing a batch mesh)
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
@@ -350,12 +349,14 @@ int build_tiles(Context* c, int tile_blocks) {
   if (!dalloc(c, &c->d_tile_row, tiles.size()) || !dalloc(c, &c->d_row_tile, (size_t)c->nnd) ||
       !dalloc(c, &c->d_blob_off32, (size_t)nt + 1) || !dalloc(c, &c->d_blob_off64, (size_t)nt + 1))
     return TG_ERR_OOM;
-  if (!ok(c, cudaMemcpy(c->d_tile_row, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice), "tiles") ||
-      !ok(c, cudaMemcpy(c->d_row_tile, row_tile.data(), sizeof(int) * c->nnd, cudaMemcpyHostToDevice), "rows") ||
-      !ok(c, cudaMemcpy(c->d_blob_off32, c->h_blob_off32.data(), sizeof(long long) * (nt + 1), cudaMemcpyHostToDevice),
+  cudaStream_t st = c->stream;
+  if (!ok(c, cudaMemcpyAsync(c->d_tile_row, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice, st), "tiles") ||
+      !ok(c, cudaMemcpyAsync(c->d_row_tile, row_tile.data(), sizeof(int) * c->nnd, cudaMemcpyHostToDevice, st), "rows") ||
+      !ok(c, cudaMemcpyAsync(c->d_blob_off32, c->h_blob_off32.data(), sizeof(long long) * (nt + 1), cudaMemcpyHostToDevice, st),
           "off") ||
-      !ok(c, cudaMemcpy(c->d_blob_off64, c->h_blob_off64.data(), sizeof(long long) * (nt + 1), cudaMemcpyHostToDevice),
-          "off"))
+      !ok(c, cudaMemcpyAsync(c->d_blob_off64, c->h_blob_off64.data(), sizeof(long long) * (nt + 1), cudaMemcpyHostToDevice, st),
+          "off") ||
+      !ok(c, cudaStreamSynchronize(st), "sync"))
     return TG_ERR_CUDA;
   // the captured PCG chunk bakes in the launch shape
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
@@ -422,7 +423,10 @@ int tg_element_blocks(tg_context* c, const int* blocks) {
   if (set_device(c)) return TG_ERR_CUDA;
   if (!c->d_block && !dalloc(c, &c->d_block, (size_t)c->nel)) return TG_ERR_OOM;
   c->have_blocks = true;
-  return ok(c, cudaMemcpy(c->d_block, b.data(), c->nel, cudaMemcpyHostToDevice), "blocks") ? TG_OK : TG_ERR_CUDA;
+  return ok(c, cudaMemcpyAsync(c->d_block, b.data(), c->nel, cudaMemcpyHostToDevice, c->stream), "blocks") &&
+                 ok(c, cudaStreamSynchronize(c->stream), "sync")
+             ? TG_OK
+             : TG_ERR_CUDA;
 }
 
 int tg_sizes(const tg_context* c, int* neq, long long* nnzb) {

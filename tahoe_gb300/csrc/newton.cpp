@@ -20,6 +20,14 @@ namespace {
 
 int set_device(Context* c) { return ok(c, cudaSetDevice(c->device), "cudaSetDevice") ? TG_OK : TG_ERR_CUDA; }
 
+// A copy ordered after everything queued on the context stream, complete on
+// return (a plain cudaMemcpy runs on the legacy stream, which does not wait
+// for the context's non-blocking stream).
+bool copy_sync(Context* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, const char* what) {
+  return ok(c, cudaMemcpyAsync(dst, src, bytes, kind, c->stream), what) &&
+         ok(c, cudaStreamSynchronize(c->stream), what);
+}
+
 int check_status(Context* c) {
   if (!ok(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "status") ||
       !ok(c, cudaStreamSynchronize(c->stream), "sync"))
@@ -113,7 +121,7 @@ int tg_get_tangent_csr(tg_context* c, int upper_only, double* vals) {
   const bool f32 = c->tangent_precision == TG_MIXED;
   const std::vector<long long>& off = f32 ? c->h_blob_off32 : c->h_blob_off64;
   std::vector<unsigned char> h((size_t)off[c->ntiles]);
-  if (!ok(c, cudaMemcpy(h.data(), f32 ? c->d_blob32 : c->d_blob64, h.size(), cudaMemcpyDeviceToHost), "blob"))
+  if (!copy_sync(c, h.data(), f32 ? c->d_blob32 : c->d_blob64, h.size(), cudaMemcpyDeviceToHost, "blob"))
     return TG_ERR_CUDA;
   auto value = [&](int I, int k, int pq) -> double {
     int t = 0;
@@ -233,19 +241,19 @@ int tg_reset_step(tg_context* c) {
 int tg_get_active_set(tg_context* c, signed char* flags) {
   if (!c || !flags || c->nel <= 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
-  return ok(c, cudaMemcpy(flags, c->d_j2_flags, (size_t)c->nel * 8, cudaMemcpyDeviceToHost), "flags") ? TG_OK
-                                                                                                      : TG_ERR_CUDA;
+  return copy_sync(c, flags, c->d_j2_flags, (size_t)c->nel * 8, cudaMemcpyDeviceToHost, "flags") ? TG_OK
+                                                                                                    : TG_ERR_CUDA;
 }
 
 int tg_get_j2_state(tg_context* c, double* alpha, double* eps_p) {
   if (!c || c->nel <= 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
   const size_t nip = (size_t)c->nel * 8;
-  if (alpha && !ok(c, cudaMemcpy(alpha, c->d_j2_alpha, sizeof(double) * nip, cudaMemcpyDeviceToHost), "alpha"))
+  if (alpha && !copy_sync(c, alpha, c->d_j2_alpha, sizeof(double) * nip, cudaMemcpyDeviceToHost, "alpha"))
     return TG_ERR_CUDA;
   if (eps_p) {
     std::vector<double> h(nip * 6);
-    if (!ok(c, cudaMemcpy(h.data(), c->d_j2_epsp, sizeof(double) * nip * 6, cudaMemcpyDeviceToHost), "epsp"))
+    if (!copy_sync(c, h.data(), c->d_j2_epsp, sizeof(double) * nip * 6, cudaMemcpyDeviceToHost, "epsp"))
       return TG_ERR_CUDA;
     for (size_t g = 0; g < nip; ++g)
       for (int k = 0; k < 6; ++k) eps_p[g * 6 + k] = h[k * nip + g];
@@ -436,8 +444,8 @@ int tg_set_segments(tg_context* c, int nseg, const int* node_off, const int* ele
   if (!dalloc(c, &c->d_seg_node, (size_t)nseg + 1) || !dalloc(c, &c->d_seg_elem, (size_t)nseg + 1) ||
       !dalloc(c, &c->d_seg_out, (size_t)nseg * 9))
     return TG_ERR_OOM;
-  return ok(c, cudaMemcpy(c->d_seg_node, node_off, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice), "seg") &&
-                 ok(c, cudaMemcpy(c->d_seg_elem, elem_off, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice), "seg")
+  return copy_sync(c, c->d_seg_node, node_off, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, "seg") &&
+                 copy_sync(c, c->d_seg_elem, elem_off, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, "seg")
              ? TG_OK
              : TG_ERR_CUDA;
 }

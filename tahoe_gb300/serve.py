@@ -54,6 +54,10 @@ def gpu_batch_solver(precision=lib.MIXED, rel_tol=1e-8, lin_rel_tol=1e-4):
             lane_state["rves"] = res
         rc, rep, rel, P = res.solve(ns, Fs, precision=precision, rel_tol=rel_tol, lin_rel_tol=lin_rel_tol)
         ok = (np.asarray(rel) < rel_tol) if rc == 0 else np.zeros(len(ns), dtype=bool)
+        if not ok.all():
+            lane_state.setdefault("failures", []).append(
+                (rc, lane_state["ctx"].L.tg_last_error(lane_state["ctx"].h).decode(), list(map(int, ns)),
+                 float(np.max(rel)) if len(rel) else None))
         return np.where(ok, 0, rc if rc != 0 else -6), P
 
     return solve
@@ -77,12 +81,13 @@ class Server:
         time_scale); returns a dict of per-request results and statistics."""
         count = len(arrivals)
         lock = threading.Lock()
-        state = {"next": 0, "ready": [], "inflight": 0.0, "done": 0, "peak": 0.0}
+        state = {"next": 0, "ready": [], "inflight": 0.0, "done": 0, "peak": 0.0, "retried": 0}
         start = np.full(count, np.nan)
         finish = np.full(count, np.nan)
         status = np.zeros(count, dtype=np.int64)
         P = np.full((count, 3, 3), np.nan)
         batches = []
+        errors = []
         need = np.array([self.bytes_fn(n) for n in ns])
         t0 = time.perf_counter()
 
@@ -123,8 +128,24 @@ class Server:
                 start[take] = ts
                 try:
                     st, Pb = self.solve_batch(ns[take], Fs[take], lane_state)
-                except Exception:  # a failed batch reports its requests and the lane carries on
+                except Exception as e:  # a failed batch reports its requests and the lane carries on
                     st, Pb = np.full(len(take), -2), np.full((len(take), 3, 3), np.nan)
+                    with lock:
+                        errors.append((lid, len(take), str(e)))
+                st = np.asarray(st)
+                bad = np.nonzero(st != 0)[0]
+                if len(take) > 1 and len(bad):
+                    # requests of a failed batch are retried alone
+                    for j in bad:
+                        rid = take[j]
+                        try:
+                            s1, P1 = self.solve_batch(ns[[rid]], Fs[[rid]], lane_state)
+                            st[j], Pb[j] = s1[0], P1[0]
+                        except Exception as e:
+                            with lock:
+                                errors.append((lid, 1, str(e)))
+                    with lock:
+                        state["retried"] += len(bad)
                 te = now()
                 with lock:
                     finish[take] = te
@@ -151,6 +172,9 @@ class Server:
             "mean_batch": float(np.mean([b[1] for b in batches])) if batches else 0.0,
             "max_concurrent_lanes": _max_overlap(batches),
             "peak_inflight_bytes": state["peak"],
+            "errors": errors,
+            "retried": state["retried"],
+            "failures": [f for st in self.lane_states for f in st.get("failures", [])],
         }
 
 
