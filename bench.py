@@ -189,6 +189,13 @@ def run_ours(args):
     from tahoe_gb300 import lib, workloads
     prec = lib.MIXED if args.precision == "mixed" else lib.FP64
     mesh, model, ctx = setup_c2(local, prec)
+    tuning = None
+    if not args.no_tune:
+        # launch shapes picked by the autotuner on this mesh and state
+        from tahoe_gb300 import autotune
+        t = autotune.Tuner(reps=20)
+        tuning = t.tune(ctx, prec, lib.TOTAL_LAGRANGIAN)
+        tuning = {k: tuning[k] for k in ("tile_blocks", "stages", "tangent_epb", "spmv_ms", "tangent_ms", "cached")}
 
     # warm-up (also captures the PCG graph)
     its_seen = []
@@ -295,6 +302,7 @@ def run_ours(args):
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/Newton iteration", "h2d_bytes_per_step": nnd * 32,
                 "d2h_bytes_per_step": nnd * 32},
         "gpu_launches": int(launches),
+        "tuning": tuning,
         "clocks": clocks,
     }
     line.update(extra)
@@ -387,6 +395,10 @@ def run_c4(args):
         ms = c.timer_stop()
         out[name] = dict(ms=ms, rc=rc, newton=rep.iterations, pcg=rep.pcg_iterations, worst_rel=float(rel.max()),
                          P=P, ms_tangent=rep.ms_tangent, ms_solve=rep.ms_solve, ms_residual=rep.ms_residual)
+        # consistent macro tangent of every RVE at the converged state
+        c.timer_start()
+        Cm, cits = c.macro_tangent(np.ones(len(ns)), precision=prec, precond=precond, lin_rel_tol=1e-7)
+        out[name].update(C=Cm, ms_macro=c.timer_stop(), macro_pcg=cits)
     b = argparse.Namespace(nel=c.nel, nnd=c.nnd)
     Pm, Pf = out["mixed"]["P"], out["fp64"]["P"]
     err = float(np.abs(Pm - Pf).max() / np.abs(Pf).max())
@@ -408,6 +420,10 @@ def run_c4(args):
         "worst_rve_rel_residual": {k: v["worst_rel"] for k, v in out.items()},
         "status": {k: v["rc"] for k, v in out.items()},
         "P_rel_err_mixed_vs_fp64": err,
+        "macro_tangent_ms": {k: round(v["ms_macro"], 2) for k, v in out.items()},
+        "macro_tangent_pcg_iterations": {k: v["macro_pcg"] for k, v in out.items()},
+        "macro_tangent_rel_err_mixed_vs_fp64": float(np.abs(out["mixed"]["C"] - out["fp64"]["C"]).max() /
+                                                     np.abs(out["fp64"]["C"]).max()),
         "P_rel_err_mixed_vs_fp64_worst_rve": float(per_rve.max()),
         "template_setup_s": round(t_setup, 3),
         "precond": args.precond,
@@ -507,6 +523,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--quick", action="store_true", help="skip the full load-step comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shapes, no autotuning")
     ap.add_argument("--ref-pcg-iters", type=int, default=600)
     ap.add_argument("--kernel", choices=sorted(KERNELS), help="time standalone launches of one kernel only")
     ap.add_argument("--launches", type=int, default=3)

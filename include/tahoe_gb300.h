@@ -241,6 +241,17 @@ int tg_segment_average_stress(tg_context* ctx, const double* vol0, double* P);
  * seg_rel (nseg, may be NULL) receives each RVE's final relative residual. */
 int tg_newton_solve_segmented(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report,
                               double* seg_rel);
+/* Consistent macro tangent dP/dF of every RVE at the current (converged)
+ * state, by static condensation onto the prescribed boundary dofs: for each
+ * of the nine unit perturbations dF = e_k (x) e_L the interior response
+ * K_ii du_i = -K_ib (dF X)_b is solved (PCG with params' precision,
+ * preconditioner, lin_rel_tol, lin_max_it) and dP = (1/V0) sum_a (K du)_a (x)
+ * X_a.  C is nseg*81 doubles, C[s*81 + (3j+J)*9 + (3k+L)] = dP_jJ/dF_kL;
+ * vol0 as for tg_segment_average_stress.  No reference counterpart (FE^2 is
+ * not in the reference; the definition is checked against finite
+ * differences of the averaged stress). */
+int tg_segment_macro_tangent(tg_context* ctx, const tg_newton_params* params, const double* vol0, double* C,
+                             int* pcg_iterations);
 
 /* ---- resident templates and composed batch meshes ----------------------
  * No reference counterpart (serving side of the FE^2 batch): a mesh used
@@ -273,6 +284,11 @@ int tg_predict_affine(tg_context* ctx, const double* F, const tg_newton_params* 
  * through a ring of `stages` (2 or 3) shared-memory buffers.  Defaults
  * 640 / 2.  Changing the tile size drops the assembled tangent. */
 int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
+/* elements per CTA of the tangent kernel: 2, 4 or 8 (default 8); element
+ * matrices are bitwise the same for every choice */
+int tg_tangent_config(tg_context* ctx, int elems_per_block);
+/* the current launch shapes (any pointer may be NULL) */
+int tg_tuning_get(const tg_context* ctx, int* tile_blocks, int* stages, int* tangent_elems_per_block);
 
 /* CUDA events on the context stream around caller-defined work */
 int tg_timer_start(tg_context* ctx);

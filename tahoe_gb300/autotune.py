@@ -1,0 +1,110 @@
+"""Launch-shape autotuner for the hot kernels.
+
+Two shapes are tuned on the mesh a context holds, by timing the kernels
+themselves (CUDA events, tg_time_kernel) on the current state:
+
+  * the streamed PCG product: rows per tile (the unit of the tile-contiguous
+    matrix storage, in block nonzeros) x depth of the shared-memory ring;
+  * the element tangent: elements per CTA (one thread per upper node-pair
+    block of each element).
+
+Results are cached per (GPU, precision, formulation, mesh-size bucket) in a
+JSON table, so a serving process tunes once per kind of mesh.  Element
+matrices do not depend on the tangent shape (bitwise), and a different tile
+size only regroups rows, so tuning changes timings, not results beyond the
+rounding order of the Krylov dot products.
+"""
+import json
+import math
+import os
+
+from . import lib
+
+SPMV_TILES = (256, 384, 512, 640, 768, 1024, 1536)
+SPMV_STAGES = (2, 3)
+TANGENT_EPB = (2, 4, 8)
+KERNEL_SPMV, KERNEL_TANGENT = 0, 2
+
+_DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tuning.json")
+
+
+def signature(ctx, precision, formulation, gpu="gpu0"):
+    """Cache key: mesh sizes bucketed to powers of two (shapes are chosen for
+    the size class, not the exact mesh)."""
+    b = lambda x: 1 << max(0, int(math.log2(max(1, x))))
+    return "%s|p%d|f%d|nnd%d|nel%d" % (gpu, precision, formulation, b(ctx.nnd), b(ctx.nel))
+
+
+def pick(timings):
+    """Fastest candidate of {config: ms}; ties go to the first listed."""
+    best, best_ms = None, float("inf")
+    for cfg, ms in timings.items():
+        if ms is not None and ms < best_ms:
+            best, best_ms = cfg, ms
+    return best, best_ms
+
+
+class Tuner:
+    def __init__(self, cache_path=_DEFAULT_CACHE, reps=20, tiles=SPMV_TILES, stages=SPMV_STAGES, epbs=TANGENT_EPB):
+        self.cache_path = cache_path
+        self.reps = reps
+        self.tiles, self.stages, self.epbs = tiles, stages, epbs
+        self.table = {}
+        if cache_path and os.path.exists(cache_path):
+            try:
+                with open(cache_path) as f:
+                    self.table = json.load(f)
+            except (OSError, ValueError):
+                self.table = {}
+
+    def save(self):
+        if not self.cache_path:
+            return
+        os.makedirs(os.path.dirname(self.cache_path), exist_ok=True)
+        tmp = self.cache_path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(self.table, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.cache_path)
+
+    @staticmethod
+    def apply(ctx, cfg):
+        ctx.spmv_config(cfg["tile_blocks"], cfg["stages"])
+        ctx.tangent_config(cfg["tangent_epb"])
+
+    def tune(self, ctx, precision, formulation, gpu="gpu0", force=False, timer=None):
+        """Tunes (or takes from the cache) and applies the shapes; returns the
+        chosen config with the measured timings.  The context must hold a
+        mesh and a state on which a tangent can be formed.  `timer(ctx, which,
+        reps)` defaults to the library's kernel timer."""
+        key = signature(ctx, precision, formulation, gpu)
+        if not force and key in self.table:
+            cfg = self.table[key]
+            self.apply(ctx, cfg)
+            return dict(cfg, cached=True)
+        timer = timer or (lambda c, which, reps: c.time_kernel(which, reps))
+        spmv = {}
+        for t in self.tiles:
+            for s in self.stages:
+                try:
+                    ctx.spmv_config(t, s)
+                    ctx.tangent(precision)  # assemble into the new tile layout
+                    spmv[(t, s)] = timer(ctx, KERNEL_SPMV, self.reps)
+                except lib.TahoeError:
+                    spmv[(t, s)] = None  # ring does not fit on an SM
+        (tb, st), spmv_ms = pick(spmv)
+        ctx.spmv_config(tb, st)
+        ctx.tangent(precision)
+        tang = {}
+        for e in self.epbs:
+            ctx.tangent_config(e)
+            tang[e] = timer(ctx, KERNEL_TANGENT, max(3, self.reps // 4))
+        epb, tang_ms = pick(tang)
+        cfg = {"tile_blocks": tb, "stages": st, "tangent_epb": epb, "spmv_ms": spmv_ms, "tangent_ms": tang_ms}
+        self.apply(ctx, cfg)
+        ctx.tangent(precision)
+        self.table[key] = cfg
+        self.save()
+        out = dict(cfg, cached=False)
+        out["spmv_sweep"] = {"%dx%d" % k: v for k, v in spmv.items()}
+        out["tangent_sweep"] = {str(k): v for k, v in tang.items()}
+        return out

@@ -35,7 +35,8 @@ def _stale():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = _sources() + glob.glob(os.path.join(SRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    deps = (_sources() + glob.glob(os.path.join(SRC, "*.h")) + glob.glob(os.path.join(SRC, "*.cuh")) +
+            glob.glob(os.path.join(INCLUDE, "*.h")))
     return any(os.path.getmtime(p) > t for p in deps)
 
 

@@ -392,6 +392,20 @@ int tg_spmv_config(tg_context* c, int tile_blocks, int stages) {
   return build_tiles(c, tile_blocks);
 }
 
+int tg_tangent_config(tg_context* c, int elems_per_block) {
+  if (!c || (elems_per_block != 2 && elems_per_block != 4 && elems_per_block != 8)) return TG_ERR_ARG;
+  c->tangent_epb = elems_per_block;
+  return TG_OK;
+}
+
+int tg_tuning_get(const tg_context* c, int* tile_blocks, int* stages, int* tangent_elems_per_block) {
+  if (!c) return TG_ERR_ARG;
+  if (tile_blocks) *tile_blocks = c->spmv_tile_blocks;
+  if (stages) *stages = c->spmv_stages;
+  if (tangent_elems_per_block) *tangent_elems_per_block = c->tangent_epb;
+  return TG_OK;
+}
+
 int tg_element_set(tg_context* c, int formulation) {
   if (!c || (formulation != TG_SMALL_STRAIN && formulation != TG_TOTAL_LAGRANGIAN)) return TG_ERR_ARG;
   c->formulation = formulation;

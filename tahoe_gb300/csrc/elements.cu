@@ -497,8 +497,9 @@ __global__ void __launch_bounds__(256) gather_residual_kernel(
 // ---------------------------------------------------------------------------
 // tangent
 // ---------------------------------------------------------------------------
-constexpr int kTanElems = 8;                   // elements per CTA
-constexpr int kTanThreads = kTanElems * kSlots;  // 288
+// elements per CTA (kTanElems by default; 2 and 4 selectable through
+// tg_tangent_config); one thread per upper node-pair block of each element
+constexpr int kTanElems = 8;
 
 __device__ __forceinline__ void slot_pair(int slot, int& a, int& b) {
   int start = 0;
@@ -514,8 +515,8 @@ __device__ __forceinline__ void slot_pair(int slot, int& a, int& b) {
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kTanThreads) tangent_kernel(const double* __restrict__ X, int nnd,
+template <typename T, int kTanElems>
+__global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const double* __restrict__ X, int nnd,
                                                               const int* __restrict__ conn,
                                                               const int8_t* __restrict__ blk, int nel,
                                                               const double4_32a* __restrict__ u, MatTable mt,
@@ -719,14 +720,22 @@ int launch_residual_commit(Context* c, int commit) {
   return ok(c, cudaGetLastError(), "gather_residual_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
+template <int EPB>
+void launch_tangent_epb(Context* c, int precision) {
+  const int grid = (c->nel + EPB - 1) / EPB;
+  if (precision == TG_MIXED)
+    tangent_kernel<float, EPB><<<grid, EPB * kSlots, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel,
+                                                                     c->d_u, c->mats, j2view(c), c->d_Ke32, c->d_status);
+  else
+    tangent_kernel<double, EPB><<<grid, EPB * kSlots, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel,
+                                                                      c->d_u, c->mats, j2view(c), c->d_Ke64, c->d_status);
+}
+
 int launch_tangent(Context* c, int precision) {
-  const int grid = (c->nel + kTanElems - 1) / kTanElems;
-  if (precision == TG_MIXED) {
-    tangent_kernel<float><<<grid, kTanThreads, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u,
-                                                               c->mats, j2view(c), c->d_Ke32, c->d_status);
-  } else {
-    tangent_kernel<double><<<grid, kTanThreads, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u,
-                                                                c->mats, j2view(c), c->d_Ke64, c->d_status);
+  switch (c->tangent_epb) {
+    case 2: launch_tangent_epb<2>(c, precision); break;
+    case 4: launch_tangent_epb<4>(c, precision); break;
+    default: launch_tangent_epb<kTanElems>(c, precision); break;
   }
   c->launches++;
   return ok(c, cudaGetLastError(), "tangent_kernel") ? TG_OK : TG_ERR_CUDA;

@@ -477,6 +477,35 @@ int tg_segment_average_stress(tg_context* c, const double* vol0, double* P) {
   return s;
 }
 
+int tg_segment_macro_tangent(tg_context* c, const tg_newton_params* P, const double* vol0, double* C,
+                             int* pcg_iterations) {
+  if (!c || !P || !C || c->nseg <= 0 || c->nnd <= 0) return TG_ERR_ARG;
+  if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  if (pcg_iterations) *pcg_iterations = 0;
+  // tangent at the current (converged) state
+  int s = form_tangent(c, P->precision);
+  if (s) return s;
+  double *d_vol = nullptr, *d_C = nullptr;
+  if (!ok(c, cudaMallocAsync((void**)&d_C, sizeof(double) * 81 * c->nseg, c->stream), "alloc") ||
+      (vol0 && !ok(c, cudaMallocAsync((void**)&d_vol, sizeof(double) * c->nseg, c->stream), "alloc")))
+    return TG_ERR_OOM;
+  if (vol0 && !ok(c, cudaMemcpyAsync(d_vol, vol0, sizeof(double) * c->nseg, cudaMemcpyHostToDevice, c->stream), "vol"))
+    s = TG_ERR_CUDA;
+  int total = 0;
+  // columns kL: boundary perturbations v = dF X with dF = e_k (x) e_L,
+  // interior responses K_ii du_i = -K_ib v_b (nine right-hand sides, one
+  // multi-vector PCG), dP = (1/V0) sum_a (K w)_a (x) X_a with w = v + du
+  if (!s) s = macro_tangent_mrhs(c, P->precision, P->precond, P->lin_rel_tol, P->lin_max_it, d_vol, d_C, &total);
+  if (!s && !ok(c, cudaMemcpyAsync(C, d_C, sizeof(double) * 81 * c->nseg, cudaMemcpyDeviceToHost, c->stream), "C"))
+    s = TG_ERR_CUDA;
+  for (void* p : {(void*)d_C, (void*)d_vol})
+    if (p) cudaFreeAsync(p, c->stream);
+  if (!ok(c, cudaStreamSynchronize(c->stream), "sync") && !s) s = TG_ERR_CUDA;
+  if (pcg_iterations) *pcg_iterations = total;
+  return s;
+}
+
 int tg_newton_solve_segmented(tg_context* c, const tg_newton_params* P, tg_newton_report* rep, double* seg_rel) {
   if (!c || !P || c->nseg <= 0) return TG_ERR_ARG;
   if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
@@ -575,7 +604,10 @@ int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
   if (!c || reps <= 0 || !ms || which < 0 || which > 4) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
   if (which <= 1) return time_pcg_kernel(c, which, reps, ms);
-  if ((which == 2 || which == 3) && c->tangent_precision < 0) return TG_ERR_ARG;
+  if ((which == 2 || which == 3) && c->tangent_precision < 0) {
+    c->err = "form a tangent first (its precision is the one timed)";
+    return TG_ERR_ARG;
+  }
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);

@@ -99,6 +99,7 @@ struct Context {
   int* d_tile_row = nullptr;
   int spmv_tile_blocks = kTileBlocks;
   int spmv_stages = 2;
+  int tangent_epb = 8;         // elements per CTA of the tangent kernel (2, 4, 8)
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
   std::vector<int> h_rowptr, h_col;
@@ -235,6 +236,15 @@ int launch_blob_structure(Context* c, int precision);
 // segmented (per-RVE) reductions over node / element ranges
 int launch_segment_norms(Context* c, int nseg, const int* d_node_off, double* d_out);
 int launch_segment_stress(Context* c, int nseg, const int* d_elem_off, double* d_out);
+// macro tangent of every segment (static condensation by nine solves)
+int launch_macro_perturb(Context* c, int k, int L, double4_32a* d_v);
+int launch_macro_combine(Context* c, const double4_32a* d_v, double4_32a* d_w);
+// columns kL .. kL+ncols-1 of the macro tangent; d_w holds ncols nodal vectors
+int launch_segment_macro(Context* c, const double4_32a* d_w, int kL, int ncols, const double* d_vol0,
+                         double* d_out);
+// the nine condensation solves as one multi-vector PCG (mrhs.cu)
+int macro_tangent_mrhs(Context* c, int precision, int precond, double rel_tol, int max_it, const double* d_vol,
+                       double* d_C, int* iters);
 int form_tangent(Context* c, int precision);
 int launch_element_dump(Context* c, int first, int count, double* dKe, double* dfint);
 int launch_close_step(Context* c, int reset);
@@ -250,8 +260,9 @@ size_t pcg_scratch_bytes(const Context* c);
 int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
                       int max_it, int precond, int* iters, double* rel_res);
 int launch_residual_nocommit(Context* c);
-// rhs = R - K v on active rows (v nodal, K the last tangent), FP64 accumulation
-int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs);
+// rhs = R - K v on active rows (v nodal, K the last tangent), FP64
+// accumulation; with zero_base, rhs = -K v
+int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs, bool zero_base = false, int nvec = 1);
 int launch_diff(Context* c, const double4_32a* a, const double4_32a* b, double4_32a* out);
 int launch_gather_eq(Context* c, const double4_32a* d_nodal, double* d_eq);
 int launch_scatter_eq(Context* c, const double* d_eq, double4_32a* d_nodal);

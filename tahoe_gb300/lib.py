@@ -79,11 +79,14 @@ _SIGS = {
     "tg_timer_stop": (ctypes.c_int, [_vp, _dp]),
     "tg_time_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     "tg_spmv_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "tg_tangent_config": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
     "tg_segment_residual_norms": (ctypes.c_int, [_vp, _dp]),
     "tg_segment_average_stress": (ctypes.c_int, [_vp, _dp, _dp]),
     "tg_newton_solve_segmented": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), ctypes.POINTER(NewtonReport),
                                                  _dp]),
+    "tg_segment_macro_tangent": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), _dp, _dp, _ip]),
     "tg_template_add": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, _ip]),
     "tg_mesh_compose": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
     "tg_set_affine_prescribed": (ctypes.c_int, [_vp, _dp]),
@@ -398,8 +401,27 @@ class Context:
             self._chk(rc, "tg_newton_solve_segmented")
         return rc, R, rel
 
+    def macro_tangent(self, vol0=None, precision=MIXED, precond=PRECOND_JACOBI, lin_rel_tol=1e-8, lin_max_it=20000):
+        """(nseg, 9, 9) consistent macro tangents dP_jJ/dF_kL at the current
+        state, and the PCG iterations of the nine solves."""
+        P = NewtonParams(0.0, 0.0, 1e30, 1 << 30, precision, precond, lin_rel_tol, lin_max_it)
+        C = np.zeros(self.nseg * 81)
+        v = None if vol0 is None else np.ascontiguousarray(vol0, dtype=np.float64)
+        its = ctypes.c_int(0)
+        self._chk(self.L.tg_segment_macro_tangent(self.h, ctypes.byref(P), _d(v), _d(C), ctypes.byref(its)),
+                  "tg_segment_macro_tangent")
+        return C.reshape(-1, 9, 9), its.value
+
     def spmv_config(self, tile_blocks, stages):
         self._chk(self.L.tg_spmv_config(self.h, int(tile_blocks), int(stages)), "tg_spmv_config")
+
+    def tangent_config(self, elems_per_block):
+        self._chk(self.L.tg_tangent_config(self.h, int(elems_per_block)), "tg_tangent_config")
+
+    def tuning(self):
+        t, s, e = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        self._chk(self.L.tg_tuning_get(self.h, ctypes.byref(t), ctypes.byref(s), ctypes.byref(e)), "tg_tuning_get")
+        return {"tile_blocks": t.value, "stages": s.value, "tangent_epb": e.value}
 
     def time_kernel(self, which, reps):
         ms = ctypes.c_double(0)

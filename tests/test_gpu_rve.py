@@ -76,3 +76,30 @@ def test_rve_alone_equals_rve_in_batch(batch):
         rc1, rep1, rel1, P1 = one.solve(precision=lib.MIXED, rel_tol=1e-8)
         assert rc1 == 0
         assert rel_err(P1[0], P[r]) < 1e-6, r
+
+
+def test_macro_tangent_matches_oracle_finite_differences(batch):
+    """dP/dF by static condensation on the GPU against central differences of
+    the oracle's averaged stress (reaction sum), per RVE; major symmetry of the
+    hyperelastic tangent; mixed form against FP64."""
+    ns, Fs = batch
+    ns, Fs = ns[:2], Fs[:2]
+    b = rve.RVEBatch(ns, Fs)
+    b.setup()
+    rc, rep, rel, P = b.solve(precision=lib.FP64, rel_tol=1e-12, lin_rel_tol=1e-12)
+    assert rc == 0
+    C64, its = b.ctx.macro_tangent(b.vol0, precision=lib.FP64, lin_rel_tol=1e-12)
+    assert its > 0
+    h = 1e-5
+    for r, (n, F) in enumerate(zip(ns, Fs)):
+        Cfd = np.zeros((9, 9))
+        for kL in range(9):
+            dF = np.zeros(9)
+            dF[kL] = h
+            Pp = oracle_rve(int(n), F + dF.reshape(3, 3))[1]
+            Pm = oracle_rve(int(n), F - dF.reshape(3, 3))[1]
+            Cfd[:, kL] = (Pp - Pm).reshape(9) / (2 * h)
+        assert rel_err(C64[r], Cfd) < 1e-6, r
+        assert rel_err(C64[r], C64[r].T) < 1e-9, r
+    Cm, _ = b.ctx.macro_tangent(b.vol0, precision=lib.MIXED, lin_rel_tol=1e-7)
+    assert rel_err(Cm, C64) < 1e-5
