@@ -496,6 +496,75 @@ def run_c5(args):
     print(json.dumps(line))
 
 
+def run_c3(args):
+    """Configuration 3: small-strain J2 plate 96 x 96 x 48 under cyclic
+    uniaxial displacement (+-0.5 % strain over 40 steps).  Both forms run the
+    same load history through the reference's step sequence (Newton to 1e-8
+    per step, Jacobi-PCG, load-step cuts where Newton fails); the final active
+    (yielding) set of the mixed form is compared bitwise with the plain FP64
+    form's, and the displacements at every original step end are compared."""
+    from tahoe_gb300 import autotune, lib, workloads
+    nsteps = args.c3_steps
+    out, flags_ref, u_last = {}, {}, {}
+    for name, prec in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
+        mesh, model, run = workloads.c3(nsteps=40)
+        model.setup()
+        c = model.ctx
+        if not args.no_tune:
+            # shapes tuned on the undeformed state (tangents only: no residual
+            # is formed, so no history is touched)
+            c.set_iteration(-1)
+            autotune.Tuner(reps=10).tune(c, prec, lib.SMALL_STRAIN)
+        rec = dict(newton=[], pcg=[], mismatch=[])
+        c.timer_start()
+        hist, reps = model.run(nsteps, 1.0, rel_tol=1e-8, abs_tol=1e-10, max_iterations=12, div_tol=1e3,
+                               precision=prec, precond=lib.PRECOND_JACOBI, lin_rel_tol=1e-4, lin_max_it=50000,
+                               max_step_cuts=args.max_step_cuts, quick_solve_iter=args.quick_solve_iter)
+        total_ms = c.timer_stop()
+        rec["total_ms"] = total_ms
+        rec["cuts"] = model.step_cuts
+        for r in reps:
+            rs = r if isinstance(r, list) else [r]
+            rec["newton"].append(sum(x.iterations for x in rs))
+            rec["pcg"].append(sum(x.pcg_iterations for x in rs))
+        fl = c.active_set()
+        rec["flags_final"] = {str(k): int((fl == k).sum()) for k in (0, 1, 3, 7)}
+        if name == "mixed":
+            flags_ref["final"] = fl
+        else:
+            rec["mismatch"].append(int((fl != flags_ref["final"]).sum()))
+        u_last[name] = hist
+        out[name] = rec
+        c.close()
+    m, f = out["mixed"], out["fp64"]
+    tot = {k: v["total_ms"] for k, v in out.items()}
+    its = {k: sum(v["newton"]) for k, v in out.items()}
+    line = {
+        "metric": "Newton-step time", "value": round(tot["mixed"] / max(its["mixed"], 1), 3),
+        "unit": "ms/Newton iteration", "higher_is_better": False, "n_gpus": 1,
+        "config": {"workload": "C3: small-strain J2 (E 200e3, nu 0.3, yield 250, H 1000) plate 96x96x48 hex8, "
+                               "x=0 clamped, x=L gripped with u_x cycling to +-0.5%% strain, %d of 40 steps, "
+                               "Newton to 1e-8 (at most 12 iterations), Jacobi-PCG 1e-4, load-step cuts as "
+                               "TimeManagerT (max %d, quick_solve_iter %d)"
+                               % (nsteps, args.max_step_cuts, args.quick_solve_iter),
+                   "elements": int(mesh.nel), "nodes": int(mesh.nnd), "gauss_points": int(mesh.nel * 8)},
+        "load_steps": nsteps,
+        "total_ms": {k: round(v, 1) for k, v in tot.items()},
+        "ms_per_load_step": {k: round(v / nsteps, 1) for k, v in tot.items()},
+        "newton_iterations": its,
+        "pcg_iterations": {k: int(sum(v["pcg"])) for k, v in out.items()},
+        "ms_per_newton_iteration": {k: round(tot[k] / max(its[k], 1), 3) for k in out},
+        "step_cuts": {k: v["cuts"] for k, v in out.items()},
+        "newton_per_step": {k: v["newton"] for k, v in out.items()},
+        "flags_final": {k: v["flags_final"] for k, v in out.items()},
+        "active_set_mismatch_final": f["mismatch"][0],
+        "active_set_bit_exact": f["mismatch"][0] == 0,
+        "u_rel_err_mixed_vs_fp64_worst_step": float(max(
+            np.abs(a - b).max() / max(np.abs(b).max(), 1e-300) for a, b in zip(u_last["mixed"], u_last["fp64"]))),
+    }
+    print(json.dumps(line))
+
+
 def run_kernel_only(args):
     """Standalone launches of one hot kernel on the C2 state (for ncu): the
     step's prescribed values applied directly, residual, tangent, then
@@ -528,7 +597,11 @@ def main():
     ap.add_argument("--kernel", choices=sorted(KERNELS), help="time standalone launches of one kernel only")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--n", type=int, default=64, help="mesh size per side for --kernel")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--c3-steps", type=int, default=40, help="C3 load steps to run (of 40)")
+    ap.add_argument("--max-step-cuts", type=int, default=6, help="C3 load-step cuts allowed (TimeManagerT)")
+    ap.add_argument("--quick-solve-iter", type=int, default=0,
+                    help="C3 NLSolver quick_solve_iter (<= 1: a cut step is never doubled back)")
     ap.add_argument("--rves", type=int, default=4096)
     ap.add_argument("--rates", default="1000,5000,20000,50000", help="C5 arrival rates per second")
     ap.add_argument("--requests", type=int, default=2000, help="C5 requests per rate")
@@ -541,6 +614,8 @@ def main():
         run_c4(args)
     elif args.workload == "c5" and args.impl == "ours":
         run_c5(args)
+    elif args.workload == "c3" and args.impl == "ours":
+        run_c3(args)
     elif args.kernel:
         run_kernel_only(args)
     elif args.impl == "reference":

@@ -917,6 +917,120 @@ int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int 
   return 0;
 }
 
+namespace {
+/* One load step of NLSolver::Solve at time t from the current state; its =
+ * Newton iterations made.  0 converged, else failure (state not restored). */
+int newton_step(Model* M, double t, double rel_tol, double abs_tol, int max_its, double div_tol, int solver,
+                double lin_tol, int* its_out) {
+  const int n = M->neq;
+  std::vector<double> R(n), du(n), val(M->bindx.size());
+  const double sc = M->schedule(t);
+  for (const KBC& k : M->kbc) M->u[k.node * 3 + k.dof] = k.scheduled ? sc * k.value : 0.0;
+  int iteration = -1, its = 0;
+  *its_out = 0;
+  if (form(*M, M->u.data(), t, iteration, R.data(), nullptr)) return 1;
+  double err0 = 0;
+  for (double v : R) err0 += v * v;
+  err0 = std::sqrt(err0);
+  bool converged = err0 < abs_tol;
+  while (!converged) {
+    if (form(*M, M->u.data(), t, iteration, nullptr, val.data())) return 1;
+    std::fill(du.begin(), du.end(), 0.0);
+    int s = (solver == 0) ? dense_solve(*M, val.data(), R.data(), du.data())
+                          : (pcg(*M, val.data(), R.data(), du.data(), lin_tol, 100000, nullptr) < 0 ? -1 : 0);
+    if (s) return 1;
+    for (int i = 0; i < M->nnd * 3; ++i)
+      if (M->eqnos[i] > 0) M->u[i] += du[M->eqnos[i] - 1];
+    ++iteration;
+    *its_out = ++its;
+    if (form(*M, M->u.data(), t, iteration, R.data(), nullptr)) return 1;
+    double err = 0;
+    for (double v : R) err += v * v;
+    err = std::sqrt(err);
+    const double rel = err / err0;
+    if (!(rel <= div_tol)) return 1;
+    if (rel < rel_tol || err < abs_tol) converged = true;
+    else if (iteration >= max_its) return 1;
+  }
+  return 0;
+}
+}  // namespace
+
+/* The load-step sequence of TimeManagerT with step cuts around NLSolver
+ * (TimeManagerT::Step/DecreaseLoadStep/IncreaseLoadStep/DoDecreaseStep/
+ * DoIncreaseStep, TimeManagerT.cpp:55-150,350-375; NLSolver::DoConverged,
+ * NLSolver.cpp:517-539; FEManagerT::ResetStep restoring the last converged
+ * state, J2SSC0HardeningT::Reset).  A failed step is reset and retried at
+ * half the time step while fewer than max_cuts halvings are in force; after
+ * quick_count consecutive steps converged with fewer than quick_iter
+ * iterations (NLSolver's iteration counter, -1 based) the step is doubled
+ * back at an even step number.  u_hist / its_hist are written at the original
+ * step times k*dt (its: Newton iterations summed over the sub-steps);
+ * *cuts_out counts the cuts made.  Returns 0, or the 1-based original step
+ * that failed with no cut left. */
+int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its, double div_tol,
+                 int solver, double lin_tol, int max_cuts, int quick_iter, int quick_count, double* u_hist,
+                 int* its_hist, int* cuts_out) {
+  Model* M = static_cast<Model*>(m);
+  ensure_setup(*M);
+  enum { kSame, kDecrease, kIncrease };
+  int step_num = 0, num_steps = nsteps, cuts = 0, status = kSame, quick = 0, total_cuts = 0, its_acc = 0;
+  double tstep = dt, t = 0.0;
+  std::vector<double> u0;
+  if (cuts_out) *cuts_out = 0;
+  while (step_num < num_steps) {
+    if (status == kDecrease) {
+      ++cuts;
+      tstep /= 2;
+      num_steps *= 2;
+      step_num *= 2;
+    } else if (status == kIncrease) {
+      --cuts;
+      tstep *= 2;
+      num_steps /= 2;
+      step_num /= 2;
+    }
+    status = kSame;
+    ++step_num;
+    t += tstep;
+    u0 = M->u;
+    int its = 0;
+    const int s = newton_step(M, t, rel_tol, abs_tol, max_its, div_tol, solver, lin_tol, &its);
+    its_acc += its;
+    if (s) {
+      /* ResetStep: last converged displacements, J2 flags "reset" */
+      M->u = u0;
+      for (J2Card& c : M->j2)
+        if (c.allocated)
+          for (int ip = 0; ip < 8; ++ip) c.flags[ip] = ORC_J2_RESET;
+      t -= tstep;
+      --step_num;
+      if (cuts >= max_cuts) return (int)std::floor(t / dt + 1e-9) + 1;
+      status = kDecrease;
+      ++total_cuts;
+      if (cuts_out) *cuts_out = total_cuts;
+      continue;
+    }
+    for (J2Card& c : M->j2) j2_update(c);
+    /* NLSolver::DoConverged: fNumIteration is its - 1 here */
+    if (quick_iter > 1 && its - 1 < quick_iter) {
+      if (++quick >= quick_count && cuts > 0 && step_num % 2 == 0 && num_steps % 2 == 0 && step_num < num_steps) {
+        status = kIncrease;
+        quick = 0;
+      }
+    } else {
+      quick = 0;
+    }
+    const double k = std::round(t / dt);
+    if (std::fabs(t - k * dt) <= 1e-9 * dt && k >= 1) {
+      if (u_hist) std::memcpy(u_hist + (size_t)(k - 1) * M->nnd * 3, M->u.data(), sizeof(double) * M->nnd * 3);
+      if (its_hist) its_hist[(size_t)k - 1] = its_acc;
+      its_acc = 0;
+    }
+  }
+  return 0;
+}
+
 int orc_j2_state(void* m, signed char* flags, double* alpha, double* eps_p) {
   Model* M = static_cast<Model*>(m);
   ensure_setup(*M);

@@ -78,6 +78,14 @@ int orc_pcg(void* m, const double* val, const double* b, double* x, double rel_t
  * per step.  Returns 0 on success, step index+1 of the first failure otherwise. */
 int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its,
             double div_tol, int solver, double lin_tol, double* u_hist, int* its_hist);
+/* orc_run inside TimeManagerT's step sequence with load-step cuts (a failed
+ * step is reset and retried at half the step, at most max_cuts halvings in
+ * force; the step is doubled back after quick_count quick convergences of
+ * fewer than quick_iter iterations).  u_hist / its_hist at the original
+ * steps k*dt; *cuts_out = cuts made.  0, or the failing original step. */
+int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its, double div_tol,
+                 int solver, double lin_tol, int max_cuts, int quick_iter, int quick_count, double* u_hist,
+                 int* its_hist, int* cuts_out);
 
 /* J2 state after the last converged step (nel*8 each; alpha per IP). */
 int orc_j2_state(void* m, signed char* flags, double* alpha, double* eps_p);

@@ -44,6 +44,9 @@ def lib():
             ("orc_pcg", [_dp, _dp, _dp, ctypes.c_double, ctypes.c_int, _dp]),
             ("orc_run", [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                          ctypes.c_double, ctypes.c_int, ctypes.c_double, _dp, _ip]),
+            ("orc_run_cuts", [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                              ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int, _dp, _ip, _ip]),
             ("orc_j2_state", [ctypes.c_void_p, _dp, _dp]),
             ("orc_nodal_internal_force", [_dp, ctypes.c_int, _dp]),
             ("orc_get_u", [_dp]),
@@ -177,6 +180,18 @@ class OracleModel:
         s = lib().orc_run(self.h, nsteps, dt, rel_tol, abs_tol, max_its, div_tol, solver, lin_tol,
                           _d(uh), _i(its))
         return s, uh, its
+
+    def run_cuts(self, nsteps, dt, rel_tol=1e-12, abs_tol=1e-10, max_its=10, div_tol=10.0, solver=0,
+                 lin_tol=1e-12, max_cuts=0, quick_iter=6, quick_count=3):
+        """run() inside the reference's step sequence with load-step cuts;
+        returns (status, u at the original steps, iterations per original
+        step, cuts made)."""
+        uh = np.zeros((nsteps, self.nnd, 3))
+        its = np.zeros(nsteps, dtype=np.int32)
+        cuts = ctypes.c_int(0)
+        s = lib().orc_run_cuts(self.h, nsteps, dt, rel_tol, abs_tol, max_its, div_tol, solver, lin_tol, max_cuts,
+                               quick_iter, quick_count, _d(uh), _i(its), ctypes.byref(cuts))
+        return s, uh, its, cuts.value
 
     def j2_state(self):
         fl = np.zeros(self.nel * 8, dtype=np.int8)

@@ -140,19 +140,80 @@ class SolidModel:
         return 0
 
     def run(self, nsteps, dt, rel_tol=1e-12, abs_tol=1e-10, max_iterations=10, div_tol=10.0, precision=lib.FP64,
-            precond=lib.PRECOND_JACOBI, lin_rel_tol=1e-12, lin_max_it=20000, on_step=None, predictor=False):
+            precond=lib.PRECOND_JACOBI, lin_rel_tol=1e-12, lin_max_it=20000, on_step=None, predictor=False,
+            max_step_cuts=0, quick_solve_iter=6, quick_solve_count=3):
+        """The load-step sequence of TimeManagerT around NLSolver (device
+        Newton per step).  A step whose Newton iteration fails is reset to the
+        last converged state (FEManagerT::ResetStep: displacements from the
+        step-start snapshot, J2 flags reset) and retried at half the time step
+        while fewer than max_step_cuts halvings are in force
+        (TimeManagerT::DecreaseLoadStep / DoDecreaseStep,
+        TimeManagerT.cpp:119-136,350-362); after quick_solve_count consecutive
+        steps converged with NLSolver's iteration counter below
+        quick_solve_iter the step is doubled back at an even step number
+        (NLSolver::DoConverged, NLSolver.cpp:517-539; IncreaseLoadStep,
+        TimeManagerT.cpp:140-150).  Returns the displacements at the original
+        step times k*dt and, per original step, the Newton reports of its
+        converged sub-steps; self.step_cuts counts the cuts made.  Raises
+        TahoeError when a step fails with no cut left."""
         if self.ctx is None:
             self.setup()
         c = self.ctx
         hist, reports = [], []
-        for step in range(1, nsteps + 1):
-            self.apply_step(step * dt, (precision, precond, lin_rel_tol) if predictor else None)
-            rc, rep = c.newton(rel_tol, abs_tol, div_tol, max_iterations, precision, precond, lin_rel_tol, lin_max_it)
+        step_num, num_steps, cuts, status, quick = 0, nsteps, 0, "same", 0
+        tstep, t = float(dt), 0.0
+        self.step_cuts = 0
+        sub = []
+        while step_num < num_steps:
+            if status == "decrease":
+                cuts += 1
+                tstep /= 2
+                num_steps *= 2
+                step_num *= 2
+            elif status == "increase":
+                cuts -= 1
+                tstep *= 2
+                num_steps //= 2
+                step_num //= 2
+            status = "same"
+            step_num += 1
+            t += tstep
+            c.checkpoint()
+            self.apply_step(t, (precision, precond, lin_rel_tol) if predictor else None)
+            rc, rep = c.newton(rel_tol, abs_tol, div_tol, max_iterations, precision, precond, lin_rel_tol, lin_max_it,
+                               check=False)
+            if rc != lib.TG_OK:
+                # bad Jacobian, non-finite values, no convergence, divergence:
+                # NLSolver's kFailed, answered by a step cut; anything else
+                # (arguments, CUDA, memory) is raised at once
+                if rc not in (-4, -5, -6, -7):
+                    c._chk(rc, "tg_newton_solve")
+                c.rollback()
+                c.reset_step()
+                t -= tstep
+                step_num -= 1
+                if cuts >= max_step_cuts:
+                    c._chk(rc, "tg_newton_solve (no step cut left)")
+                status = "decrease"
+                self.step_cuts += 1
+                continue
             if on_step is not None:
-                on_step(step, c)
+                on_step(step_num, c)
             c.close_step()
-            hist.append(c.get_u())
-            reports.append(rep)
+            sub.append(rep)
+            if quick_solve_iter > 1 and rep.iterations - 1 < quick_solve_iter:
+                quick += 1
+                if quick >= quick_solve_count and cuts > 0 and step_num % 2 == 0 and num_steps % 2 == 0 \
+                        and step_num < num_steps:
+                    status = "increase"
+                    quick = 0
+            else:
+                quick = 0
+            k = round(t / dt)
+            if k >= 1 and abs(t - k * dt) <= 1e-9 * dt:
+                hist.append(c.get_u())
+                reports.append(sub[0] if len(sub) == 1 else sub)
+                sub = []
         return np.array(hist), reports
 
 

@@ -10,7 +10,8 @@ residual) must reach 1e-6 relative displacement error against FP64.
 import numpy as np
 import pytest
 
-from tahoe_gb300 import lib
+from oracle.pyoracle import OracleModel
+from tahoe_gb300 import lib, workloads
 from tahoe_gb300.meshgen import BoxMesh
 from tahoe_gb300.model import SolidModel, model_from_fixture
 from tests.helpers import (GOLDEN_NAMES, cube_case, golden_displacements, load_fixture, msr_to_upper_csr,
@@ -224,6 +225,31 @@ def test_j2_active_set_bit_exact_over_cyclic_steps():
     assert rel_err(ag, ao) < 1e-8
     assert rel_err(hist, uh_o) < 1e-8
     assert (fo == 0).sum() + (fo == 3).sum() > 0  # some points yielded
+
+
+def test_j2_plate_step_cuts_match_oracle():
+    """C3-style J2 plate (16 x 16 x 8) with a load step large enough that
+    Newton fails: both sides cut the step (TimeManagerT semantics) the same
+    number of times, the displacements at the original step ends agree, and
+    the active set is bit-exact; the mixed form takes the same cuts."""
+    mesh, o, _ = workloads.c3(nx=16, ny=16, nz=8, nsteps=40,
+                              add=lambda X, conn, form, mat: OracleModel(X, conn, form, [mat], threads=8))
+    st, uh_o, its_o, cuts_o = o.run_cuts(3, 2.0, 1e-8, 1e-10, 25, 1e3, 1, 1e-12, max_cuts=4)
+    assert st == 0 and cuts_o >= 1
+    fo, ao, eo = o.j2_state()
+    res = {}
+    for prec in (lib.FP64, lib.MIXED):
+        _, g, _ = workloads.c3(nx=16, ny=16, nz=8, nsteps=40)
+        hist, reps = g.run(3, 2.0, rel_tol=1e-8, abs_tol=1e-10, max_iterations=25, div_tol=1e3, precision=prec,
+                           lin_rel_tol=1e-12 if prec == lib.FP64 else 1e-6, lin_max_it=50000, max_step_cuts=4)
+        res[prec] = (hist, g.step_cuts, g.ctx.active_set())
+    hist, cuts, fg = res[lib.FP64]
+    assert cuts == cuts_o
+    assert np.array_equal(fg, fo)
+    assert rel_err(hist, uh_o) < 1e-7
+    hm, cm, fm = res[lib.MIXED]
+    assert cm == cuts_o and np.array_equal(fm, fg)
+    assert rel_err(hm, hist) < 1e-6
 
 
 def test_inverted_element_reports_bad_jacobian():
