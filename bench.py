@@ -529,10 +529,15 @@ def run_c3(args):
             rec["pcg"].append(sum(x.pcg_iterations for x in rs))
         fl = c.active_set()
         rec["flags_final"] = {str(k): int((fl == k).sum()) for k in (0, 1, 3, 7)}
+        # yielding set: points that yielded in the last step (kReset after
+        # CloseStep) or are plastic; allocation: elements that ever voted to
+        # allocate (also in intermediate Newton iterations)
+        yielding, alloc = (fl == 0) | (fl == 3), fl != lib.J2_UNALLOCATED
         if name == "mixed":
-            flags_ref["final"] = fl
+            flags_ref["final"] = (yielding, alloc)
         else:
-            rec["mismatch"].append(int((fl != flags_ref["final"]).sum()))
+            rec["mismatch"].append(int((yielding != flags_ref["final"][0]).sum()))
+            rec["alloc_mismatch"] = int((alloc != flags_ref["final"][1]).sum())
         u_last[name] = hist
         out[name] = rec
         c.close()
@@ -557,8 +562,9 @@ def run_c3(args):
         "step_cuts": {k: v["cuts"] for k, v in out.items()},
         "newton_per_step": {k: v["newton"] for k, v in out.items()},
         "flags_final": {k: v["flags_final"] for k, v in out.items()},
-        "active_set_mismatch_final": f["mismatch"][0],
+        "yielding_set_mismatch_final": f["mismatch"][0],
         "active_set_bit_exact": f["mismatch"][0] == 0,
+        "allocated_points_mismatch_final": f["alloc_mismatch"],
         "u_rel_err_mixed_vs_fp64_worst_step": float(max(
             np.abs(a - b).max() / max(np.abs(b).max(), 1e-300) for a, b in zip(u_last["mixed"], u_last["fp64"]))),
     }
