@@ -195,7 +195,8 @@ def run_ours(args):
         from tahoe_gb300 import autotune
         t = autotune.Tuner(reps=20)
         tuning = t.tune(ctx, prec, lib.TOTAL_LAGRANGIAN)
-        tuning = {k: tuning[k] for k in ("tile_blocks", "stages", "tangent_epb", "spmv_ms", "tangent_ms", "cached")}
+        tuning = {k: tuning.get(k) for k in ("tile_blocks", "stages", "release", "tangent_epb", "spmv_ms", "tangent_ms",
+                                             "cached", "spmv_sweep")}
 
     # warm-up (also captures the PCG graph)
     its_seen = []

@@ -284,6 +284,10 @@ int tg_predict_affine(tg_context* ctx, const double* F, const tg_newton_params* 
  * through a ring of `stages` (2 or 3) shared-memory buffers.  Defaults
  * 640 / 2.  Changing the tile size drops the assembled tangent. */
 int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
+/* stage release of the streamed product: 0 (default) every CTA waits at a
+ * barrier after each staged tile; 1 each warp releases the stage on an
+ * mbarrier and moves on (results are bitwise the same) */
+int tg_spmv_release(tg_context* ctx, int per_warp);
 /* elements per CTA of the tangent kernel: 2, 4 or 8 (default 8); element
  * matrices are bitwise the same for every choice */
 int tg_tangent_config(tg_context* ctx, int elems_per_block);

@@ -4,7 +4,8 @@ Two shapes are tuned on the mesh a context holds, by timing the kernels
 themselves (CUDA events, tg_time_kernel) on the current state:
 
   * the streamed PCG product: rows per tile (the unit of the tile-contiguous
-    matrix storage, in block nonzeros) x depth of the shared-memory ring;
+    matrix storage, in block nonzeros) x depth of the shared-memory ring x
+    stage release (CTA barrier per tile, or per-warp release on an mbarrier);
   * the element tangent: elements per CTA (one thread per upper node-pair
     block of each element).
 
@@ -22,6 +23,7 @@ from . import lib
 
 SPMV_TILES = (256, 384, 512, 640, 768, 1024, 1536)
 SPMV_STAGES = (2, 3)
+SPMV_RELEASE = (0, 1)
 TANGENT_EPB = (2, 4, 8)
 KERNEL_SPMV, KERNEL_TANGENT = 0, 2
 
@@ -45,10 +47,11 @@ def pick(timings):
 
 
 class Tuner:
-    def __init__(self, cache_path=_DEFAULT_CACHE, reps=20, tiles=SPMV_TILES, stages=SPMV_STAGES, epbs=TANGENT_EPB):
+    def __init__(self, cache_path=_DEFAULT_CACHE, reps=20, tiles=SPMV_TILES, stages=SPMV_STAGES, epbs=TANGENT_EPB,
+                 releases=SPMV_RELEASE):
         self.cache_path = cache_path
         self.reps = reps
-        self.tiles, self.stages, self.epbs = tiles, stages, epbs
+        self.tiles, self.stages, self.epbs, self.releases = tiles, stages, epbs, releases
         self.table = {}
         if cache_path and os.path.exists(cache_path):
             try:
@@ -69,6 +72,7 @@ class Tuner:
     @staticmethod
     def apply(ctx, cfg):
         ctx.spmv_config(cfg["tile_blocks"], cfg["stages"])
+        ctx.spmv_release(cfg.get("release", 0))
         ctx.tangent_config(cfg["tangent_epb"])
 
     def tune(self, ctx, precision, formulation, gpu="gpu0", force=False, timer=None):
@@ -88,23 +92,29 @@ class Tuner:
                 try:
                     ctx.spmv_config(t, s)
                     ctx.tangent(precision)  # assemble into the new tile layout
-                    spmv[(t, s)] = timer(ctx, KERNEL_SPMV, self.reps)
                 except lib.TahoeError:
-                    spmv[(t, s)] = None  # ring does not fit on an SM
-        (tb, st), spmv_ms = pick(spmv)
+                    for r in self.releases:
+                        spmv[(t, s, r)] = None  # ring does not fit on an SM
+                    continue
+                for r in self.releases:
+                    ctx.spmv_release(r)
+                    spmv[(t, s, r)] = timer(ctx, KERNEL_SPMV, self.reps)
+        (tb, st, rl), spmv_ms = pick(spmv)
         ctx.spmv_config(tb, st)
+        ctx.spmv_release(rl)
         ctx.tangent(precision)
         tang = {}
         for e in self.epbs:
             ctx.tangent_config(e)
             tang[e] = timer(ctx, KERNEL_TANGENT, max(3, self.reps // 4))
         epb, tang_ms = pick(tang)
-        cfg = {"tile_blocks": tb, "stages": st, "tangent_epb": epb, "spmv_ms": spmv_ms, "tangent_ms": tang_ms}
+        cfg = {"tile_blocks": tb, "stages": st, "release": rl, "tangent_epb": epb, "spmv_ms": spmv_ms,
+               "tangent_ms": tang_ms}
         self.apply(ctx, cfg)
         ctx.tangent(precision)
         self.table[key] = cfg
         self.save()
         out = dict(cfg, cached=False)
-        out["spmv_sweep"] = {"%dx%d" % k: v for k, v in spmv.items()}
+        out["spmv_sweep"] = {"%dx%dr%d" % k: v for k, v in spmv.items()}
         out["tangent_sweep"] = {str(k): v for k, v in tang.items()}
         return out

@@ -392,6 +392,16 @@ int tg_spmv_config(tg_context* c, int tile_blocks, int stages) {
   return build_tiles(c, tile_blocks);
 }
 
+int tg_spmv_release(tg_context* c, int per_warp) {
+  if (!c || (per_warp != 0 && per_warp != 1)) return TG_ERR_ARG;
+  c->spmv_warp_release = per_warp;
+  // the captured PCG chunk bakes in the kernel
+  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
+  c->pcg_graph = nullptr;
+  c->pcg_graph_key = -1;
+  return TG_OK;
+}
+
 int tg_tangent_config(tg_context* c, int elems_per_block) {
   if (!c || (elems_per_block != 2 && elems_per_block != 4 && elems_per_block != 8)) return TG_ERR_ARG;
   c->tangent_epb = elems_per_block;

@@ -107,6 +107,87 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
 }
 
 
+// The rows of one staged tile handled by this warp: 8 lanes per row, 4 rows
+// per warp at a time, each lane over every 8th block; q = A p_new and p_new
+// written for the rows, p_new.q accumulated into v.
+template <typename T>
+__device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps, T beta,
+                                               const typename Vec4<T>::type* __restrict__ z,
+                                               const typename Vec4<T>::type* __restrict__ pold,
+                                               typename Vec4<T>::type* __restrict__ pnew,
+                                               typename Vec4<T>::type* __restrict__ q, Acc<T>& v0) {
+  using V = typename Vec4<T>::type;
+  const int sub = lane & 7;
+  Acc<T>* v = &v0;
+  const int* hdr = reinterpret_cast<const int*>(base);
+  const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
+  const int* rp = hdr + 4;
+  const int* cl = rp + ceil4(nrows + 1);
+  const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
+  for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
+    const bool live = li < nrows;
+    const int I = r0 + li;
+    V zi, pi;
+    if (live && sub == 0) {
+      zi = z[I];
+      pi = pold[I];
+    }
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    const int e0 = live ? rp[li] : 0;
+    const int e1 = live ? rp[li + 1] : 0;
+    // the first 4 blocks of this lane (a hex8 row has at most 27): all
+    // column indices, then all neighbour gathers, then the arithmetic, so
+    // the L2 round trips of one lane overlap instead of chaining
+    {
+      int Jk[4];
+      V zk[4], pk[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = e0 + sub + 8 * u;
+        Jk[u] = j < e1 ? cl[j] : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (Jk[u] >= 0) {
+          zk[u] = z[Jk[u]];
+          pk[u] = pold[Jk[u]];
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (Jk[u] >= 0) {
+          const T* vv = pl + e0 + sub + 8 * u;
+          const T x = zk[u].x + beta * pk[u].x, y = zk[u].y + beta * pk[u].y, w = zk[u].z + beta * pk[u].z;
+          a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
+          a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
+          a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
+        }
+    }
+    for (int j = e0 + sub + 32; j < e1; j += 8) {
+      const int J = cl[j];
+      const T* vv = pl + j;
+      const V zj = z[J], pj = pold[J];
+      const T x = zj.x + beta * pj.x, y = zj.y + beta * pj.y, w = zj.z + beta * pj.z;
+      a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
+      a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
+      a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (live && sub == 0) {
+      const V pn = mk<V, T>(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z);
+      q[I] = mk<V, T>(a0, a1, a2);
+      pnew[I] = pn;
+      v[0].add_prod(pn.x, a0);
+      v[0].add_prod(pn.y, a1);
+      v[0].add_prod(pn.z, a2);
+    }
+  }
+}
+
 // q = A p_new with p_new = z + beta p_old formed at every gathered node, on a
 // persistent grid.  Each CTA streams its row tiles through a ring of NST
 // shared-memory stages: one bulk copy per tile (the tile-contiguous storage
@@ -169,74 +250,7 @@ __global__ void __launch_bounds__(256) pcg_spmv_kernel(int ntiles, const long lo
       stuck = s;
       break;
     }
-    const unsigned char* base = smem + (size_t)s * cap;
-    const int* hdr = reinterpret_cast<const int*>(base);
-    const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
-    const int* rp = hdr + 4;
-    const int* cl = rp + ceil4(nrows + 1);
-    const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
-    for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
-      const bool live = li < nrows;
-      const int I = r0 + li;
-      V zi, pi;
-      if (live && sub == 0) {
-        zi = z[I];
-        pi = pold[I];
-      }
-      T a0 = T(0), a1 = T(0), a2 = T(0);
-      const int e0 = live ? rp[li] : 0;
-      const int e1 = live ? rp[li + 1] : 0;
-      // the first 4 blocks of this lane (a hex8 row has at most 27): all
-      // column indices, then all neighbour gathers, then the arithmetic, so
-      // the L2 round trips of one lane overlap instead of chaining
-      {
-        int Jk[4];
-        V zk[4], pk[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int j = e0 + sub + 8 * u;
-          Jk[u] = j < e1 ? cl[j] : -1;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (Jk[u] >= 0) {
-            zk[u] = z[Jk[u]];
-            pk[u] = pold[Jk[u]];
-          }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (Jk[u] >= 0) {
-            const T* vv = pl + e0 + sub + 8 * u;
-            const T x = zk[u].x + beta * pk[u].x, y = zk[u].y + beta * pk[u].y, w = zk[u].z + beta * pk[u].z;
-            a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
-            a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
-            a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
-          }
-      }
-      for (int j = e0 + sub + 32; j < e1; j += 8) {
-        const int J = cl[j];
-        const T* vv = pl + j;
-        const V zj = z[J], pj = pold[J];
-        const T x = zj.x + beta * pj.x, y = zj.y + beta * pj.y, w = zj.z + beta * pj.z;
-        a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
-        a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
-        a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
-      }
-#pragma unroll
-      for (int o = 4; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-      }
-      if (live && sub == 0) {
-        const V pn = mk<V, T>(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z);
-        q[I] = mk<V, T>(a0, a1, a2);
-        pnew[I] = pn;
-        v[0].add_prod(pn.x, a0);
-        v[0].add_prod(pn.y, a1);
-        v[0].add_prod(pn.z, a2);
-      }
-    }
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, beta, z, pold, pnew, q, v[0]);
     __syncthreads();  // stage s is free for the copy issued next iteration
   }
   if (stuck >= 0 && threadIdx.x == 0) {
@@ -247,6 +261,113 @@ __global__ void __launch_bounds__(256) pcg_spmv_kernel(int ntiles, const long lo
       const unsigned parity = ((phases >> k) & 1u) ^ (k == stuck ? 1u : 0u);
       mbar_wait(&bars[k], parity, kWaitLimit);  // bounded even when nothing is pending
     }
+    sc->done = 2;
+    sc->fail = 5;
+  }
+  double tot[1];
+  if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
+    sc->pq = tot[0];
+    if (sc->done == 2) return;
+    if (!(tot[0] > 0.0) || !isfinite(tot[0])) {
+      sc->done = 2;
+      sc->fail = isfinite(tot[0]) ? 2 : 3;
+    } else {
+      sc->alpha = sc->rz / tot[0];
+    }
+  }
+}
+
+// The same product with per-warp stage release: instead of a CTA barrier at
+// the end of every tile, each warp arrives on the stage's "empty" mbarrier
+// when its rows are done, and the producing thread waits on it (bounded)
+// before the next bulk copy into that stage, so a warp that finishes a tile
+// early moves on to the next staged tile.  Consumer reads are ordered before
+// the next copy by the mbarrier release/acquire and a proxy fence.
+template <typename T, int NST>
+__global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long long* __restrict__ blob_off,
+                                                          const unsigned char* __restrict__ blob, int cap,
+                                                          const typename Vec4<T>::type* __restrict__ z,
+                                                          const typename Vec4<T>::type* __restrict__ pold,
+                                                          typename Vec4<T>::type* __restrict__ pnew,
+                                                          typename Vec4<T>::type* __restrict__ q, double* partials,
+                                                          PcgScalars* sc, int* status) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[NST];
+  __shared__ __align__(8) uint64_t empty[NST];
+  __shared__ volatile int abort_flag;
+  if (((volatile PcgScalars*)sc)->done) return;
+  const T beta = T(sc->beta);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NST; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], nwarps);
+    }
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  Acc<T> v[1];
+  const int t0 = blockIdx.x, G = gridDim.x;
+  // producer bookkeeping (thread 0): copies issued / completions seen per
+  // stage, and the parity of the next "empty" completion per stage
+  int issued[NST], seen[NST];
+#pragma unroll
+  for (int k = 0; k < NST; ++k) issued[k] = seen[k] = 0;
+  unsigned eph = 0u;
+  auto issue = [&](int t, int stage) {
+    const long long o0 = blob_off[t], o1 = blob_off[t + 1];
+    const unsigned bytes = (unsigned)(o1 - o0);
+    mbar_expect_tx(&full[stage], bytes);
+    bulk_copy(smem + (size_t)stage * cap, blob + o0, bytes, &full[stage]);
+  };
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NST - 1; ++k)
+      if (t0 + k * G < ntiles) {
+        issue(t0 + k * G, k);
+        ++issued[k];
+      }
+  unsigned phases = 0u;  // parity of each stage's next "full" completion
+  int it = 0;
+  for (int t = t0; t < ntiles; ++it, t += G) {
+    if (abort_flag) break;
+    const int s = it % NST;
+    const int tn = t + (NST - 1) * G;
+    if (threadIdx.x == 0 && tn < ntiles) {
+      const int sn = (it + NST - 1) % NST;
+      bool free_ok = true;
+      if (it >= 1) {  // stage sn held the tile of iteration it-1
+        free_ok = mbar_wait(&empty[sn], (eph >> sn) & 1u, kWaitLimit);
+        eph ^= 1u << sn;
+      }
+      if (free_ok) {
+        fence_async_smem();
+        issue(tn, sn);
+        ++issued[sn];
+      } else {
+        abort_flag = 1;
+      }
+    }
+    const bool got = mbar_wait(&full[s], (phases >> s) & 1u, kWaitLimit);
+    phases ^= 1u << s;
+    if (!got) {
+      abort_flag = 1;
+      break;
+    }
+    if (threadIdx.x == 0) ++seen[s];
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, beta, z, pold, pnew, q, v[0]);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0) {
+    // a wait timed out: record it, drain the copies still in flight
+    // (bounded) and leave the solve flagged as broken down
+    atomicOr(status, kStatusWaitTimeout);
+    for (int k = 0; k < NST; ++k)
+      if (issued[k] > seen[k]) mbar_wait(&full[k], (unsigned)(seen[k] & 1), kWaitLimit);
     sc->done = 2;
     sc->fail = 5;
   }
@@ -316,6 +437,7 @@ struct Grids {
   int spmv, vec;
   size_t spmv_smem;
   int stages;
+  int warp_release = 0;
 };
 
 // persistent grid for the streamed SpMV: as many CTAs as fit (shared memory
@@ -334,18 +456,23 @@ int spmv_config_n(Context* c, Grids& g) {
     c->err = "SpMV tile ring does not fit in shared memory (reduce tile_blocks or stages)";
     return TG_ERR_CAPACITY;
   }
+  auto kern = c->spmv_warp_release ? pcg_spmv_wr_kernel<T, NST> : pcg_spmv_kernel<T, NST>;
+  // both variants get the attribute (the scratch-vector solve always uses
+  // the CTA-barrier kernel)
   if (!ok(c, cudaFuncSetAttribute(pcg_spmv_kernel<T, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)g.spmv_smem), "smem attribute") ||
+      !ok(c, cudaFuncSetAttribute(pcg_spmv_wr_kernel<T, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)g.spmv_smem), "smem attribute"))
     return TG_ERR_CUDA;
   int per_sm = 0;
-  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_spmv_kernel<T, NST>, 256, g.spmv_smem),
-          "occupancy"))
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, g.spmv_smem), "occupancy"))
     return TG_ERR_CUDA;
   if (per_sm < 1) {
     c->err = "SpMV tile does not fit in shared memory";
     return TG_ERR_CAPACITY;
   }
   g.spmv = std::max(1, std::min(c->ntiles, kNumSMs * per_sm));
+  g.warp_release = c->spmv_warp_release;
   return TG_OK;
 }
 template <typename T>
@@ -365,14 +492,21 @@ void launch_spmv(Context* c, const Grids& g, const void* z, const void* pold, vo
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);
-  if (g.stages == 3)
-    pcg_spmv_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, (const V*)z,
-                                                                   (const V*)pold, (V*)pnew, (V*)c->d_q,
-                                                                   c->d_partials, c->d_pcg, c->d_status);
-  else
-    pcg_spmv_kernel<T, 2><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, (const V*)z,
-                                                                   (const V*)pold, (V*)pnew, (V*)c->d_q,
-                                                                   c->d_partials, c->d_pcg, c->d_status);
+#define TG_SPMV_ARGS                                                                                         \
+  c->ntiles, off, blob, cap, (const V*)z, (const V*)pold, (V*)pnew, (V*)c->d_q, c->d_partials, c->d_pcg, \
+      c->d_status
+  if (g.warp_release) {
+    if (g.stages == 3)
+      pcg_spmv_wr_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
+    else
+      pcg_spmv_wr_kernel<T, 2><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
+  } else {
+    if (g.stages == 3)
+      pcg_spmv_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
+    else
+      pcg_spmv_kernel<T, 2><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
+  }
+#undef TG_SPMV_ARGS
 }
 Grids grids(const Context* c) {
   Grids g;

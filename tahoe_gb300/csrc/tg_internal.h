@@ -99,6 +99,7 @@ struct Context {
   int* d_tile_row = nullptr;
   int spmv_tile_blocks = kTileBlocks;
   int spmv_stages = 2;
+  int spmv_warp_release = 0;   // 1: per-warp stage release instead of a CTA barrier per tile
   int tangent_epb = 8;         // elements per CTA of the tangent kernel (2, 4, 8)
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b

@@ -80,6 +80,7 @@ _SIGS = {
     "tg_time_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     "tg_spmv_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "tg_tangent_config": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tg_spmv_release": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
     "tg_segment_residual_norms": (ctypes.c_int, [_vp, _dp]),
@@ -414,6 +415,9 @@ class Context:
 
     def spmv_config(self, tile_blocks, stages):
         self._chk(self.L.tg_spmv_config(self.h, int(tile_blocks), int(stages)), "tg_spmv_config")
+
+    def spmv_release(self, per_warp):
+        self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")
 
     def tangent_config(self, elems_per_block):
         self._chk(self.L.tg_tangent_config(self.h, int(elems_per_block)), "tg_tangent_config")

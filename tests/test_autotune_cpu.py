@@ -9,7 +9,7 @@ from tahoe_gb300 import autotune, lib
 class FakeCtx:
     def __init__(self, nnd=5000, nel=4000):
         self.nnd, self.nel = nnd, nel
-        self.cfg = {"tile_blocks": 640, "stages": 2, "tangent_epb": 8}
+        self.cfg = {"tile_blocks": 640, "stages": 2, "tangent_epb": 8, "release": 0}
         self.tangents = 0
 
     def spmv_config(self, t, s):
@@ -17,6 +17,9 @@ class FakeCtx:
             raise lib.TahoeError(-8, "tg_spmv_config", "does not fit")
         self.cfg["tile_blocks"], self.cfg["stages"] = t, s
         self.formed = False  # a new tile layout drops the assembled tangent
+
+    def spmv_release(self, r):
+        self.cfg["release"] = r
 
     def tangent_config(self, e):
         self.cfg["tangent_epb"] = e
@@ -30,7 +33,7 @@ def fake_timer(ctx, which, reps):
     assert getattr(ctx, "formed", False), "kernel timed without a formed tangent"
     c = ctx.cfg
     if which == autotune.KERNEL_SPMV:
-        return abs(c["tile_blocks"] - 768) / 100.0 + (0.5 if c["stages"] == 3 else 0.0) + 1.0
+        return abs(c["tile_blocks"] - 768) / 100.0 + (0.5 if c["stages"] == 3 else 0.0) + 1.0 - 0.1 * c["release"]
     return {2: 3.0, 4: 1.5, 8: 2.0}[c["tangent_epb"]]
 
 
@@ -40,10 +43,10 @@ def test_picks_fastest_and_caches(tmp_path):
     ctx = FakeCtx()
     out = t.tune(ctx, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=fake_timer)
     assert not out["cached"]
-    assert (out["tile_blocks"], out["stages"], out["tangent_epb"]) == (768, 2, 4)
-    assert ctx.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4}
+    assert (out["tile_blocks"], out["stages"], out["release"], out["tangent_epb"]) == (768, 2, 1, 4)
+    assert ctx.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1}
     # 1024x3 and 1536x2/3 do not fit and are skipped, not chosen
-    assert out["spmv_sweep"]["1536x2"] is None and out["spmv_sweep"]["1024x3"] is None
+    assert out["spmv_sweep"]["1536x2r0"] is None and out["spmv_sweep"]["1024x3r1"] is None
     with open(path) as f:
         table = json.load(f)
     assert len(table) == 1
@@ -51,7 +54,7 @@ def test_picks_fastest_and_caches(tmp_path):
     ctx2 = FakeCtx(nnd=5100, nel=4050)  # same size class
     t2 = autotune.Tuner(cache_path=path)
     out2 = t2.tune(ctx2, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=lambda *a: 1 / 0)
-    assert out2["cached"] and ctx2.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4}
+    assert out2["cached"] and ctx2.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1}
     # another size class or precision is tuned separately
     assert autotune.signature(FakeCtx(nnd=50000), lib.MIXED, 1) != autotune.signature(ctx, lib.MIXED, 1)
     assert autotune.signature(ctx, lib.FP64, 1) != autotune.signature(ctx, lib.MIXED, 1)

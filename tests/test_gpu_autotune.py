@@ -51,6 +51,13 @@ def test_tuned_shapes_applied_and_solution_unchanged(tmp_path):
     out = t.tune(c, lib.MIXED, lib.TOTAL_LAGRANGIAN)
     assert not out["cached"]
     assert c.tuning() == {k: out[k] for k in ("tile_blocks", "stages", "tangent_epb")}
+    # the two stage-release variants of the product give bitwise the same solve
+    sols = []
+    for r in (0, 1):
+        c.spmv_release(r)
+        c.tangent(lib.MIXED)
+        sols.append(c.pcg(R, rel_tol=1e-7)[:2])
+    assert np.array_equal(sols[0][0], sols[1][0]) and sols[0][1] == sols[1][1]
     c.tangent(lib.MIXED)
     du1 = c.pcg(R, rel_tol=1e-7)[0]
     assert rel_err(du1, du0) < 1e-5
