@@ -38,6 +38,7 @@ enum tg_status {
 };
 
 enum tg_formulation { TG_SMALL_STRAIN = 0, TG_TOTAL_LAGRANGIAN = 1 };
+enum tg_strain_displacement { TG_STRAIN_STANDARD = 0, TG_STRAIN_BBAR = 1 };
 
 enum tg_material_kind {
   TG_MAT_SS_HOOKEAN = 0,  /* small_strain_StVenant / small_strain_Hookean: {E,nu} or C[36] row-major */
@@ -81,6 +82,11 @@ int tg_mesh_upload(tg_context* ctx, int nnd, const double* coords_soa, int nel, 
                    const int* eqnos);
 /* small_strain / total_lagrangian (ElementListT.cpp:738,752) */
 int tg_element_set(tg_context* ctx, int formulation);
+/* strain_displacement option of small_strain (SmallStrainT.cpp:46-91,
+ * 327-421): TG_STRAIN_STANDARD, or TG_STRAIN_BBAR for the mean-dilatation
+ * B-bar of SolidElementT::Set_B_bar (SolidElementT.cpp:956-1044); ignored by
+ * total_lagrangian */
+int tg_element_strain_displacement(tg_context* ctx, int option);
 /* material of element block `block` (SSSolidMatList3DT.cpp:199-207,
  * FSSolidMatList3DT.cpp:409-415) */
 int tg_material_set(tg_context* ctx, int block, int kind, const double* params, int nparams);

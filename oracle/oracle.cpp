@@ -302,6 +302,7 @@ struct Model {
   std::vector<int> conn;  /* nel*8 */
   std::vector<int> block; /* nel */
   int form = ORC_SMALL_STRAIN;
+  bool bbar = false; /* small strain with B-bar (SmallStrainT kMeanDilBbar) */
   std::vector<Material> mats;
   std::vector<double> sx, sy; /* schedule */
   std::vector<KBC> kbc;
@@ -395,9 +396,10 @@ double ip_gradients(const double* Xe, int ip, double dNdx[3][8]) {
 }
 
 /* B^T D B accumulation with B from SolidElementT::Set_B (SolidElementT.cpp:889-918) */
-void add_btdb(const double g[3][8], const double D[36], double scale, double* Ke) {
-  double B[6][24];
-  std::memset(B, 0, sizeof(B));
+/* strain-displacement matrix, Voigt rows [11,22,33,23,13,12] with
+ * engineering shear (SolidElementT::Set_B, SolidElementT.cpp:854-920) */
+void set_b(const double g[3][8], double B[6][24]) {
+  std::memset(B, 0, sizeof(double) * 6 * 24);
   for (int a = 0; a < 8; ++a) {
     B[0][3 * a] = g[0][a];
     B[4][3 * a] = g[2][a];
@@ -409,6 +411,22 @@ void add_btdb(const double g[3][8], const double D[36], double scale, double* Ke
     B[3][3 * a + 2] = g[1][a];
     B[4][3 * a + 2] = g[0][a];
   }
+}
+
+/* B-bar of Hughes (4.5.11-16) (SolidElementT::Set_B_bar,
+ * SolidElementT.cpp:956-1044): the normal rows of node a's columns take
+ * (mean_a - grad_a)/3 added, the element-mean dilatation replacing the
+ * point dilatation. */
+void set_b_bar(const double g[3][8], const double mean[3][8], double B[6][24]) {
+  set_b(g, B);
+  for (int a = 0; a < 8; ++a)
+    for (int d = 0; d < 3; ++d) {
+      const double f = (mean[d][a] - g[d][a]) / 3.0;
+      for (int r = 0; r < 3; ++r) B[r][3 * a + d] += f;
+    }
+}
+
+void add_btdb_b(const double B[6][24], const double D[36], double scale, double* Ke) {
   double DB[6][24];
   for (int i = 0; i < 6; ++i)
     for (int q = 0; q < 24; ++q) {
@@ -422,6 +440,12 @@ void add_btdb(const double g[3][8], const double D[36], double scale, double* Ke
       for (int k = 0; k < 6; ++k) a += B[k][p] * DB[k][q];
       Ke[p * 24 + q] += scale * a;
     }
+}
+
+void add_btdb(const double g[3][8], const double D[36], double scale, double* Ke) {
+  double B[6][24];
+  set_b(g, B);
+  add_btdb_b(B, D, scale, Ke);
 }
 
 /* Element Ke and internal force.  Small strain: SmallStrainT::FormKd/FormStiffness
@@ -448,6 +472,24 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
     if (update_state) card = &M.j2[e];
     else { scratch = M.j2[e]; card = &scratch; }
   }
+  /* B-bar: mean shape-function gradients over the element
+   * (SmallStrainT::SetMeanGradient, SmallStrainT.cpp:404-421) */
+  const bool bbar = M.bbar && M.form == ORC_SMALL_STRAIN;
+  double mean[3][8] = {{0}};
+  if (bbar) {
+    double vol = 0.0;
+    for (int ip = 0; ip < 8; ++ip) {
+      double g[3][8];
+      const double detj = ip_gradients(Xe, ip, g);
+      if (!(detj > 0.0)) return -1;
+      const double wdet = S.w[ip] * detj;
+      vol += wdet;
+      for (int d = 0; d < 3; ++d)
+        for (int a = 0; a < 8; ++a) mean[d][a] += wdet * g[d][a];
+    }
+    for (int d = 0; d < 3; ++d)
+      for (int a = 0; a < 8; ++a) mean[d][a] /= vol;
+  }
   for (int ip = 0; ip < 8; ++ip) {
     double g[3][8];
     double detj = ip_gradients(Xe, ip, g);
@@ -455,15 +497,16 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
     double wdet = S.w[ip] * detj;
     double s[6], D[36];
     if (M.form == ORC_SMALL_STRAIN) {
-      /* strain = sym(grad u), tensor components */
-      double H[9] = {0};
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-          double a = 0;
-          for (int n = 0; n < 8; ++n) a += ue[n * 3 + i] * g[j][n];
-          H[i * 3 + j] = a;
-        }
-      double eps[6] = {H[0], H[4], H[8], 0.5 * (H[5] + H[7]), 0.5 * (H[2] + H[6]), 0.5 * (H[1] + H[3])};
+      double B[6][24];
+      if (bbar) set_b_bar(g, mean, B);
+      else set_b(g, B);
+      /* strain = B u, shear halved to tensor components */
+      double eps[6];
+      for (int r = 0; r < 6; ++r) {
+        double a = 0;
+        for (int q = 0; q < 24; ++q) a += B[r][q] * ue[q];
+        eps[r] = r < 3 ? a : 0.5 * a;
+      }
       if (m.kind == ORC_MAT_SS_J2) {
         /* the tangent reads the state left by the last residual evaluation
          * (FormStiffness calls only c_ijkl) */
@@ -474,12 +517,13 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
         std::memcpy(D, m.C, sizeof(D));
       }
       if (wantK) {
-        add_btdb(g, D, wdet, out.Ke);
+        add_btdb_b(B, D, wdet, out.Ke);
       } else {
-        for (int a = 0; a < 8; ++a) {
-          out.fint[a * 3 + 0] += wdet * (g[0][a] * s[0] + g[2][a] * s[4] + g[1][a] * s[5]);
-          out.fint[a * 3 + 1] += wdet * (g[1][a] * s[1] + g[2][a] * s[3] + g[0][a] * s[5]);
-          out.fint[a * 3 + 2] += wdet * (g[2][a] * s[2] + g[1][a] * s[3] + g[0][a] * s[4]);
+        /* fint = B^T sigma (SmallStrainT::FormKd) */
+        for (int q = 0; q < 24; ++q) {
+          double a = 0;
+          for (int r = 0; r < 6; ++r) a += B[r][q] * s[r];
+          out.fint[q] += wdet * a;
         }
       }
     } else {
@@ -751,6 +795,10 @@ void* orc_model_create(int nnd, const double* X, int nel, const int* conn) {
 void orc_model_free(void* m) { delete static_cast<Model*>(m); }
 int orc_set_formulation(void* m, int form) {
   static_cast<Model*>(m)->form = form;
+  return 0;
+}
+int orc_set_bbar(void* m, int on) {
+  static_cast<Model*>(m)->bbar = on != 0;
   return 0;
 }
 /* parameters:

@@ -43,6 +43,9 @@ enum { ORC_J2_PLASTIC = 0, ORC_J2_ELASTIC = 1, ORC_J2_RESET = 3, ORC_J2_UNALLOCA
 void* orc_model_create(int nnd, const double* X, int nel, const int* conn);
 void orc_model_free(void* m);
 int orc_set_formulation(void* m, int form);
+/* small strain only: 1 = B-bar strain-displacement (SmallStrainT
+ * strain_displacement="B-bar", mean dilatation, SmallStrainT.cpp:337-421) */
+int orc_set_bbar(void* m, int on);
 int orc_set_material(void* m, int block, int kind, const double* p, int np);
 int orc_set_element_blocks(void* m, const int* block_of_element);
 int orc_set_schedule(void* m, int npts, const double* x, const double* y);

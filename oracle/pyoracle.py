@@ -30,6 +30,7 @@ def lib():
         L.orc_model_free.argtypes = [ctypes.c_void_p]
         for name, args in [
             ("orc_set_formulation", [ctypes.c_int]),
+            ("orc_set_bbar", [ctypes.c_int]),
             ("orc_set_material", [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]),
             ("orc_set_element_blocks", [_ip]),
             ("orc_set_schedule", [ctypes.c_int, _dp, _dp]),
@@ -88,13 +89,14 @@ def material_params(mat):
 
 
 class OracleModel:
-    def __init__(self, X, conn, formulation, materials, blocks=None, threads=1):
+    def __init__(self, X, conn, formulation, materials, blocks=None, threads=1, bbar=False):
         L = lib()
         self.X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, 3)
         self.conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 8)
         self.nnd, self.nel = self.X.shape[0], self.conn.shape[0]
         self.h = L.orc_model_create(self.nnd, _d(self.X), self.nel, _i(self.conn))
         L.orc_set_formulation(self.h, FORMS[formulation])
+        L.orc_set_bbar(self.h, int(bool(bbar)))
         if isinstance(materials, dict):
             materials = [materials]
         for b, m in enumerate(materials):
@@ -220,7 +222,8 @@ class OracleModel:
 
 
 def model_from_fixture(fx, threads=1):
-    m = OracleModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], threads=threads)
+    m = OracleModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], threads=threads,
+                    bbar=fx.get("strain_displacement") == "B-bar")
     m.set_schedule(fx["schedule"])
     for n, d, v, s in fx["kbc"]:
         m.add_kbc(n, d, v, s)

@@ -416,6 +416,12 @@ int tg_tuning_get(const tg_context* c, int* tile_blocks, int* stages, int* tange
   return TG_OK;
 }
 
+int tg_element_strain_displacement(tg_context* c, int option) {
+  if (!c || (option != TG_STRAIN_STANDARD && option != TG_STRAIN_BBAR)) return TG_ERR_ARG;
+  c->mats.bbar = option == TG_STRAIN_BBAR;
+  return TG_OK;
+}
+
 int tg_element_set(tg_context* c, int formulation) {
   if (!c || (formulation != TG_SMALL_STRAIN && formulation != TG_TOTAL_LAGRANGIAN)) return TG_ERR_ARG;
   c->formulation = formulation;

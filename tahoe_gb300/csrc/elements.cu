@@ -294,6 +294,31 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
     wdet = point_gradients<double>(sX[le], ip, g);  // weight 1 (HexahedronT.cpp:1545)
     if (!(wdet > 0.0)) bad = true;
   }
+  // B-bar: element-mean shape-function gradients (SmallStrainT::SetMeanGradient,
+  // SmallStrainT.cpp:404-421), summed over the element's 8 lanes
+  const bool bbar = mt.bbar && mt.formulation == TG_SMALL_STRAIN;  // uniform
+  double mean[3][8];
+  if (bbar) {
+    const bool use = valid && !bad;
+    double vol = use ? wdet : 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int a = 0; a < 8; ++a) mean[d][a] = use ? wdet * g[d][a] : 0.0;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      vol += __shfl_xor_sync(0xffffffffu, vol, o);
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int a = 0; a < 8; ++a) mean[d][a] += __shfl_xor_sync(0xffffffffu, mean[d][a], o);
+    }
+    const double iv = vol > 0.0 ? 1.0 / vol : 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int a = 0; a < 8; ++a) mean[d][a] *= iv;
+  }
   const bool is_j2 = valid && m.kind == TG_MAT_SS_J2;
   bool j2_alloc = false;
   double rel[6] = {0, 0, 0, 0, 0, 0};
@@ -316,6 +341,17 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
     eps[3] = 0.5 * (H[5] + H[7]);
     eps[4] = 0.5 * (H[2] + H[6]);
     eps[5] = 0.5 * (H[1] + H[3]);
+    if (bbar) {
+      // Hughes (4.5.11-16): the point dilatation replaced by the element mean
+      double th = 0.0;
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+        th += mean[0][a] * sU[le][a][0] + mean[1][a] * sU[le][a][1] + mean[2][a] * sU[le][a][2];
+      const double dv = (th - (H[0] + H[4] + H[8])) / 3.0;
+      eps[0] += dv;
+      eps[1] += dv;
+      eps[2] += dv;
+    }
     if (is_j2) {
       j2_alloc = j2.alloc[e] != 0;
       if (j2_alloc)
@@ -369,6 +405,14 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
         f[a][0] = wdet * (g[0][a] * s[0] + g[2][a] * s[4] + g[1][a] * s[5]);
         f[a][1] = wdet * (g[1][a] * s[1] + g[2][a] * s[3] + g[0][a] * s[5]);
         f[a][2] = wdet * (g[2][a] * s[2] + g[1][a] * s[3] + g[0][a] * s[4]);
+      }
+      if (bbar) {
+        // B-bar^T sigma: the normal rows carry (mean_a - grad_a)/3
+        const double tr = wdet * (s[0] + s[1] + s[2]) / 3.0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) f[a][d] += tr * (mean[d][a] - g[d][a]);
       }
     } else {
       double F[9];
@@ -526,6 +570,8 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
   __shared__ T sG[kTanElems][8][3][8];  // per point spatial gradients
   __shared__ T sD[kTanElems][8][36];    // per point moduli (scaled)
   __shared__ T sS[kTanElems][8][6];     // per point Cauchy stress (scaled, TL only)
+  __shared__ T sW[kTanElems][8];        // per point w det J (B-bar mean gradients)
+  __shared__ T sM[kTanElems][3][8];     // element-mean gradients (B-bar)
   const int tid = threadIdx.x;
   const int e0 = blockIdx.x * kTanElems;
 
@@ -612,9 +658,33 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
       for (int k = 0; k < 36; ++k) sD[le][ip][k] = scale * D[k];
 #pragma unroll
       for (int k = 0; k < 6; ++k) sS[le][ip][k] = scale * s[k];
+      sW[le][ip] = okm ? detj : T(0);
     }
   }
   __syncthreads();
+  const bool bbar = mt.bbar && mt.formulation == TG_SMALL_STRAIN;
+  if (bbar) {
+    // element-mean gradients (SmallStrainT::SetMeanGradient, :404-421)
+    if (tid < kTanElems * 8) {
+      const int le = tid >> 3, a = tid & 7;
+      if (e0 + le < nel) {
+        T vol = T(0), m0 = T(0), m1 = T(0), m2 = T(0);
+#pragma unroll
+        for (int ip = 0; ip < 8; ++ip) {
+          const T w = sW[le][ip];
+          vol += w;
+          m0 += w * sG[le][ip][0][a];
+          m1 += w * sG[le][ip][1][a];
+          m2 += w * sG[le][ip][2][a];
+        }
+        const T iv = vol > T(0) ? T(1) / vol : T(0);
+        sM[le][0][a] = m0 * iv;
+        sM[le][1][a] = m1 * iv;
+        sM[le][2][a] = m2 * iv;
+      }
+    }
+    __syncthreads();
+  }
 
   const int le = tid / kSlots, slot = tid - le * kSlots;
   const int e = e0 + le;
@@ -636,6 +706,21 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
 #pragma unroll
       for (int j = 0; j < 3; ++j)
         h[V][j] = D[V * 6 + vgt(j, 0)] * gb[0] + D[V * 6 + vgt(j, 1)] * gb[1] + D[V * 6 + vgt(j, 2)] * gb[2];
+    if (bbar) {
+      // B-bar columns: normal rows plus f = (mean - grad)/3 (Hughes 4.5.11-16)
+      const T fa[3] = {(sM[le][0][a] - ga[0]) / T(3), (sM[le][1][a] - ga[1]) / T(3), (sM[le][2][a] - ga[2]) / T(3)};
+      const T fb[3] = {(sM[le][0][b] - gb[0]) / T(3), (sM[le][1][b] - gb[1]) / T(3), (sM[le][2][b] - gb[2]) / T(3)};
+#pragma unroll
+      for (int V = 0; V < 6; ++V) {
+        const T ds = D[V * 6 + 0] + D[V * 6 + 1] + D[V * 6 + 2];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) h[V][j] += fb[j] * ds;
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) K[i * 3 + j] += fa[i] * (h[0][j] + h[1][j] + h[2][j]);
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll

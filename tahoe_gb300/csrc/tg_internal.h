@@ -33,6 +33,7 @@ struct MatParams {
 struct MatTable {
   int nblocks;
   int formulation;
+  int bbar;  // small strain: B-bar (mean dilatation) strain-displacement
   MatParams m[kMaxBlocks];
 };
 

@@ -17,6 +17,7 @@ ERRORS = {
     -6: "TG_ERR_NOT_CONVERGED", -7: "TG_ERR_DIVERGED", -8: "TG_ERR_CAPACITY",
 }
 SMALL_STRAIN, TOTAL_LAGRANGIAN = 0, 1
+STRAIN_STANDARD, STRAIN_BBAR = 0, 1
 MAT_SS_HOOKEAN, MAT_SS_J2, MAT_FS_SIMO, MAT_FS_STVENANT = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 PRECOND_JACOBI, PRECOND_BLOCK_JACOBI = 0, 1
@@ -80,6 +81,7 @@ _SIGS = {
     "tg_time_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     "tg_spmv_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "tg_tangent_config": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tg_element_strain_displacement": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_spmv_release": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
@@ -415,6 +417,9 @@ class Context:
 
     def spmv_config(self, tile_blocks, stages):
         self._chk(self.L.tg_spmv_config(self.h, int(tile_blocks), int(stages)), "tg_spmv_config")
+
+    def set_strain_displacement(self, option):
+        self._chk(self.L.tg_element_strain_displacement(self.h, int(option)), "tg_element_strain_displacement")
 
     def spmv_release(self, per_warp):
         self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")

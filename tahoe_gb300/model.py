@@ -24,6 +24,7 @@ ELEMENT_GROUPS = {
     "total_lagrangian": lib.TOTAL_LAGRANGIAN,
     "updated_lagrangian": lib.TOTAL_LAGRANGIAN,
 }
+STRAIN_DISPLACEMENT = {"standard": lib.STRAIN_STANDARD, "B-bar": lib.STRAIN_BBAR}
 MATERIALS = {
     "small_strain_StVenant": lib.MAT_SS_HOOKEAN,
     "small_strain_Hookean": lib.MAT_SS_HOOKEAN,
@@ -66,8 +67,10 @@ def schedule_value(pts, t):
 
 
 class SolidModel:
-    def __init__(self, X, conn, formulation, materials, blocks=None, device=0):
+    def __init__(self, X, conn, formulation, materials, blocks=None, device=0, strain_displacement="standard"):
         self.X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+        # small_strain's strain_displacement option ("standard" | "B-bar")
+        self.strain_displacement = STRAIN_DISPLACEMENT[strain_displacement]
         self.conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 8)
         self.formulation = ELEMENT_GROUPS.get(formulation, formulation)
         if isinstance(materials, dict):
@@ -104,6 +107,7 @@ class SolidModel:
         c = lib.Context(self.device)
         c.upload(self.X, self.conn, eq)
         c.set_formulation(self.formulation)
+        c.set_strain_displacement(self.strain_displacement)
         for b, m in enumerate(self.materials):
             kind, p = material_params(m)
             c.set_material(b, kind, p)
@@ -218,7 +222,8 @@ class SolidModel:
 
 
 def model_from_fixture(fx, device=0):
-    m = SolidModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], device=device)
+    m = SolidModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], device=device,
+                   strain_displacement=fx.get("strain_displacement", "standard"))
     m.set_schedule(fx["schedule"])
     for n, d, v, s in fx["kbc"]:
         m.add_kbc(n, d, v, s)

@@ -35,6 +35,8 @@ DECKS = [
      ["benchmark/beam.Newton.TotLag.io0.run"]),
     ("beam_newton_updlag", "level.0/3D.elastostatic/beam.Newton.xml",
      ["benchmark/beam.Newton.io0.run"]),
+    ("beam_bbar", "level.0/3D.elastostatic/beam.B_bar.xml",
+     ["benchmark/beam.B_bar.io0.run"]),
 ]
 
 
