@@ -171,6 +171,14 @@ int tg_pcg_solve_noalloc(tg_context* ctx, const double* rhs_device, double* du_d
  * J2SSC0HardeningT::Update/Reset, J2SSC0HardeningT.cpp:204,244) */
 int tg_close_step(tg_context* ctx);
 int tg_reset_step(tg_context* ctx);
+/* Nodal stresses of the .run output at the current state (no history
+ * written): SolidElementT::ComputeOutput (SolidElementT.cpp:1540-1570) --
+ * Cauchy stress at the integration points extrapolated to the element nodes
+ * (HexahedronT::SetExtrapolation, HexahedronT.cpp:2071) and averaged over the
+ * elements sharing a node (GroupAverageT.cpp:40-56).  out: nnd*6, Voigt
+ * [11,22,33,23,13,12].  Call before tg_close_step, as the reference writes
+ * output before the element groups close the step. */
+int tg_nodal_stress(tg_context* ctx, double* out);
 /* per-integration-point flags (nel*8, tg_j2_flag) -- the active set */
 int tg_get_active_set(tg_context* ctx, signed char* flags);
 /* equivalent plastic strain alpha (nel*8) and plastic strain (nel*8*6) */

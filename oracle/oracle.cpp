@@ -372,6 +372,7 @@ void build_msr(const Model& M, bool upper, std::vector<int>& bindx) {
 struct ElemOut {
   double Ke[576];
   double fint[24];
+  double sig[8][6]; /* Cauchy stress per integration point (residual pass) */
 };
 
 /* element geometry at one IP: ParentDomainT::ComputeDNa (ParentDomainT.cpp:426-470);
@@ -516,6 +517,7 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
         hooke(m.C, eps, s);
         std::memcpy(D, m.C, sizeof(D));
       }
+      if (!wantK) std::memcpy(out.sig[ip], s, sizeof(double) * 6);
       if (wantK) {
         add_btdb_b(B, D, wdet, out.Ke);
       } else {
@@ -538,6 +540,7 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
       if (!(J > 0.0)) return -1;
       if (m.kind == ORC_MAT_FS_SIMO) simo(m, F, s, wantK ? D : nullptr);
       else stvenant(m, F, s, wantK ? D : nullptr);
+      if (!wantK) std::memcpy(out.sig[ip], s, sizeof(double) * 6);
       double Fi[9];
       inv3(F, J, Fi);
       /* spatial gradients dN/dx_k = sum_J dN/dX_J Finv(J,k) */
@@ -966,6 +969,39 @@ int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int 
 }
 
 namespace {
+/* Nodal stresses as written to the .run output (SolidElementT::ComputeOutput,
+ * SolidElementT.cpp:1540-1570): Cauchy stress at every integration point
+ * extrapolated to the element's nodes with the hex8 smoothing matrix of
+ * HexahedronT::SetExtrapolation (HexahedronT.cpp:2071-2140, entries
+ * (1 + sqrt3 * s_a . t_p)/8 for node signs s_a and point signs t_p), then
+ * averaged over the elements sharing each node (GroupAverageT,
+ * GroupAverageT.cpp:40-56).  Voigt order [11,22,33,23,13,12]. */
+int nodal_stress(Model& M, const double* u, int iteration, double* out) {
+  static const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                               {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  const double r3 = std::sqrt(3.0);
+  std::vector<int> count(M.nnd, 0);
+  std::fill(out, out + (size_t)M.nnd * 6, 0.0);
+  ElemOut o;
+  for (int e = 0; e < M.nel; ++e) {
+    if (element(M, e, u, iteration, false, o, false)) return -1;
+    for (int a = 0; a < 8; ++a) {
+      const int n = M.conn[e * 8 + a];
+      ++count[n];
+      for (int p = 0; p < 8; ++p) {
+        const double w = 0.125 * (1.0 + r3 * (sg[a][0] * sg[p][0] + sg[a][1] * sg[p][1] + sg[a][2] * sg[p][2]));
+        for (int c = 0; c < 6; ++c) out[(size_t)n * 6 + c] += w * o.sig[p][c];
+      }
+    }
+  }
+  for (int n = 0; n < M.nnd; ++n)
+    if (count[n])
+      for (int c = 0; c < 6; ++c) out[(size_t)n * 6 + c] /= count[n];
+  return 0;
+}
+}  // namespace
+
+namespace {
 /* One load step of NLSolver::Solve at time t from the current state; its =
  * Newton iterations made.  0 converged, else failure (state not restored). */
 int newton_step(Model* M, double t, double rel_tol, double abs_tol, int max_its, double div_tol, int solver,
@@ -1018,7 +1054,7 @@ int newton_step(Model* M, double t, double rel_tol, double abs_tol, int max_its,
  * that failed with no cut left. */
 int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its, double div_tol,
                  int solver, double lin_tol, int max_cuts, int quick_iter, int quick_count, double* u_hist,
-                 int* its_hist, int* cuts_out) {
+                 int* its_hist, int* cuts_out, double* s_hist) {
   Model* M = static_cast<Model*>(m);
   ensure_setup(*M);
   enum { kSame, kDecrease, kIncrease };
@@ -1059,6 +1095,12 @@ int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol,
       if (cuts_out) *cuts_out = total_cuts;
       continue;
     }
+    const double kk = std::round(t / dt);
+    const bool at_output = std::fabs(t - kk * dt) <= 1e-9 * dt && kk >= 1;
+    /* output before the element groups close the step (FEManagerT::CloseStep,
+     * FEManagerT.cpp:625-645) */
+    if (at_output && s_hist && nodal_stress(*M, M->u.data(), its - 1, s_hist + (size_t)(kk - 1) * M->nnd * 6))
+      return (int)kk;
     for (J2Card& c : M->j2) j2_update(c);
     /* NLSolver::DoConverged: fNumIteration is its - 1 here */
     if (quick_iter > 1 && its - 1 < quick_iter) {
@@ -1077,6 +1119,13 @@ int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol,
     }
   }
   return 0;
+}
+
+
+int orc_nodal_stress(void* m, const double* u, int iteration, double* out) {
+  Model* M = static_cast<Model*>(m);
+  ensure_setup(*M);
+  return nodal_stress(*M, u, iteration, out);
 }
 
 int orc_j2_state(void* m, signed char* flags, double* alpha, double* eps_p) {

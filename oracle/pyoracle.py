@@ -47,7 +47,8 @@ def lib():
                          ctypes.c_double, ctypes.c_int, ctypes.c_double, _dp, _ip]),
             ("orc_run_cuts", [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                               ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
-                              ctypes.c_int, _dp, _ip, _ip]),
+                              ctypes.c_int, _dp, _ip, _ip, _dp]),
+            ("orc_nodal_stress", [_dp, ctypes.c_int, _dp]),
             ("orc_j2_state", [ctypes.c_void_p, _dp, _dp]),
             ("orc_nodal_internal_force", [_dp, ctypes.c_int, _dp]),
             ("orc_get_u", [_dp]),
@@ -64,7 +65,7 @@ def lib():
 
 
 def _d(a):
-    return a.ctypes.data_as(_dp)
+    return None if a is None else a.ctypes.data_as(_dp)
 
 
 def _i(a):
@@ -184,16 +185,28 @@ class OracleModel:
         return s, uh, its
 
     def run_cuts(self, nsteps, dt, rel_tol=1e-12, abs_tol=1e-10, max_its=10, div_tol=10.0, solver=0,
-                 lin_tol=1e-12, max_cuts=0, quick_iter=6, quick_count=3):
+                 lin_tol=1e-12, max_cuts=0, quick_iter=6, quick_count=3, want_stress=False):
         """run() inside the reference's step sequence with load-step cuts;
         returns (status, u at the original steps, iterations per original
-        step, cuts made)."""
+        step, cuts made) and, with want_stress, the nodal output stresses
+        per original step."""
         uh = np.zeros((nsteps, self.nnd, 3))
         its = np.zeros(nsteps, dtype=np.int32)
+        sh = np.zeros((nsteps, self.nnd, 6)) if want_stress else None
         cuts = ctypes.c_int(0)
         s = lib().orc_run_cuts(self.h, nsteps, dt, rel_tol, abs_tol, max_its, div_tol, solver, lin_tol, max_cuts,
-                               quick_iter, quick_count, _d(uh), _i(its), ctypes.byref(cuts))
+                               quick_iter, quick_count, _d(uh), _i(its), ctypes.byref(cuts), _d(sh))
+        if want_stress:
+            return s, uh, its, cuts.value, sh
         return s, uh, its, cuts.value
+
+    def nodal_stress(self, u, iteration=0):
+        out = np.zeros(self.nnd * 6)
+        s = lib().orc_nodal_stress(self.h, _d(np.ascontiguousarray(u, dtype=np.float64).reshape(-1)), int(iteration),
+                                   _d(out))
+        if s:
+            raise RuntimeError("oracle nodal stress status %d" % s)
+        return out.reshape(-1, 6)
 
     def j2_state(self):
         fl = np.zeros(self.nel * 8, dtype=np.int8)

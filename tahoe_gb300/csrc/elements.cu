@@ -259,7 +259,8 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
                                                        const int* __restrict__ conn, const int8_t* __restrict__ blk,
                                                        int nel, const double4_32a* __restrict__ u, MatTable mt,
                                                        J2View j2, int iteration, int commit_state,
-                                                       double4_32a* __restrict__ fint, int* status) {
+                                                       double4_32a* __restrict__ fint, int* status,
+                                                       double* __restrict__ ip_sig) {
   __shared__ double sX[kResElems][8][3];
   __shared__ double sU[kResElems][8][3];
   const int tid = threadIdx.x;
@@ -445,6 +446,12 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
           for (int i = 0; i < 3; ++i) f[a][i] = scale * (sm[i * 3 + 0] * gx[0] + sm[i * 3 + 1] * gx[1] + sm[i * 3 + 2] * gx[2]);
         }
       }
+    }
+    if (ip_sig) {
+      // output pass: the point's Cauchy stress (SolidElementT::ComputeOutput)
+      double* o = ip_sig + ((long long)e * 8 + ip) * 6;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) o[k] = bad ? 0.0 : s[k];
     }
   }
   if (bad) {
@@ -780,10 +787,11 @@ J2View j2view(Context* c) {
   return v;
 }
 
-int residual_impl(Context* c, int commit_state) {
+int residual_impl(Context* c, int commit_state, double* d_ip_sig = nullptr) {
   const int grid = (c->nel + kResElems - 1) / kResElems;
   residual_kernel<<<grid, 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats,
-                                               j2view(c), c->iteration, commit_state, c->d_fint, c->d_status);
+                                               j2view(c), c->iteration, commit_state, c->d_fint, c->d_status,
+                                               d_ip_sig);
   c->launches++;
   return ok(c, cudaGetLastError(), "residual_kernel") ? TG_OK : TG_ERR_CUDA;
 }
@@ -803,6 +811,50 @@ int launch_residual_commit(Context* c, int commit) {
                                                       c->d_resid);
   c->launches++;
   return ok(c, cudaGetLastError(), "gather_residual_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+namespace {
+// Nodal output stress: every incident element's point stresses extrapolated
+// to the node with the hex8 smoothing matrix (HexahedronT::SetExtrapolation,
+// HexahedronT.cpp:2071-2140: (1 + sqrt3 s_a . t_p)/8 for node signs s_a and
+// point signs t_p), averaged over the incident elements (GroupAverageT).
+__global__ void nodal_stress_kernel(int nnd, const int* __restrict__ nptr, const int* __restrict__ nlist,
+                                    const double* __restrict__ ip_sig, double* __restrict__ out) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnd) return;
+  const double r3 = 1.7320508075688772;  // sqrt(3)
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const int k0 = nptr[n], k1 = nptr[n + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int code = nlist[k];
+    const long long e = code >> 3;
+    const int a = code & 7;
+    const int sa0 = (a == 1 || a == 2 || a == 5 || a == 6) ? 1 : -1;
+    const int sa1 = (a == 2 || a == 3 || a == 6 || a == 7) ? 1 : -1;
+    const int sa2 = a >= 4 ? 1 : -1;
+    for (int p = 0; p < 8; ++p) {
+      const int sp0 = (p == 1 || p == 2 || p == 5 || p == 6) ? 1 : -1;
+      const int sp1 = (p == 2 || p == 3 || p == 6 || p == 7) ? 1 : -1;
+      const int sp2 = p >= 4 ? 1 : -1;
+      const double w = 0.125 * (1.0 + r3 * (double)(sa0 * sp0 + sa1 * sp1 + sa2 * sp2));
+      const double* sg = ip_sig + (e * 8 + p) * 6;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) acc[c] += w * sg[c];
+    }
+  }
+  const double inv = k1 > k0 ? 1.0 / (double)(k1 - k0) : 0.0;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) out[(long long)n * 6 + c] = acc[c] * inv;
+}
+}  // namespace
+
+int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out) {
+  int s = residual_impl(c, 0, d_ip_sig);
+  if (s) return s;
+  nodal_stress_kernel<<<(c->nnd + 255) / 256, 256, 0, c->stream>>>(c->nnd, c->d_node_elem_ptr, c->d_node_elem,
+                                                                    d_ip_sig, d_out);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "nodal_stress_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
 template <int EPB>

@@ -238,6 +238,23 @@ int tg_reset_step(tg_context* c) {
   return s;
 }
 
+int tg_nodal_stress(tg_context* c, double* out) {
+  if (!c || !out || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  double *d_ip = nullptr, *d_out = nullptr;
+  if (!ok(c, cudaMallocAsync((void**)&d_ip, sizeof(double) * 48 * (size_t)c->nel, c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&d_out, sizeof(double) * 6 * (size_t)c->nnd, c->stream), "alloc"))
+    return TG_ERR_OOM;
+  int s = launch_nodal_stress(c, d_ip, d_out);
+  if (!s) s = check_status(c);
+  if (!s && !copy_sync(c, out, d_out, sizeof(double) * 6 * (size_t)c->nnd, cudaMemcpyDeviceToHost, "stress"))
+    s = TG_ERR_CUDA;
+  cudaFreeAsync(d_ip, c->stream);
+  cudaFreeAsync(d_out, c->stream);
+  if (!ok(c, cudaStreamSynchronize(c->stream), "sync") && !s) s = TG_ERR_CUDA;
+  return s;
+}
+
 int tg_get_active_set(tg_context* c, signed char* flags) {
   if (!c || !flags || c->nel <= 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;

@@ -262,6 +262,9 @@ size_t pcg_scratch_bytes(const Context* c);
 int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
                       int max_it, int precond, int* iters, double* rel_res);
 int launch_residual_nocommit(Context* c);
+// output pass (no history written): point stresses into d_ip_sig (nel*8*6),
+// extrapolated and averaged nodal stresses into d_out (nnd*6)
+int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out);
 // rhs = R - K v on active rows (v nodal, K the last tangent), FP64
 // accumulation; with zero_base, rhs = -K v
 int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs, bool zero_base = false, int nvec = 1);

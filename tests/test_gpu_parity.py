@@ -40,14 +40,25 @@ def random_u(nnd, scale, seed):
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
 def test_golden_decks_on_gpu(name):
+    """Displacements and the nodal output stresses (extrapolated, averaged;
+    written before the step is closed) against the reference's .run files."""
     fx = load_fixture(name)
     m = model_from_fixture(fx)
     sv = fx["solver"]
+    stress = {}
+
+    def on_step(step, ctx):
+        stress[step - 1] = ctx.nodal_stress()
+
     hist, reps = m.run(fx["nsteps"], fx["dt"], rel_tol=sv["rel_tol"], abs_tol=sv["abs_tol"],
                        max_iterations=sv["max_its"], div_tol=sv["div_tol"], precision=lib.FP64,
-                       lin_rel_tol=1e-14, lin_max_it=5000)
+                       lin_rel_tol=1e-14, lin_max_it=5000, on_step=on_step)
     for step, ref in golden_displacements(fx).items():
         assert rel_err(hist[step], ref) < 1e-9, (name, step)
+    for o in fx["outputs"]:
+        step = int(round(o["time"] / fx["dt"])) - 1
+        ref = np.array(o["rows"])[:, 3:9]
+        assert rel_err(stress[step], ref) < 1e-9, (name, step)
 
 
 @pytest.mark.parametrize("jitter", [0.0, 0.2])

@@ -20,6 +20,22 @@ def test_oracle_reproduces_golden_displacements(name):
         assert rel_err(uh[step], ref) < 1e-11, (name, step)
 
 
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_oracle_nodal_stress_matches_golden(name):
+    """Output stresses (integration-point Cauchy stress extrapolated to the
+    nodes and averaged over elements) against the .run files' s11..s12."""
+    fx = load_fixture(name)
+    m = model_from_fixture(fx)
+    sv = fx["solver"]
+    status, uh, its, cuts, sh = m.run_cuts(fx["nsteps"], fx["dt"], sv["rel_tol"], sv["abs_tol"], sv["max_its"],
+                                           sv["div_tol"], 0, want_stress=True)
+    assert status == 0 and cuts == 0
+    for o in fx["outputs"]:
+        step = int(round(o["time"] / fx["dt"])) - 1
+        ref = np.array(o["rows"])[:, o["labels"].index("s11"):o["labels"].index("s12") + 1]
+        assert rel_err(sh[step], ref) < 1e-11, (name, step)
+
+
 def test_oracle_j2_alpha_matches_golden():
     fx = load_fixture("mat08_j2_cube")
     m = model_from_fixture(fx)
