@@ -179,6 +179,12 @@ int tg_reset_step(tg_context* ctx);
  * [11,22,33,23,13,12].  Call before tg_close_step, as the reference writes
  * output before the element groups close the step. */
 int tg_nodal_stress(tg_context* ctx, double* out);
+/* Nodal material output of the small-strain J2 material (alpha, von Mises
+ * stress, pressure; J2SSKStV::ComputeOutput, J2SSKStV.cpp:181-207), point
+ * values extrapolated and averaged as the stresses; out: nnd*3.  Alpha is
+ * zero at points of other materials; von Mises stress and pressure are
+ * formed from their stress. */
+int tg_nodal_material_output(tg_context* ctx, double* out);
 /* per-integration-point flags (nel*8, tg_j2_flag) -- the active set */
 int tg_get_active_set(tg_context* ctx, signed char* flags);
 /* equivalent plastic strain alpha (nel*8) and plastic strain (nel*8*6) */

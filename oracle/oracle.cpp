@@ -373,6 +373,7 @@ struct ElemOut {
   double Ke[576];
   double fint[24];
   double sig[8][6]; /* Cauchy stress per integration point (residual pass) */
+  double mat[8][3]; /* J2 material output per point: alpha, von Mises, pressure */
 };
 
 /* element geometry at one IP: ParentDomainT::ComputeDNa (ParentDomainT.cpp:426-470);
@@ -517,7 +518,20 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
         hooke(m.C, eps, s);
         std::memcpy(D, m.C, sizeof(D));
       }
-      if (!wantK) std::memcpy(out.sig[ip], s, sizeof(double) * 6);
+      if (!wantK) {
+        std::memcpy(out.sig[ip], s, sizeof(double) * 6);
+        /* J2SSKStV::ComputeOutput (J2SSKStV.cpp:181-207) */
+        const double p = (s[0] + s[1] + s[2]) / 3.0;
+        double dv[3] = {s[0] - p, s[1] - p, s[2] - p};
+        double i2 = s[3] * s[3] + s[4] * s[4] + s[5] * s[5] - dv[0] * dv[1] - dv[1] * dv[2] - dv[2] * dv[0];
+        if (i2 < 0.0) i2 = 0.0;
+        double al = 0.0;
+        if (card && card->allocated)
+          al = card->alpha[ip] + (card->flags[ip] == ORC_J2_PLASTIC ? std::sqrt(2.0 / 3.0) * card->dgamma[ip] : 0.0);
+        out.mat[ip][0] = al;
+        out.mat[ip][1] = std::sqrt(3.0 * i2);
+        out.mat[ip][2] = p;
+      }
       if (wantK) {
         add_btdb_b(B, D, wdet, out.Ke);
       } else {
@@ -540,7 +554,16 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
       if (!(J > 0.0)) return -1;
       if (m.kind == ORC_MAT_FS_SIMO) simo(m, F, s, wantK ? D : nullptr);
       else stvenant(m, F, s, wantK ? D : nullptr);
-      if (!wantK) std::memcpy(out.sig[ip], s, sizeof(double) * 6);
+      if (!wantK) {
+        std::memcpy(out.sig[ip], s, sizeof(double) * 6);
+        const double p = (s[0] + s[1] + s[2]) / 3.0;
+        double dv[3] = {s[0] - p, s[1] - p, s[2] - p};
+        double i2 = s[3] * s[3] + s[4] * s[4] + s[5] * s[5] - dv[0] * dv[1] - dv[1] * dv[2] - dv[2] * dv[0];
+        if (i2 < 0.0) i2 = 0.0;
+        out.mat[ip][0] = 0.0;
+        out.mat[ip][1] = std::sqrt(3.0 * i2);
+        out.mat[ip][2] = p;
+      }
       double Fi[9];
       inv3(F, J, Fi);
       /* spatial gradients dN/dx_k = sum_J dN/dX_J Finv(J,k) */
@@ -976,12 +999,14 @@ namespace {
  * (1 + sqrt3 * s_a . t_p)/8 for node signs s_a and point signs t_p), then
  * averaged over the elements sharing each node (GroupAverageT,
  * GroupAverageT.cpp:40-56).  Voigt order [11,22,33,23,13,12]. */
-int nodal_stress(Model& M, const double* u, int iteration, double* out) {
+int nodal_output(Model& M, const double* u, int iteration, double* out, int what) {
+  /* what: 0 stresses (nnd*6), 1 J2 material output alpha/VM/pressure (nnd*3) */
   static const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
   const double r3 = std::sqrt(3.0);
+  const int nv = what == 0 ? 6 : 3;
   std::vector<int> count(M.nnd, 0);
-  std::fill(out, out + (size_t)M.nnd * 6, 0.0);
+  std::fill(out, out + (size_t)M.nnd * nv, 0.0);
   ElemOut o;
   for (int e = 0; e < M.nel; ++e) {
     if (element(M, e, u, iteration, false, o, false)) return -1;
@@ -990,15 +1015,17 @@ int nodal_stress(Model& M, const double* u, int iteration, double* out) {
       ++count[n];
       for (int p = 0; p < 8; ++p) {
         const double w = 0.125 * (1.0 + r3 * (sg[a][0] * sg[p][0] + sg[a][1] * sg[p][1] + sg[a][2] * sg[p][2]));
-        for (int c = 0; c < 6; ++c) out[(size_t)n * 6 + c] += w * o.sig[p][c];
+        const double* v = what == 0 ? o.sig[p] : o.mat[p];
+        for (int c = 0; c < nv; ++c) out[(size_t)n * nv + c] += w * v[c];
       }
     }
   }
   for (int n = 0; n < M.nnd; ++n)
     if (count[n])
-      for (int c = 0; c < 6; ++c) out[(size_t)n * 6 + c] /= count[n];
+      for (int c = 0; c < nv; ++c) out[(size_t)n * nv + c] /= count[n];
   return 0;
 }
+int nodal_stress(Model& M, const double* u, int iteration, double* out) { return nodal_output(M, u, iteration, out, 0); }
 }  // namespace
 
 namespace {
@@ -1054,7 +1081,7 @@ int newton_step(Model* M, double t, double rel_tol, double abs_tol, int max_its,
  * that failed with no cut left. */
 int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its, double div_tol,
                  int solver, double lin_tol, int max_cuts, int quick_iter, int quick_count, double* u_hist,
-                 int* its_hist, int* cuts_out, double* s_hist) {
+                 int* its_hist, int* cuts_out, double* s_hist, double* m_hist) {
   Model* M = static_cast<Model*>(m);
   ensure_setup(*M);
   enum { kSame, kDecrease, kIncrease };
@@ -1101,6 +1128,9 @@ int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol,
      * FEManagerT.cpp:625-645) */
     if (at_output && s_hist && nodal_stress(*M, M->u.data(), its - 1, s_hist + (size_t)(kk - 1) * M->nnd * 6))
       return (int)kk;
+    if (at_output && m_hist &&
+        nodal_output(*M, M->u.data(), its - 1, m_hist + (size_t)(kk - 1) * M->nnd * 3, 1))
+      return (int)kk;
     for (J2Card& c : M->j2) j2_update(c);
     /* NLSolver::DoConverged: fNumIteration is its - 1 here */
     if (quick_iter > 1 && its - 1 < quick_iter) {
@@ -1126,6 +1156,11 @@ int orc_nodal_stress(void* m, const double* u, int iteration, double* out) {
   Model* M = static_cast<Model*>(m);
   ensure_setup(*M);
   return nodal_stress(*M, u, iteration, out);
+}
+int orc_nodal_material_output(void* m, const double* u, int iteration, double* out) {
+  Model* M = static_cast<Model*>(m);
+  ensure_setup(*M);
+  return nodal_output(*M, u, iteration, out, 1);
 }
 
 int orc_j2_state(void* m, signed char* flags, double* alpha, double* eps_p) {

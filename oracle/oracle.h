@@ -88,11 +88,15 @@ int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int 
  * steps k*dt; *cuts_out = cuts made.  0, or the failing original step. */
 int orc_run_cuts(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int max_its, double div_tol,
                  int solver, double lin_tol, int max_cuts, int quick_iter, int quick_count, double* u_hist,
-                 int* its_hist, int* cuts_out, double* s_hist);
+                 int* its_hist, int* cuts_out, double* s_hist, double* m_hist);
 /* nodal stresses of the .run output (extrapolated from the integration
  * points, averaged over elements; nnd*6, Voigt [11,22,33,23,13,12]) at u with
  * the current history; s_hist of orc_run_cuts holds them per original step */
 int orc_nodal_stress(void* m, const double* u, int iteration, double* out);
+/* J2 material output (alpha, von Mises, pressure; J2SSKStV::ComputeOutput)
+ * extrapolated and averaged the same way (nnd*3); m_hist of orc_run_cuts
+ * holds it per original step */
+int orc_nodal_material_output(void* m, const double* u, int iteration, double* out);
 
 /* J2 state after the last converged step (nel*8 each; alpha per IP). */
 int orc_j2_state(void* m, signed char* flags, double* alpha, double* eps_p);

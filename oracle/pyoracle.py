@@ -47,8 +47,9 @@ def lib():
                          ctypes.c_double, ctypes.c_int, ctypes.c_double, _dp, _ip]),
             ("orc_run_cuts", [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                               ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
-                              ctypes.c_int, _dp, _ip, _ip, _dp]),
+                              ctypes.c_int, _dp, _ip, _ip, _dp, _dp]),
             ("orc_nodal_stress", [_dp, ctypes.c_int, _dp]),
+            ("orc_nodal_material_output", [_dp, ctypes.c_int, _dp]),
             ("orc_j2_state", [ctypes.c_void_p, _dp, _dp]),
             ("orc_nodal_internal_force", [_dp, ctypes.c_int, _dp]),
             ("orc_get_u", [_dp]),
@@ -193,10 +194,12 @@ class OracleModel:
         uh = np.zeros((nsteps, self.nnd, 3))
         its = np.zeros(nsteps, dtype=np.int32)
         sh = np.zeros((nsteps, self.nnd, 6)) if want_stress else None
+        mh = np.zeros((nsteps, self.nnd, 3)) if want_stress else None
         cuts = ctypes.c_int(0)
         s = lib().orc_run_cuts(self.h, nsteps, dt, rel_tol, abs_tol, max_its, div_tol, solver, lin_tol, max_cuts,
-                               quick_iter, quick_count, _d(uh), _i(its), ctypes.byref(cuts), _d(sh))
+                               quick_iter, quick_count, _d(uh), _i(its), ctypes.byref(cuts), _d(sh), _d(mh))
         if want_stress:
+            self.material_output_hist = mh
             return s, uh, its, cuts.value, sh
         return s, uh, its, cuts.value
 

@@ -28,6 +28,7 @@ namespace tg {
 namespace {
 
 constexpr double kSqrt23 = 0.81649658092772603273;  // sqrt(2/3)
+constexpr int kOutPerPoint = 9;  // output pass: stress (6) + J2 material output (3)
 constexpr double kYieldTol = 1.0e-10;                // J2SSC0HardeningT.cpp:17
 constexpr double kGauss = 0.57735026918962576451;    // 1/sqrt(3)
 
@@ -322,6 +323,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   }
   const bool is_j2 = valid && m.kind == TG_MAT_SS_J2;
   bool j2_alloc = false;
+  double alpha_h = 0.0, alpha_out = 0.0;  // history alpha; alpha written by the output pass
   double rel[6] = {0, 0, 0, 0, 0, 0};
   double ftr = 0.0, nr = 0.0;
   const long long gid = (long long)e * 8 + ip;
@@ -365,6 +367,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
         for (int k = 0; k < 6; ++k) rel[k] = 2.0 * m.mu * dev[k];
         nr = sqrt(sym_dot(rel, rel));
         const double alpha = j2_alloc ? j2.alpha[gid] : 0.0;
+        alpha_h = alpha;
         ftr = nr - kSqrt23 * (m.hard_a * alpha + m.hard_b);
         yield_vote = ftr > kYieldTol;
       }
@@ -389,6 +392,9 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
 #pragma unroll
             for (int k = 0; k < 6; ++k) s[k] += -2.0 * m.mu * dg * (rel[k] / nr);
           }
+          // J2SSKStV::ComputeOutput (J2SSKStV.cpp:181-207): alpha with the
+          // pending increment of a plastic point
+          alpha_out = alpha_h + (plastic ? kSqrt23 * dg : 0.0);
           if (commit_state) {
             j2.flags[gid] = plastic ? (int8_t)TG_J2_PLASTIC : (int8_t)TG_J2_ELASTIC;
             j2.dgamma[gid] = dg;
@@ -449,9 +455,18 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
     }
     if (ip_sig) {
       // output pass: the point's Cauchy stress (SolidElementT::ComputeOutput)
-      double* o = ip_sig + ((long long)e * 8 + ip) * 6;
+      // and the J2 material output (alpha, von Mises, pressure;
+      // J2SSKStV::ComputeOutput, J2SSKStV.cpp:181-207)
+      double* o = ip_sig + ((long long)e * 8 + ip) * kOutPerPoint;
 #pragma unroll
       for (int k = 0; k < 6; ++k) o[k] = bad ? 0.0 : s[k];
+      const double p = (s[0] + s[1] + s[2]) / 3.0;
+      const double d0 = s[0] - p, d1 = s[1] - p, d2 = s[2] - p;
+      double i2 = s[3] * s[3] + s[4] * s[4] + s[5] * s[5] - d0 * d1 - d1 * d2 - d2 * d0;
+      i2 = i2 < 0.0 ? 0.0 : i2;
+      o[6] = bad ? 0.0 : alpha_out;
+      o[7] = bad ? 0.0 : sqrt(3.0 * i2);
+      o[8] = bad ? 0.0 : p;
     }
   }
   if (bad) {
@@ -823,7 +838,9 @@ __global__ void nodal_stress_kernel(int nnd, const int* __restrict__ nptr, const
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nnd) return;
   const double r3 = 1.7320508075688772;  // sqrt(3)
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  double acc[kOutPerPoint];
+#pragma unroll
+  for (int c = 0; c < kOutPerPoint; ++c) acc[c] = 0.0;
   const int k0 = nptr[n], k1 = nptr[n + 1];
   for (int k = k0; k < k1; ++k) {
     const int code = nlist[k];
@@ -837,14 +854,14 @@ __global__ void nodal_stress_kernel(int nnd, const int* __restrict__ nptr, const
       const int sp1 = (p == 2 || p == 3 || p == 6 || p == 7) ? 1 : -1;
       const int sp2 = p >= 4 ? 1 : -1;
       const double w = 0.125 * (1.0 + r3 * (double)(sa0 * sp0 + sa1 * sp1 + sa2 * sp2));
-      const double* sg = ip_sig + (e * 8 + p) * 6;
+      const double* sg = ip_sig + (e * 8 + p) * kOutPerPoint;
 #pragma unroll
-      for (int c = 0; c < 6; ++c) acc[c] += w * sg[c];
+      for (int c = 0; c < kOutPerPoint; ++c) acc[c] += w * sg[c];
     }
   }
   const double inv = k1 > k0 ? 1.0 / (double)(k1 - k0) : 0.0;
 #pragma unroll
-  for (int c = 0; c < 6; ++c) out[(long long)n * 6 + c] = acc[c] * inv;
+  for (int c = 0; c < kOutPerPoint; ++c) out[(long long)n * kOutPerPoint + c] = acc[c] * inv;
 }
 }  // namespace
 

@@ -238,20 +238,44 @@ int tg_reset_step(tg_context* c) {
   return s;
 }
 
-int tg_nodal_stress(tg_context* c, double* out) {
-  if (!c || !out || c->nnd <= 0) return TG_ERR_ARG;
-  if (set_device(c)) return TG_ERR_CUDA;
+namespace {
+// nodal output values (nnd x 9: stress, then alpha, von Mises, pressure)
+int nodal_output(tg_context* c, std::vector<double>& h) {
   double *d_ip = nullptr, *d_out = nullptr;
-  if (!ok(c, cudaMallocAsync((void**)&d_ip, sizeof(double) * 48 * (size_t)c->nel, c->stream), "alloc") ||
-      !ok(c, cudaMallocAsync((void**)&d_out, sizeof(double) * 6 * (size_t)c->nnd, c->stream), "alloc"))
+  if (!ok(c, cudaMallocAsync((void**)&d_ip, sizeof(double) * 72 * (size_t)c->nel, c->stream), "alloc") ||
+      !ok(c, cudaMallocAsync((void**)&d_out, sizeof(double) * 9 * (size_t)c->nnd, c->stream), "alloc"))
     return TG_ERR_OOM;
+  h.resize((size_t)c->nnd * 9);
   int s = launch_nodal_stress(c, d_ip, d_out);
   if (!s) s = check_status(c);
-  if (!s && !copy_sync(c, out, d_out, sizeof(double) * 6 * (size_t)c->nnd, cudaMemcpyDeviceToHost, "stress"))
+  if (!s && !copy_sync(c, h.data(), d_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, "output"))
     s = TG_ERR_CUDA;
   cudaFreeAsync(d_ip, c->stream);
   cudaFreeAsync(d_out, c->stream);
   if (!ok(c, cudaStreamSynchronize(c->stream), "sync") && !s) s = TG_ERR_CUDA;
+  return s;
+}
+}  // namespace
+
+int tg_nodal_stress(tg_context* c, double* out) {
+  if (!c || !out || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  std::vector<double> h;
+  const int s = nodal_output(c, h);
+  if (!s)
+    for (int n = 0; n < c->nnd; ++n)
+      for (int k = 0; k < 6; ++k) out[(size_t)n * 6 + k] = h[(size_t)n * 9 + k];
+  return s;
+}
+
+int tg_nodal_material_output(tg_context* c, double* out) {
+  if (!c || !out || c->nnd <= 0) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  std::vector<double> h;
+  const int s = nodal_output(c, h);
+  if (!s)
+    for (int n = 0; n < c->nnd; ++n)
+      for (int k = 0; k < 3; ++k) out[(size_t)n * 3 + k] = h[(size_t)n * 9 + 6 + k];
   return s;
 }
 

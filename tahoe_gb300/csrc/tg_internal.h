@@ -262,8 +262,9 @@ size_t pcg_scratch_bytes(const Context* c);
 int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
                       int max_it, int precond, int* iters, double* rel_res);
 int launch_residual_nocommit(Context* c);
-// output pass (no history written): point stresses into d_ip_sig (nel*8*6),
-// extrapolated and averaged nodal stresses into d_out (nnd*6)
+// output pass (no history written): per point the Cauchy stress and the J2
+// material output (alpha, von Mises, pressure) into d_ip_sig (nel*8*9), the
+// extrapolated, element-averaged nodal values into d_out (nnd*9)
 int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out);
 // rhs = R - K v on active rows (v nodal, K the last tangent), FP64
 // accumulation; with zero_base, rhs = -K v

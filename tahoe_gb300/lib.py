@@ -83,6 +83,7 @@ _SIGS = {
     "tg_tangent_config": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_element_strain_displacement": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_nodal_stress": (ctypes.c_int, [_vp, _dp]),
+    "tg_nodal_material_output": (ctypes.c_int, [_vp, _dp]),
     "tg_spmv_release": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
@@ -288,6 +289,11 @@ class Context:
         out = np.zeros(self.nnd * 6)
         self._chk(self.L.tg_nodal_stress(self.h, _d(out)), "tg_nodal_stress")
         return out.reshape(-1, 6)
+
+    def nodal_material_output(self):
+        out = np.zeros(self.nnd * 3)
+        self._chk(self.L.tg_nodal_material_output(self.h, _d(out)), "tg_nodal_material_output")
+        return out.reshape(-1, 3)
 
     def active_set(self):
         f = np.zeros(self.nel * 8, dtype=np.int8)

@@ -45,10 +45,11 @@ def test_golden_decks_on_gpu(name):
     fx = load_fixture(name)
     m = model_from_fixture(fx)
     sv = fx["solver"]
-    stress = {}
+    stress, matout = {}, {}
 
     def on_step(step, ctx):
         stress[step - 1] = ctx.nodal_stress()
+        matout[step - 1] = ctx.nodal_material_output()
 
     hist, reps = m.run(fx["nsteps"], fx["dt"], rel_tol=sv["rel_tol"], abs_tol=sv["abs_tol"],
                        max_iterations=sv["max_its"], div_tol=sv["div_tol"], precision=lib.FP64,
@@ -59,6 +60,10 @@ def test_golden_decks_on_gpu(name):
         step = int(round(o["time"] / fx["dt"])) - 1
         ref = np.array(o["rows"])[:, 3:9]
         assert rel_err(stress[step], ref) < 1e-9, (name, step)
+        if "alpha" in o["labels"]:
+            L = o["labels"]
+            mref = np.array(o["rows"])[:, L.index("alpha"):L.index("press") + 1]
+            assert rel_err(matout[step], mref) < 1e-9, (name, step)
 
 
 @pytest.mark.parametrize("jitter", [0.0, 0.2])

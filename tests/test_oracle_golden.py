@@ -36,6 +36,22 @@ def test_oracle_nodal_stress_matches_golden(name):
         assert rel_err(sh[step], ref) < 1e-11, (name, step)
 
 
+def test_oracle_j2_material_output_matches_golden():
+    """alpha, von Mises stress and pressure (J2SSKStV::ComputeOutput),
+    extrapolated and averaged, against the J2 deck's .run columns."""
+    fx = load_fixture("mat08_j2_cube")
+    m = model_from_fixture(fx)
+    sv = fx["solver"]
+    status, uh, its, cuts, sh = m.run_cuts(fx["nsteps"], fx["dt"], sv["rel_tol"], sv["abs_tol"], sv["max_its"],
+                                           sv["div_tol"], 0, want_stress=True)
+    assert status == 0
+    for o in fx["outputs"]:
+        step = int(round(o["time"] / fx["dt"])) - 1
+        L = o["labels"]
+        ref = np.array(o["rows"])[:, L.index("alpha"):L.index("press") + 1]
+        assert rel_err(m.material_output_hist[step], ref) < 1e-11, step
+
+
 def test_oracle_j2_alpha_matches_golden():
     fx = load_fixture("mat08_j2_cube")
     m = model_from_fixture(fx)
