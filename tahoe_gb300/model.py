@@ -85,11 +85,21 @@ class SolidModel:
         self.ctx = None
 
     # boundary conditions -------------------------------------------------
-    def set_schedule(self, pts):
-        self.schedule = [tuple(p) for p in pts]
+    def set_schedule(self, pts, number=1):
+        """Schedule function `number` (1-based, as the deck's schedule ids);
+        schedule 1 also scales the external forces and tractions."""
+        if not hasattr(self, "schedules"):
+            self.schedules = {}
+        self.schedules[int(number)] = [tuple(p) for p in pts]
+        if int(number) == 1:
+            self.schedule = self.schedules[1]
 
     def add_kbc(self, node, dof, value=0.0, scheduled=False):
-        self.kbc.append((int(node), int(dof), float(value), bool(scheduled)))
+        """Prescribed dof: fixed at 0 (scheduled False), or value times
+        schedule 1 (True) or schedule n (an int n >= 1) -- KBC_CardT's fixed /
+        prescribed codes."""
+        n = int(scheduled) if not isinstance(scheduled, bool) else (1 if scheduled else 0)
+        self.kbc.append((int(node), int(dof), float(value), n))
 
     def add_force(self, node, dof, value):
         self.forces.append((int(node), int(dof), float(value)))
@@ -126,7 +136,7 @@ class SolidModel:
         self.eqnos = eq
         self._kbc_idx = np.array([n * 3 + d for (n, d, _, _) in self.kbc], dtype=np.int32)
         self._kbc_val = np.array([v for (_, _, v, _) in self.kbc])
-        self._kbc_sch = np.array([s for (_, _, _, s) in self.kbc], dtype=bool)
+        self._kbc_sch = np.array([s for (_, _, _, s) in self.kbc], dtype=np.int64)
         return c
 
     def apply_step(self, t, predictor=None):
@@ -135,7 +145,9 @@ class SolidModel:
         is applied through tg_predict_prescribed instead of directly."""
         sc = schedule_value(self.schedule, t)
         self.ctx.set_load_factor(sc)
-        vals = np.where(self._kbc_sch, sc * self._kbc_val, 0.0)
+        scheds = getattr(self, "schedules", {1: self.schedule})
+        factors = np.array([0.0] + [schedule_value(scheds.get(n), t) for n in range(1, max(scheds, default=1) + 1)])
+        vals = np.where(self._kbc_sch > 0, factors[np.minimum(self._kbc_sch, len(factors) - 1)] * self._kbc_val, 0.0)
         if predictor is not None:
             prec, pc, tol = predictor
             return self.ctx.predict_prescribed(self._kbc_idx, vals, precision=prec, precond=pc, lin_rel_tol=tol)
@@ -201,6 +213,7 @@ class SolidModel:
                 status = "decrease"
                 self.step_cuts += 1
                 continue
+            self.current_time = t
             if on_step is not None:
                 on_step(step_num, c)
             c.close_step()

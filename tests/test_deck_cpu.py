@@ -1,0 +1,51 @@
+"""Deck glue on the host (no GPU): the TahoeII geometry and XML deck readers
+on the repository's own test decks, the model they describe, and the .run
+writer read back by the .run reader."""
+import os
+
+import numpy as np
+
+from tahoe_gb300 import deck as dk
+from tahoe_gb300.meshgen import BoxMesh
+
+DECKS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks")
+
+
+def test_geometry_reader():
+    X, conn, nodesets, sidesets = dk.read_geom(os.path.join(DECKS, "cube8.geom"))
+    m = BoxMesh(2, 2, 2)
+    assert np.allclose(X, m.X) and np.array_equal(np.asarray(conn), m.conn)
+    assert sorted(nodesets[1]) == sorted(m.face_nodes(2, 0).tolist())
+    assert sorted(nodesets[2]) == sorted(m.face_nodes(2, 1).tolist())
+    el, fc = m.face_facets(0, 1)
+    assert sorted(sidesets[1]) == sorted(zip(el.tolist(), fc.tolist()))
+
+
+def test_deck_to_model():
+    d = dk.Deck(os.path.join(DECKS, "cube8_j2.xml"))
+    assert d.formulation == "small_strain" and d.material["kind"] == "ss_j2"
+    assert d.nsteps == 3 and d.dt == 1.0 and d.max_step_cuts == 3
+    m = d.model()
+    # 9 bottom nodes x 3 fixed dofs + 9 top nodes prescribed in z (schedule 1)
+    assert len(m.kbc) == 36
+    assert sum(1 for k in m.kbc if k[3] == 1) == 9 and all(k[2] == -0.006 for k in m.kbc if k[3] == 1)
+    eq = m.equations()
+    assert (eq > 0).sum() == 27 * 3 - 36
+    t = dk.Deck(os.path.join(DECKS, "cube8_tl_traction.xml"))
+    mt = t.model()
+    assert mt.formulation == 1 and len(mt.forces) == 9 and len(mt.tractions) == 4
+
+
+def test_run_file_round_trip(tmp_path):
+    d = dk.Deck(os.path.join(DECKS, "cube8_j2.xml"))
+    rng = np.random.default_rng(0)
+    res = [(float(k + 1), rng.standard_normal((27, 3)), rng.standard_normal((27, 6)), rng.standard_normal((27, 3)))
+           for k in range(2)]
+    path = str(tmp_path / "out.run")
+    dk.write_run(path, d, res)
+    back = dk.read_run(path)
+    assert len(back) == 2
+    for (t, u, s, mo), b in zip(res, back):
+        assert b["time"] == t
+        assert b["labels"] == ["D_X", "D_Y", "D_Z", "s11", "s22", "s33", "s23", "s13", "s12", "alpha", "VM", "press"]
+        assert np.allclose(np.array(b["rows"]), np.hstack([u, s, mo]), rtol=1e-11, atol=1e-300)
