@@ -228,6 +228,15 @@ int tg_newton_iteration(tg_context* ctx, const tg_newton_params* params, double*
 int tg_predict_prescribed(tg_context* ctx, int n, const int* dof_index, const double* values,
                           const tg_newton_params* params, int* pcg_iterations);
 
+/* Restart image of the state a step sequence resumes from (the role of
+ * ElementBaseT/ContinuumElementT::WriteRestart/ReadRestart,
+ * ElementBaseT.cpp:299-345, and the nodal field's restart data): the
+ * displacements and every J2 history array, in a versioned host buffer of
+ * tg_state_size bytes.  Loading checks the version and that the mesh sizes
+ * and materials match; the caller restores time and load factor. */
+int tg_state_size(tg_context* ctx, long long* bytes);
+int tg_state_save(tg_context* ctx, void* buffer, long long bytes);
+int tg_state_load(tg_context* ctx, const void* buffer, long long bytes);
 /* Device snapshot of the displacement and residual, and its restore: the
  * last-converged-state reset of FEManagerT::ResetStep (FEManagerT.cpp:247-262)
  * used for step cuts; also lets a caller repeat an identical iteration. */

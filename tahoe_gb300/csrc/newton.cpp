@@ -279,6 +279,95 @@ int tg_nodal_material_output(tg_context* c, double* out) {
   return s;
 }
 
+// Restart snapshot: a versioned host image of the state needed to resume a
+// step sequence bitwise -- displacements and the J2 history arrays (flags,
+// allocation, alpha, dgamma, |s|, plastic strain, unit normal).
+namespace {
+struct StateHeader {
+  char magic[8];  // "TGSTATE"
+  int version, nnd, nel, has_j2;
+  long long bytes;
+};
+constexpr int kStateVersion = 1;
+
+struct StatePart {
+  void* dev;
+  size_t bytes;
+};
+
+std::vector<StatePart> state_parts(tg_context* c) {
+  const size_t nip = (size_t)c->nel * 8;
+  std::vector<StatePart> p = {{c->d_u, sizeof(double4_32a) * c->nnd}};
+  if (c->has_j2) {
+    p.push_back({c->d_j2_flags, nip});
+    p.push_back({c->d_j2_alloc, (size_t)c->nel});
+    p.push_back({c->d_j2_alpha, sizeof(double) * nip});
+    p.push_back({c->d_j2_dgamma, sizeof(double) * nip});
+    p.push_back({c->d_j2_norm, sizeof(double) * nip});
+    p.push_back({c->d_j2_epsp, sizeof(double) * nip * 6});
+    p.push_back({c->d_j2_nhat, sizeof(double) * nip * 6});
+  }
+  return p;
+}
+
+long long state_bytes(tg_context* c) {
+  long long b = sizeof(StateHeader);
+  for (const StatePart& q : state_parts(c)) b += (long long)((q.bytes + 15) / 16 * 16);
+  return b;
+}
+}  // namespace
+
+int tg_state_size(tg_context* c, long long* bytes) {
+  if (!c || !bytes || c->nnd <= 0) return TG_ERR_ARG;
+  *bytes = state_bytes(c);
+  return TG_OK;
+}
+
+int tg_state_save(tg_context* c, void* buf, long long bytes) {
+  if (!c || !buf || c->nnd <= 0 || bytes < state_bytes(c)) return TG_ERR_ARG;
+  if (set_device(c)) return TG_ERR_CUDA;
+  StateHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, "TGSTATE", 8);
+  h.version = kStateVersion;
+  h.nnd = c->nnd;
+  h.nel = c->nel;
+  h.has_j2 = c->has_j2 ? 1 : 0;
+  h.bytes = state_bytes(c);
+  unsigned char* out = static_cast<unsigned char*>(buf);
+  std::memcpy(out, &h, sizeof(h));
+  size_t off = sizeof(h);
+  for (const StatePart& q : state_parts(c)) {
+    if (!ok(c, cudaMemcpyAsync(out + off, q.dev, q.bytes, cudaMemcpyDeviceToHost, c->stream), "state")) return TG_ERR_CUDA;
+    off += (q.bytes + 15) / 16 * 16;
+  }
+  return ok(c, cudaStreamSynchronize(c->stream), "sync") ? TG_OK : TG_ERR_CUDA;
+}
+
+int tg_state_load(tg_context* c, const void* buf, long long bytes) {
+  if (!c || !buf || c->nnd <= 0 || bytes < (long long)sizeof(StateHeader)) return TG_ERR_ARG;
+  StateHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, "TGSTATE", 8) != 0 || h.version != kStateVersion) {
+    c->err = "not a state image of this library version";
+    return TG_ERR_ARG;
+  }
+  if (h.nnd != c->nnd || h.nel != c->nel || h.has_j2 != (c->has_j2 ? 1 : 0) || h.bytes != state_bytes(c) ||
+      bytes < h.bytes) {
+    c->err = "state image does not match the mesh and materials of this context";
+    return TG_ERR_ARG;
+  }
+  if (set_device(c)) return TG_ERR_CUDA;
+  const unsigned char* in = static_cast<const unsigned char*>(buf);
+  size_t off = sizeof(h);
+  for (const StatePart& q : state_parts(c)) {
+    if (!ok(c, cudaMemcpyAsync(q.dev, in + off, q.bytes, cudaMemcpyHostToDevice, c->stream), "state")) return TG_ERR_CUDA;
+    off += (q.bytes + 15) / 16 * 16;
+  }
+  c->have_du = false;
+  return ok(c, cudaStreamSynchronize(c->stream), "sync") ? TG_OK : TG_ERR_CUDA;
+}
+
 int tg_get_active_set(tg_context* c, signed char* flags) {
   if (!c || !flags || c->nel <= 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;

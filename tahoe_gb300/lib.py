@@ -83,6 +83,9 @@ _SIGS = {
     "tg_tangent_config": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_element_strain_displacement": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_nodal_stress": (ctypes.c_int, [_vp, _dp]),
+    "tg_state_size": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "tg_state_save": (ctypes.c_int, [_vp, _vp, ctypes.c_longlong]),
+    "tg_state_load": (ctypes.c_int, [_vp, _vp, ctypes.c_longlong]),
     "tg_nodal_material_output": (ctypes.c_int, [_vp, _dp]),
     "tg_spmv_release": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
@@ -289,6 +292,18 @@ class Context:
         out = np.zeros(self.nnd * 6)
         self._chk(self.L.tg_nodal_stress(self.h, _d(out)), "tg_nodal_stress")
         return out.reshape(-1, 6)
+
+    def state_save(self):
+        """Restart image of the device state (bytes)."""
+        n = ctypes.c_longlong(0)
+        self._chk(self.L.tg_state_size(self.h, ctypes.byref(n)), "tg_state_size")
+        buf = np.zeros(n.value, dtype=np.uint8)
+        self._chk(self.L.tg_state_save(self.h, buf.ctypes.data_as(_vp), n.value), "tg_state_save")
+        return buf.tobytes()
+
+    def state_load(self, image):
+        buf = np.frombuffer(image, dtype=np.uint8).copy()
+        self._chk(self.L.tg_state_load(self.h, buf.ctypes.data_as(_vp), len(buf)), "tg_state_load")
 
     def nodal_material_output(self):
         out = np.zeros(self.nnd * 3)

@@ -157,7 +157,7 @@ class SolidModel:
 
     def run(self, nsteps, dt, rel_tol=1e-12, abs_tol=1e-10, max_iterations=10, div_tol=10.0, precision=lib.FP64,
             precond=lib.PRECOND_JACOBI, lin_rel_tol=1e-12, lin_max_it=20000, on_step=None, predictor=False,
-            max_step_cuts=0, quick_solve_iter=6, quick_solve_count=3):
+            max_step_cuts=0, quick_solve_iter=6, quick_solve_count=3, first_step=1):
         """The load-step sequence of TimeManagerT around NLSolver (device
         Newton per step).  A step whose Newton iteration fails is reset to the
         last converged state (FEManagerT::ResetStep: displacements from the
@@ -171,13 +171,14 @@ class SolidModel:
         TimeManagerT.cpp:140-150).  Returns the displacements at the original
         step times k*dt and, per original step, the Newton reports of its
         converged sub-steps; self.step_cuts counts the cuts made.  Raises
-        TahoeError when a step fails with no cut left."""
+        TahoeError when a step fails with no cut left.  first_step > 1 resumes
+        a sequence (e.g. from a restart image) at step first_step of nsteps."""
         if self.ctx is None:
             self.setup()
         c = self.ctx
         hist, reports = [], []
-        step_num, num_steps, cuts, status, quick = 0, nsteps, 0, "same", 0
-        tstep, t = float(dt), 0.0
+        step_num, num_steps, cuts, status, quick = first_step - 1, nsteps, 0, "same", 0
+        tstep, t = float(dt), (first_step - 1) * float(dt)
         self.step_cuts = 0
         sub = []
         while step_num < num_steps:
