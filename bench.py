@@ -157,10 +157,10 @@ def setup_c2(device, precision):
     return mesh, model, ctx
 
 
-def one_iteration(ctx, precision, lin_tol):
+def one_iteration(ctx, precision, lin_tol, precond=0):
     ctx.rollback()
     ctx.set_iteration(-1)
-    return ctx.newton_iteration(precision=precision, lin_rel_tol=lin_tol, lin_max_it=20000)
+    return ctx.newton_iteration(precision=precision, precond=precond, lin_rel_tol=lin_tol, lin_max_it=20000)
 
 
 def cpu_baseline(mesh, gpu_pcg_iters, threads, n_pcg=10):
@@ -188,6 +188,7 @@ def run_ours(args):
     ws, rank, local = dist_init()
     from tahoe_gb300 import lib, workloads
     prec = lib.MIXED if args.precision == "mixed" else lib.FP64
+    precond = lib.PRECOND_BLOCK_JACOBI if args.precond == "block" else lib.PRECOND_JACOBI
     mesh, model, ctx = setup_c2(local, prec)
     tuning = None
     if not args.no_tune:
@@ -201,7 +202,7 @@ def run_ours(args):
     # warm-up (also captures the PCG graph)
     its_seen = []
     for _ in range(max(args.warmup, 1)):
-        nrm, its = one_iteration(ctx, prec, LIN_TOL)
+        nrm, its = one_iteration(ctx, prec, LIN_TOL, precond)
         its_seen.append(its)
 
     sampler = ClockSampler(local)
@@ -211,7 +212,7 @@ def run_ours(args):
     ctx.timer_start()
     pcg_its = []
     for _ in range(args.steps):
-        nrm, its = one_iteration(ctx, prec, LIN_TOL)
+        nrm, its = one_iteration(ctx, prec, LIN_TOL, precond)
         pcg_its.append(its)
     ms_total = ctx.timer_stop()
     launches = ctx.launches - launches0
@@ -230,7 +231,7 @@ def run_ours(args):
         ctx.set_u(u0)
         ctx.set_iteration(-1)
         ctx.residual(want_vector=False)
-        ctx.newton_iteration(precision=prec, lin_rel_tol=LIN_TOL)
+        ctx.newton_iteration(precision=prec, precond=precond, lin_rel_tol=LIN_TOL)
         u_out = ctx.get_u()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     e2e_ms = max_over_ranks(ws, e2e_ms)
@@ -262,7 +263,7 @@ def run_ours(args):
             ctx.rollback()
             ctx.timer_start()
             rc, rep = ctx.newton(rel_tol=NEWTON_TOL, abs_tol=0.0, div_tol=10.0, max_iterations=20, precision=p,
-                                 lin_rel_tol=LIN_TOL, lin_max_it=20000, check=False)
+                                 precond=precond, lin_rel_tol=LIN_TOL, lin_max_it=20000, check=False)
             ms = ctx.timer_stop()
             res[name] = (ctx.get_u().copy(), rep, ms, rc)
         uf, um = res["fp64"][0], res["mixed"][0]
@@ -288,7 +289,8 @@ def run_ours(args):
         "dtype": "fp32 tangent+PCG, fp64 residual/dots" if prec == lib.MIXED else "fp64",
         "data": "synthetic (seeded 64^3 jittered hex8 block)",
         "config": {"workload": "C2: 64^3 hex8 total-Lagrangian Simo neo-Hookean (mu=1, kappa=10), jitter 0.2h seed 0, "
-                               "load step 1/10, one Newton iteration (inner Jacobi-PCG rel tol %g)" % LIN_TOL,
+                               "load step 1/10, one Newton iteration (inner %s-PCG rel tol %g)"
+                               % ("block-Jacobi" if args.precond == "block" else "Jacobi", LIN_TOL),
                    "nel": mesh.nel, "nodes": nnd, "dofs": nnd * 3, "equations": ctx.neq, "block_nnz": nnzb,
                    "scalar_nnz": int(nnzb * 9), "parallelism": "replicas x%d" % ws,
                    "l2": "inputs larger than L2 (block CSR %.0f MB)" % (nnzb * (9 * s_val + 4) / 1e6)},
@@ -615,7 +617,8 @@ def main():
     ap.add_argument("--plain-requests", type=int, default=200, help="C5 requests for the one-at-a-time arm")
     ap.add_argument("--lanes", type=int, default=4)
     ap.add_argument("--max-batch", type=int, default=1024)
-    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "block"])
+    ap.add_argument("--precond", default="block", choices=["jacobi", "block"],
+                    help="PCG preconditioner: block-Jacobi (3x3 node blocks) or Jacobi")
     args = ap.parse_args()
     if args.workload == "c4" and args.impl == "ours":
         run_c4(args)

@@ -135,25 +135,26 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
     T a0 = T(0), a1 = T(0), a2 = T(0);
     const int e0 = live ? rp[li] : 0;
     const int e1 = live ? rp[li + 1] : 0;
-    // the first 4 blocks of this lane (a hex8 row has at most 27): all
+    // the first 3 blocks of this lane (24 of a hex8 row's at most 27): all
     // column indices, then all neighbour gathers, then the arithmetic, so
-    // the L2 round trips of one lane overlap instead of chaining
+    // the L2 round trips of one lane overlap instead of chaining (depth 3
+    // keeps the kernel at 64 registers: 4 CTAs per SM)
     {
-      int Jk[4];
-      V zk[4], pk[4];
+      int Jk[3];
+      V zk[3], pk[3];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 3; ++u) {
         const int j = e0 + sub + 8 * u;
         Jk[u] = j < e1 ? cl[j] : -1;
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < 3; ++u)
         if (Jk[u] >= 0) {
           zk[u] = z[Jk[u]];
           pk[u] = pold[Jk[u]];
         }
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < 3; ++u)
         if (Jk[u] >= 0) {
           const T* vv = pl + e0 + sub + 8 * u;
           const T x = zk[u].x + beta * pk[u].x, y = zk[u].y + beta * pk[u].y, w = zk[u].z + beta * pk[u].z;
@@ -162,7 +163,7 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
           a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
         }
     }
-    for (int j = e0 + sub + 32; j < e1; j += 8) {
+    for (int j = e0 + sub + 24; j < e1; j += 8) {
       const int J = cl[j];
       const T* vv = pl + j;
       const V zj = z[J], pj = pold[J];
@@ -197,7 +198,7 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
 // wait is bounded; a timeout sets an error flag, drains the copies in flight
 // (bounded) and marks the solve broken down.
 template <typename T, int NST>
-__global__ void __launch_bounds__(256) pcg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off,
                                                        const unsigned char* __restrict__ blob, int cap,
                                                        const typename Vec4<T>::type* __restrict__ z,
                                                        const typename Vec4<T>::type* __restrict__ pold,

@@ -177,7 +177,7 @@ class ResidentRVEs:
         self.ctx.compose([self.template_id(n) for n in ns])
 
     def solve(self, ns, Fs, precision=lib.MIXED, rel_tol=1e-8, lin_rel_tol=1e-4, max_iterations=20,
-              precond=lib.PRECOND_JACOBI):
+              precond=lib.PRECOND_BLOCK_JACOBI):
         """Composes the batch, runs the affine predictor from the undeformed
         state and Newton to rel_tol per RVE; same returns as RVEBatch.solve."""
         c = self.ctx
