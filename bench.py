@@ -67,6 +67,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def spmv_roofline(ctx, precision):
+    """Event-timed streamed SpMV on the context's current tangent against the
+    measured copy bandwidth (algorithmic bytes as for configuration 2)."""
+    from tahoe_gb300 import lib, workloads
+    ms = ctx.time_kernel(0, 20)
+    s_val = 4 if precision == lib.MIXED else 8
+    b = workloads.spmv_bytes(ctx.block_nnz, ctx.nnd, s_val)
+    peak, kind = peaks()
+    ach = b / (ms * 1e-3) / 1e9
+    return {"kernel": "pcg_spmv_kernel", "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": int(b), "ms_per_launch": round(ms, 4)}
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -403,6 +416,8 @@ def run_c4(args):
         Cm, cits = c.macro_tangent(np.ones(len(ns)), precision=prec, precond=precond, lin_rel_tol=1e-7)
         out[name].update(C=Cm, ms_macro=c.timer_stop(), macro_pcg=cits)
     b = argparse.Namespace(nel=c.nel, nnd=c.nnd)
+    c.tangent(lib.MIXED)
+    roof = spmv_roofline(c, lib.MIXED)
     Pm, Pf = out["mixed"]["P"], out["fp64"]["P"]
     err = float(np.abs(Pm - Pf).max() / np.abs(Pf).max())
     per_rve = np.abs(Pm - Pf).reshape(len(ns), -1).max(axis=1) / np.abs(Pf).reshape(len(ns), -1).max(axis=1)
@@ -429,6 +444,7 @@ def run_c4(args):
                                                      np.abs(out["fp64"]["C"]).max()),
         "P_rel_err_mixed_vs_fp64_worst_rve": float(per_rve.max()),
         "template_setup_s": round(t_setup, 3),
+        "roofline": roof,
         "precond": args.precond,
     }
     if not args.no_cpu:
@@ -483,6 +499,12 @@ def run_c5(args):
             codes, counts = np.unique(res["status"][res["status"] != 0], return_counts=True)
             sweep[-1]["failed"] = {int(k): int(v) for k, v in zip(codes, counts)}
             sweep[-1]["errors"] = [e[2][:200] for e in res["errors"][:3]]
+    roof = None
+    lane_ctx = srv.lane_states[0].get("ctx")
+    if lane_ctx is not None and lane_ctx.nnd > 0:
+        lane_ctx.tangent(lib.MIXED)
+        roof = spmv_roofline(lane_ctx, lib.MIXED)
+        roof["on"] = "lane 0's last batch (%d nodes)" % lane_ctx.nnd
     srv.close()
     plain.close()
     top = max(sweep, key=lambda r: r["solves_per_s"])
@@ -495,6 +517,7 @@ def run_c5(args):
                                "mixed precision, Newton to 1e-8 per RVE" % (args.lanes, args.max_batch),
                    "hbm_budget_bytes": int(budget)},
         "sweep": sweep,
+        "roofline": roof,
     }
     print(json.dumps(line))
 
@@ -525,6 +548,8 @@ def run_c3(args):
                                max_step_cuts=args.max_step_cuts, quick_solve_iter=args.quick_solve_iter)
         total_ms = c.timer_stop()
         rec["total_ms"] = total_ms
+        c.tangent(prec)
+        rec["roofline"] = spmv_roofline(c, prec)
         rec["cuts"] = model.step_cuts
         for r in reps:
             rs = r if isinstance(r, list) else [r]
@@ -565,6 +590,7 @@ def run_c3(args):
         "step_cuts": {k: v["cuts"] for k, v in out.items()},
         "newton_per_step": {k: v["newton"] for k, v in out.items()},
         "flags_final": {k: v["flags_final"] for k, v in out.items()},
+        "roofline": out["mixed"]["roofline"],
         "yielding_set_mismatch_final": f["mismatch"][0],
         "active_set_bit_exact": f["mismatch"][0] == 0,
         "allocated_points_mismatch_final": f["alloc_mismatch"],
