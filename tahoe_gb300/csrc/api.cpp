@@ -154,6 +154,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->d_x = c->d_r = c->d_z = c->d_p = c->d_p1 = c->d_q = nullptr;
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
+  c->d_geo = nullptr;
   c->d_blob32 = c->d_blob64 = nullptr;
   c->nseg = 0;
   c->d_seg_node = c->d_seg_elem = nullptr;

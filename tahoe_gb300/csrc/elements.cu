@@ -261,7 +261,8 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
                                                        int nel, const double4_32a* __restrict__ u, MatTable mt,
                                                        J2View j2, int iteration, int commit_state,
                                                        double4_32a* __restrict__ fint, int* status,
-                                                       double* __restrict__ ip_sig) {
+                                                       double* __restrict__ ip_sig,
+                                                       const double* __restrict__ geo) {
   __shared__ double sX[kResElems][8][3];
   __shared__ double sU[kResElems][8][3];
   const int tid = threadIdx.x;
@@ -270,9 +271,11 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   const bool valid = e < nel;
   if (valid) {
     const int n = conn[e * 8 + ip];
-    sX[le][ip][0] = X[n];
-    sX[le][ip][1] = X[nnd + n];
-    sX[le][ip][2] = X[2 * nnd + n];
+    if (!geo) {
+      sX[le][ip][0] = X[n];
+      sX[le][ip][1] = X[nnd + n];
+      sX[le][ip][2] = X[2 * nnd + n];
+    }
     const double4_32a un = u[n];
     sU[le][ip][0] = un.x;
     sU[le][ip][1] = un.y;
@@ -293,7 +296,17 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   double g[3][8];
   double wdet = 0.0;
   if (valid) {
-    wdet = point_gradients<double>(sX[le], ip, g);  // weight 1 (HexahedronT.cpp:1545)
+    if (geo) {
+      // reference-configuration gradients and w det J, formed once per mesh
+      const long long nip = (long long)nel * 8, k = (long long)e * 8 + ip;
+#pragma unroll
+      for (int l = 0; l < 3; ++l)
+#pragma unroll
+        for (int a = 0; a < 8; ++a) g[l][a] = geo[(l * 8 + a) * nip + k];
+      wdet = geo[24 * nip + k];
+    } else {
+      wdet = point_gradients<double>(sX[le], ip, g);  // weight 1 (HexahedronT.cpp:1545)
+    }
     if (!(wdet > 0.0)) bad = true;
   }
   // B-bar: element-mean shape-function gradients (SmallStrainT::SetMeanGradient,
@@ -802,11 +815,55 @@ J2View j2view(Context* c) {
   return v;
 }
 
+// Reference-configuration shape-function gradients and w det J of every
+// point (the element geometry does not change over a mesh's life: the
+// residual reads them instead of re-forming Jacobians on the FP64 pipe).
+__global__ void geometry_kernel(const double* __restrict__ X, int nnd, const int* __restrict__ conn, int nel,
+                                double* __restrict__ geo) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nip = (long long)nel * 8;
+  if (k >= nip) return;
+  const long long e = k >> 3;
+  const int ip = (int)(k & 7);
+  double Xe[8][3];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int n = conn[e * 8 + a];
+    Xe[a][0] = X[n];
+    Xe[a][1] = X[nnd + n];
+    Xe[a][2] = X[2 * nnd + n];
+  }
+  double g[3][8];
+  const double d = point_gradients<double>(Xe, ip, g);
+#pragma unroll
+  for (int l = 0; l < 3; ++l)
+#pragma unroll
+    for (int a = 0; a < 8; ++a) geo[(l * 8 + a) * nip + k] = g[l][a];
+  geo[24 * nip + k] = d;
+}
+
 int residual_impl(Context* c, int commit_state, double* d_ip_sig = nullptr) {
+  if (!c->d_geo) {
+    // formed on first use after a mesh change; without room for it the
+    // kernel forms the gradients itself (bitwise the same values)
+    const size_t n = (size_t)c->nel * 8 * 25;
+    double* g = nullptr;
+    if (cudaMallocAsync((void**)&g, n * sizeof(double), c->stream) == cudaSuccess &&
+        cudaStreamSynchronize(c->stream) == cudaSuccess) {
+      c->allocations.push_back(g);
+      const long long nip = (long long)c->nel * 8;
+      geometry_kernel<<<(unsigned)((nip + 255) / 256), 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->nel, g);
+      c->launches++;
+      if (!ok(c, cudaGetLastError(), "geometry_kernel")) return TG_ERR_CUDA;
+      c->d_geo = g;
+    } else {
+      cudaGetLastError();
+    }
+  }
   const int grid = (c->nel + kResElems - 1) / kResElems;
   residual_kernel<<<grid, 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats,
                                                j2view(c), c->iteration, commit_state, c->d_fint, c->d_status,
-                                               d_ip_sig);
+                                               d_ip_sig, c->d_geo);
   c->launches++;
   return ok(c, cudaGetLastError(), "residual_kernel") ? TG_OK : TG_ERR_CUDA;
 }

@@ -121,6 +121,7 @@ struct Context {
   std::vector<int> h_tile_row;
   float* d_minv32 = nullptr;    // 18*nnd: Jacobi then block-Jacobi
   double* d_minv64 = nullptr;
+  double* d_geo = nullptr;      // 25 planes over nel*8 points: dN/dX (3x8), w det J (residual)
   float* d_Ke32 = nullptr;      // nel*324
   double* d_Ke64 = nullptr;
   int tangent_precision = -1;   // precision of the last tangent
