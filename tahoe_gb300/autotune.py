@@ -92,13 +92,20 @@ class Tuner:
                 try:
                     ctx.spmv_config(t, s)
                     ctx.tangent(precision)  # assemble into the new tile layout
-                except lib.TahoeError:
+                except lib.TahoeError as e:
+                    if e.code != -8:
+                        raise
                     for r in self.releases:
                         spmv[(t, s, r)] = None  # ring does not fit on an SM
                     continue
                 for r in self.releases:
                     ctx.spmv_release(r)
-                    spmv[(t, s, r)] = timer(ctx, KERNEL_SPMV, self.reps)
+                    try:
+                        spmv[(t, s, r)] = timer(ctx, KERNEL_SPMV, self.reps)
+                    except lib.TahoeError as e:
+                        if e.code != -8:  # only "does not fit" is a skipped candidate
+                            raise
+                        spmv[(t, s, r)] = None
         (tb, st, rl), spmv_ms = pick(spmv)
         ctx.spmv_config(tb, st)
         ctx.spmv_release(rl)

@@ -522,7 +522,10 @@ template <typename T>
 int capture_chunk(Context* c, const T* minv) {
   using V = typename Vec4<T>::type;
   Grids g = grids(c);
-  if (spmv_config<T>(c, g)) return TG_ERR_CUDA;
+  {
+    const int sc = spmv_config<T>(c, g);
+    if (sc) return sc;
+  }
   cudaGraph_t graph;
   if (!ok(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return TG_ERR_CUDA;
   static_assert(kChunk % 2 == 0, "p buffers alternate within a chunk");
@@ -716,7 +719,10 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
   if (s) return s;
   const T* minv = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
   Grids g = grids(c);
-  if (spmv_config<T>(c, g)) return TG_ERR_CUDA;
+  {
+    const int sc = spmv_config<T>(c, g);
+    if (sc) return sc;
+  }
   pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, c->d_R, c->d_mask, minv, c->d_partials, c->d_pcg);
   c->launches++;
   pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, c->d_R, c->d_mask, minv, (V*)c->d_x, (V*)c->d_r,

@@ -15,6 +15,7 @@ class FakeCtx:
     def spmv_config(self, t, s):
         if t * s > 3000:
             raise lib.TahoeError(-8, "tg_spmv_config", "does not fit")
+        self.last = (t, s)
         self.cfg["tile_blocks"], self.cfg["stages"] = t, s
         self.formed = False  # a new tile layout drops the assembled tangent
 
@@ -32,6 +33,9 @@ class FakeCtx:
 def fake_timer(ctx, which, reps):
     assert getattr(ctx, "formed", False), "kernel timed without a formed tangent"
     c = ctx.cfg
+    if which == autotune.KERNEL_SPMV and c["tile_blocks"] == 1024 and c["stages"] == 2 and c["release"] == 1:
+        # a ring that fits the configuration call but not the launch
+        raise lib.TahoeError(-8, "tg_time_kernel", "does not fit")
     if which == autotune.KERNEL_SPMV:
         return abs(c["tile_blocks"] - 768) / 100.0 + (0.5 if c["stages"] == 3 else 0.0) + 1.0 - 0.1 * c["release"]
     return {2: 3.0, 4: 1.5, 8: 2.0}[c["tangent_epb"]]
@@ -47,6 +51,7 @@ def test_picks_fastest_and_caches(tmp_path):
     assert ctx.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1}
     # 1024x3 and 1536x2/3 do not fit and are skipped, not chosen
     assert out["spmv_sweep"]["1536x2r0"] is None and out["spmv_sweep"]["1024x3r1"] is None
+    assert out["spmv_sweep"]["1024x2r1"] is None and out["spmv_sweep"]["1024x2r0"] is not None
     with open(path) as f:
         table = json.load(f)
     assert len(table) == 1
