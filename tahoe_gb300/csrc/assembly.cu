@@ -7,12 +7,15 @@
 // issues unit-stride stores and the product streams the matrix sequentially.  Every block gathers
 // its element contributions through the destination-sorted map built on the
 // host (ascending element order), so the sum order is fixed and the result is
-// bitwise repeatable.  Rows of prescribed dofs are zeroed; restricted to the
+// bitwise repeatable.  Element blocks are stored as three 16-byte (FP32) or
+// 32-byte (FP64) aligned rows, so a contribution is three vector loads.  Rows of prescribed dofs are zeroed; restricted to the
 // active rows and columns the values are the reference's "active equations
 // only" assembly (MSRMatrixT::Assemble, MSRMatrixT.cpp:96-143).  The diagonal block's (block-)Jacobi inverse is
 // produced in the same pass (DiagonalMatrixT, DiagonalMatrixT.cpp:91,313):
 // minv[0 .. 9*nnd) holds the Jacobi inverse, minv[9*nnd .. 18*nnd) the 3x3
 // block-Jacobi inverse, so the solve can pick either.
+#include <type_traits>
+
 #include "tg_internal.h"
 
 namespace tg {
@@ -29,6 +32,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
                                                        const uint8_t* __restrict__ mask, unsigned char* __restrict__ blob,
                                                        const long long* __restrict__ blob_off,
                                                        const int* __restrict__ row_tile, T* __restrict__ minv) {
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double4_32a>::type;
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nnd; I += warps) {
@@ -48,16 +52,19 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
       for (int c = cptr[j]; c < c1; ++c) {
         const int code = contrib[c];
         const int e = code >> 6, a = (code >> 3) & 7, b = code & 7;
+        // the element block's three padded rows: one aligned vector load each
+        const V4* src = reinterpret_cast<const V4*>(
+            Ke + ((long long)e * kSlots + (a <= b ? upper_slot(a, b) : upper_slot(b, a))) * kKeBlock);
+        const V4 k0 = src[0], k1 = src[1], k2 = src[2];
+        const T m[9] = {k0.x, k0.y, k0.z, k1.x, k1.y, k1.z, k2.x, k2.y, k2.z};
         if (a <= b) {
-          const T* src = Ke + ((long long)e * kSlots + upper_slot(a, b)) * kKeBlock;
 #pragma unroll
-          for (int k = 0; k < 9; ++k) acc[k] += src[k];
+          for (int k = 0; k < 9; ++k) acc[k] += m[k];
         } else {
-          const T* src = Ke + ((long long)e * kSlots + upper_slot(b, a)) * kKeBlock;
 #pragma unroll
           for (int p = 0; p < 3; ++p)
 #pragma unroll
-            for (int q = 0; q < 3; ++q) acc[p * 3 + q] += src[q * 3 + p];
+            for (int q = 0; q < 3; ++q) acc[p * 3 + q] += m[q * 3 + p];
         }
       }
       const int J = col[j];
@@ -192,9 +199,18 @@ int launch_blob_structure(Context* c, int precision) {
 }
 
 int launch_assemble(Context* c, int precision) {
+  // persistent grid: every CTA resident, so the rows in flight are one
+  // contiguous window of the row order and an element block read for one
+  // row is still in L2 when the neighbouring rows read it
   const int warps_per_block = 8;
+  int per_sm = 0;
+  if (!ok(c, precision == TG_MIXED
+                 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, assemble_kernel<float>, 256, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, assemble_kernel<double>, 256, 0),
+          "occupancy"))
+    return TG_ERR_CUDA;
   int grid = (c->nnd + warps_per_block - 1) / warps_per_block;
-  grid = std::min(grid, kNumSMs * 16);
+  grid = std::max(1, std::min(grid, kNumSMs * std::max(per_sm, 1)));
   if (precision == TG_MIXED)
     assemble_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_contrib_ptr,
                                                         c->d_contrib, c->d_Ke32, c->d_mask, c->d_blob32,

@@ -21,6 +21,8 @@
 // HexahedronT.cpp:23-25,1540-1548.
 #include <cmath>
 
+#include <type_traits>
+
 #include "tg_internal.h"
 
 namespace tg {
@@ -772,9 +774,18 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
       K[8] += geo;
     }
   }
-  T* out = Ke + ((long long)e * kSlots + slot) * kKeBlock;
+  // three padded rows, one aligned vector store each
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double4_32a>::type;
+  V4* out = reinterpret_cast<V4*>(Ke + ((long long)e * kSlots + slot) * kKeBlock);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) out[k] = K[k];
+  for (int p = 0; p < 3; ++p) {
+    V4 row;
+    row.x = K[p * 3 + 0];
+    row.y = K[p * 3 + 1];
+    row.z = K[p * 3 + 2];
+    row.w = T(0);
+    out[p] = row;
+  }
 }
 
 // J2 history update / reset (J2SSC0HardeningT::Update/Reset, :204-250);
@@ -966,7 +977,7 @@ __global__ void expand_ke_kernel(int first, int count, const double* __restrict_
     const int lo = a < b ? a : b, hi = a < b ? b : a;
     const int slot = lo * 8 - lo * (lo - 1) / 2 + (hi - lo);
     const double* blkp = Ke + ((long long)e * kSlots + slot) * kKeBlock;
-    outK[(long long)k * 576 + t] = (a <= b) ? blkp[i * 3 + j] : blkp[j * 3 + i];
+    outK[(long long)k * 576 + t] = (a <= b) ? blkp[i * 4 + j] : blkp[j * 4 + i];
   }
   if (threadIdx.x < 24) {
     const int a = threadIdx.x / 3, i = threadIdx.x % 3;

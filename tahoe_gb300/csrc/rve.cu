@@ -131,13 +131,13 @@ __global__ void __launch_bounds__(256) segment_macro_kernel(int nseg, const int*
         if (a <= b) {
           const T* B = Kb + upper_slot_of(a, b) * kKeBlock;
           y0 += (double)B[0] * wb.x + (double)B[1] * wb.y + (double)B[2] * wb.z;
-          y1 += (double)B[3] * wb.x + (double)B[4] * wb.y + (double)B[5] * wb.z;
-          y2 += (double)B[6] * wb.x + (double)B[7] * wb.y + (double)B[8] * wb.z;
+          y1 += (double)B[4] * wb.x + (double)B[5] * wb.y + (double)B[6] * wb.z;
+          y2 += (double)B[8] * wb.x + (double)B[9] * wb.y + (double)B[10] * wb.z;
         } else {
           const T* B = Kb + upper_slot_of(b, a) * kKeBlock;
-          y0 += (double)B[0] * wb.x + (double)B[3] * wb.y + (double)B[6] * wb.z;
-          y1 += (double)B[1] * wb.x + (double)B[4] * wb.y + (double)B[7] * wb.z;
-          y2 += (double)B[2] * wb.x + (double)B[5] * wb.y + (double)B[8] * wb.z;
+          y0 += (double)B[0] * wb.x + (double)B[4] * wb.y + (double)B[8] * wb.z;
+          y1 += (double)B[1] * wb.x + (double)B[5] * wb.y + (double)B[9] * wb.z;
+          y2 += (double)B[2] * wb.x + (double)B[6] * wb.y + (double)B[10] * wb.z;
         }
       }
       const int n = ce[a];

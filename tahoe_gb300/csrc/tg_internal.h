@@ -15,8 +15,10 @@ namespace tg {
 constexpr int kMaxBlocks = 4;      // material blocks per element group
 constexpr int kNumSMs = 152;       // GB300
 constexpr int kSlots = 36;         // upper-triangle node-pair blocks of a hex8 element
-constexpr int kKeBlock = 9;        // 3x3 block values
-constexpr int kKeStride = kSlots * kKeBlock;  // 324 values per element
+// A staged 3x3 element block is three 4-value rows (the 4th value is zero
+// padding), so a row is one 16-byte (FP32) or 32-byte (FP64) aligned vector.
+constexpr int kKeBlock = 12;
+constexpr int kKeStride = kSlots * kKeBlock;  // 432 values per element
 
 // Device status bits (set by kernels with atomicOr, never by trapping).
 enum : int { kStatusBadJacobian = 1, kStatusNaN = 2, kStatusWaitTimeout = 4 };
@@ -122,7 +124,7 @@ struct Context {
   float* d_minv32 = nullptr;    // 18*nnd: Jacobi then block-Jacobi
   double* d_minv64 = nullptr;
   double* d_geo = nullptr;      // 25 planes over nel*8 points: dN/dX (3x8), w det J (residual)
-  float* d_Ke32 = nullptr;      // nel*324
+  float* d_Ke32 = nullptr;      // nel*432: 36 upper node-pair blocks, rows padded to 4
   double* d_Ke64 = nullptr;
   int tangent_precision = -1;   // precision of the last tangent
   int tangent_precond = -1;

@@ -39,7 +39,7 @@ def rve_bytes(n, precision=lib.MIXED):
     history), estimated."""
     s = 4 if precision == lib.MIXED else 8
     nel, nnd = n ** 3, (n + 1) ** 3
-    return nel * (324 * s + 256 + 8 * 32 + 128 + 8 * 25 * 8) + nnd * (27 * (9 * s + 8) + 10 * 16 + 6 * 4 * s + 64)
+    return nel * (432 * s + 256 + 8 * 32 + 128 + 8 * 25 * 8) + nnd * (27 * (9 * s + 8) + 10 * 16 + 6 * 4 * s + 64)
 
 
 def gpu_batch_solver(precision=lib.MIXED, rel_tol=1e-8, lin_rel_tol=1e-4):
