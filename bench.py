@@ -267,6 +267,13 @@ def run_ours(args):
     peak, peak_kind = peaks()
     achieved = bytes_spmv / (t_spmv * 1e-3) / 1e9
     elements_per_s = mesh.nel / ((t_tan + t_asm) * 1e-3)
+    # the other HBM-bound kernels of the step, same peak and byte model
+    other_rooflines = {}
+    for name, b, t in (("assemble_kernel", workloads.assembly_bytes(mesh.nel, nnzb, nnd, s_val), t_asm),
+                       ("pcg_update_kernel", workloads.update_bytes(nnd, s_val), t_upd)):
+        a = b / (t * 1e-3) / 1e9
+        other_rooflines[name] = {"bound": "hbm", "achieved": round(a, 1), "peak": peak, "unit": "GB/s",
+                                 "frac": round(a / peak, 4), "algorithmic_bytes": int(b), "ms_per_launch": round(t, 5)}
 
     # full load step to NEWTON_TOL in both forms: Newton iterations, time, agreement
     extra = {}
@@ -315,6 +322,7 @@ def run_ours(args):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "algorithmic_bytes": int(bytes_spmv), "traffic": profiled_traffic(prec == lib.MIXED),
                      "traffic_source": "ncu dram__bytes_read.sum+dram__bytes_write.sum, profiles/pcg_spmv_c2_64cubed.md"},
+        "other_rooflines": other_rooflines,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/Newton iteration", "h2d_bytes_per_step": nnd * 32,
                 "d2h_bytes_per_step": nnd * 32},
         "gpu_launches": int(launches),

@@ -151,7 +151,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->pcg_vec_precision = -1;
   c->pcg_graph_key = -1;
   c->tangent_precision = -1;
-  c->d_x = c->d_r = c->d_z = c->d_p = c->d_p1 = c->d_q = nullptr;
+  c->d_x = c->d_r = c->d_z = c->d_p = c->d_q = nullptr;
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
   c->d_geo = nullptr;

@@ -1,17 +1,18 @@
 // (Block-)Jacobi preconditioned CG on the node-block CSR matrix, sm_103a.
 //
 // Each iteration is two kernels:
-//   pcg_spmv_kernel   p_new = z + beta p_old formed on the fly at every
-//                     gathered node, q = A p_new, partial p_new.q (the
-//                     product is exact each iteration; p is double-buffered
-//                     and the buffers alternate between iterations)
-//   pcg_update_kernel x += alpha p_new; r -= alpha q; z = M^-1 r; partial
-//                     r.z, r.r
-// Both end in a last-block-done reduction of their FP64 partial sums in a
-// fixed order (bitwise repeatable, no floating-point atomics) that also
-// computes alpha / beta and the convergence flag on the device.  Iterations
-// run in chunks captured once in a CUDA graph; kernels return immediately
-// once the flag is set, and the host polls the flag between chunks.
+//   pcg_spmv_kernel   q = A p, partial p.q; the last CTA forms alpha (the
+//                     product is exact each iteration: no recurrence for A p)
+//   pcg_update_kernel x += alpha p; r -= alpha q; z = M^-1 r; partial r.z,
+//                     r.r; a grid barrier (cooperative launch); every CTA
+//                     then forms the same r.z and beta from the partials in
+//                     the same order and updates its nodes' p = z + beta p in
+//                     place, so the product gathers one vector per neighbour
+// The reductions of FP64 partial sums run in a fixed order (bitwise
+// repeatable, no floating-point atomics) and compute alpha / beta and the
+// convergence flag on the device.  Iterations run in chunks captured once in
+// a CUDA graph; kernels return immediately once the flag is set, and the host
+// polls the flag between chunks.
 //
 // Vectors are stored per node, padded to 4 lanes (float4 in the mixed form,
 // double4_32a in the plain FP64 form).  Dot products and norms accumulate in
@@ -64,8 +65,8 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
                                                        const uint8_t* __restrict__ mask, const T* __restrict__ minv,
                                                        typename Vec4<T>::type* x, typename Vec4<T>::type* r,
                                                        typename Vec4<T>::type* z, typename Vec4<T>::type* p,
-                                                       typename Vec4<T>::type* p1, typename Vec4<T>::type* q,
-                                                       double* partials, PcgScalars* sc, double tol, int max_it) {
+                                                       typename Vec4<T>::type* q, double* partials, PcgScalars* sc,
+                                                       double tol, int max_it) {
   using V = typename Vec4<T>::type;
   Acc<T> v[2];
   const double scale = sc->scale;
@@ -79,8 +80,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
     x[n] = mk<V, T>(T(0), T(0), T(0));
     r[n] = mk<V, T>(rx, ry, rz);
     z[n] = mk<V, T>(zx, zy, zz);
-    p[n] = mk<V, T>(T(0), T(0), T(0));
-    p1[n] = mk<V, T>(T(0), T(0), T(0));
+    p[n] = mk<V, T>(zx, zy, zz);  // first direction p = z
     q[n] = mk<V, T>(T(0), T(0), T(0));
     v[0].add_prod(rx, zx);
     v[0].add_prod(ry, zy);
@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
     sc->tol2 = tol * tol;
     sc->max_it = max_it;
     sc->count_a = 0u;
+    sc->bar_count = 0u;
     sc->fail = 0;
     sc->done = (tot[1] == 0.0) ? 1 : (isfinite(tot[0]) && isfinite(tot[1]) ? 0 : 2);
     if (sc->done == 2) sc->fail = 1;
@@ -108,13 +109,11 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
 
 
 // The rows of one staged tile handled by this warp: 8 lanes per row, 4 rows
-// per warp at a time, each lane over every 8th block; q = A p_new and p_new
-// written for the rows, p_new.q accumulated into v.
+// per warp at a time, each lane over every 8th block; q = A p written for the
+// rows, p.q accumulated into v.
 template <typename T>
-__device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps, T beta,
-                                               const typename Vec4<T>::type* __restrict__ z,
-                                               const typename Vec4<T>::type* __restrict__ pold,
-                                               typename Vec4<T>::type* __restrict__ pnew,
+__device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
+                                               const typename Vec4<T>::type* __restrict__ p,
                                                typename Vec4<T>::type* __restrict__ q, Acc<T>& v0) {
   using V = typename Vec4<T>::type;
   const int sub = lane & 7;
@@ -127,50 +126,41 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
   for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
     const bool live = li < nrows;
     const int I = r0 + li;
-    V zi, pi;
-    if (live && sub == 0) {
-      zi = z[I];
-      pi = pold[I];
-    }
+    V pi;
+    if (live && sub == 0) pi = p[I];
     T a0 = T(0), a1 = T(0), a2 = T(0);
     const int e0 = live ? rp[li] : 0;
     const int e1 = live ? rp[li + 1] : 0;
-    // the first 3 blocks of this lane (24 of a hex8 row's at most 27): all
-    // column indices, then all neighbour gathers, then the arithmetic, so
-    // the L2 round trips of one lane overlap instead of chaining (depth 3
-    // keeps the kernel at 64 registers: 4 CTAs per SM)
+    // the first 4 blocks of this lane (32 per row, a hex8 row has at most
+    // 27): all column indices, then all neighbour gathers, then the
+    // arithmetic, so the L2 round trips of one lane overlap instead of
+    // chaining
     {
-      int Jk[3];
-      V zk[3], pk[3];
+      int Jk[4];
+      V pk[4];
 #pragma unroll
-      for (int u = 0; u < 3; ++u) {
+      for (int u = 0; u < 4; ++u) {
         const int j = e0 + sub + 8 * u;
         Jk[u] = j < e1 ? cl[j] : -1;
       }
 #pragma unroll
-      for (int u = 0; u < 3; ++u)
-        if (Jk[u] >= 0) {
-          zk[u] = z[Jk[u]];
-          pk[u] = pold[Jk[u]];
-        }
+      for (int u = 0; u < 4; ++u)
+        if (Jk[u] >= 0) pk[u] = p[Jk[u]];
 #pragma unroll
-      for (int u = 0; u < 3; ++u)
+      for (int u = 0; u < 4; ++u)
         if (Jk[u] >= 0) {
           const T* vv = pl + e0 + sub + 8 * u;
-          const T x = zk[u].x + beta * pk[u].x, y = zk[u].y + beta * pk[u].y, w = zk[u].z + beta * pk[u].z;
-          a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
-          a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
-          a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
+          a0 += vv[0 * ps] * pk[u].x + vv[1 * ps] * pk[u].y + vv[2 * ps] * pk[u].z;
+          a1 += vv[3 * ps] * pk[u].x + vv[4 * ps] * pk[u].y + vv[5 * ps] * pk[u].z;
+          a2 += vv[6 * ps] * pk[u].x + vv[7 * ps] * pk[u].y + vv[8 * ps] * pk[u].z;
         }
     }
-    for (int j = e0 + sub + 24; j < e1; j += 8) {
-      const int J = cl[j];
+    for (int j = e0 + sub + 32; j < e1; j += 8) {
+      const V pj = p[cl[j]];
       const T* vv = pl + j;
-      const V zj = z[J], pj = pold[J];
-      const T x = zj.x + beta * pj.x, y = zj.y + beta * pj.y, w = zj.z + beta * pj.z;
-      a0 += vv[0 * ps] * x + vv[1 * ps] * y + vv[2 * ps] * w;
-      a1 += vv[3 * ps] * x + vv[4 * ps] * y + vv[5 * ps] * w;
-      a2 += vv[6 * ps] * x + vv[7 * ps] * y + vv[8 * ps] * w;
+      a0 += vv[0 * ps] * pj.x + vv[1 * ps] * pj.y + vv[2 * ps] * pj.z;
+      a1 += vv[3 * ps] * pj.x + vv[4 * ps] * pj.y + vv[5 * ps] * pj.z;
+      a2 += vv[6 * ps] * pj.x + vv[7 * ps] * pj.y + vv[8 * ps] * pj.z;
     }
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) {
@@ -179,18 +169,15 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
       a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
     if (live && sub == 0) {
-      const V pn = mk<V, T>(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z);
       q[I] = mk<V, T>(a0, a1, a2);
-      pnew[I] = pn;
-      v[0].add_prod(pn.x, a0);
-      v[0].add_prod(pn.y, a1);
-      v[0].add_prod(pn.z, a2);
+      v[0].add_prod(pi.x, a0);
+      v[0].add_prod(pi.y, a1);
+      v[0].add_prod(pi.z, a2);
     }
   }
 }
 
-// q = A p_new with p_new = z + beta p_old formed at every gathered node, on a
-// persistent grid.  Each CTA streams its row tiles through a ring of NST
+// q = A p on a persistent grid.  Each CTA streams its row tiles through a ring of NST
 // shared-memory stages: one bulk copy per tile (the tile-contiguous storage
 // makes a tile one range), completing on the stage's mbarrier, is issued
 // NST-1 tiles ahead while the CTA's warps compute the current tile: 8 lanes
@@ -200,9 +187,7 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
 template <typename T, int NST>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off,
                                                        const unsigned char* __restrict__ blob, int cap,
-                                                       const typename Vec4<T>::type* __restrict__ z,
-                                                       const typename Vec4<T>::type* __restrict__ pold,
-                                                       typename Vec4<T>::type* __restrict__ pnew,
+                                                       const typename Vec4<T>::type* __restrict__ p,
                                                        typename Vec4<T>::type* __restrict__ q, double* partials,
                                                        PcgScalars* sc, int* status) {
   using V = typename Vec4<T>::type;
@@ -210,7 +195,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
   if (((volatile PcgScalars*)sc)->done) return;
-  const T beta = T(sc->beta);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -234,7 +218,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
   unsigned phases = 0u;  // bit k: parity of stage k's next completion
   int stuck = -1;
   int it = 0;
-  const int sub = lane & 7;
   for (int t = t0; t < ntiles; ++it, t += G) {
     const int s = it % NST;
     const int tn = t + (NST - 1) * G;
@@ -251,7 +234,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
       stuck = s;
       break;
     }
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, beta, z, pold, pnew, q, v[0]);
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0]);
     __syncthreads();  // stage s is free for the copy issued next iteration
   }
   if (stuck >= 0 && threadIdx.x == 0) {
@@ -287,9 +270,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
 template <typename T, int NST>
 __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long long* __restrict__ blob_off,
                                                           const unsigned char* __restrict__ blob, int cap,
-                                                          const typename Vec4<T>::type* __restrict__ z,
-                                                          const typename Vec4<T>::type* __restrict__ pold,
-                                                          typename Vec4<T>::type* __restrict__ pnew,
+                                                          const typename Vec4<T>::type* __restrict__ p,
                                                           typename Vec4<T>::type* __restrict__ q, double* partials,
                                                           PcgScalars* sc, int* status) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -297,7 +278,6 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
   __shared__ __align__(8) uint64_t empty[NST];
   __shared__ volatile int abort_flag;
   if (((volatile PcgScalars*)sc)->done) return;
-  const T beta = T(sc->beta);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -358,7 +338,7 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
       break;
     }
     if (threadIdx.x == 0) ++seen[s];
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, beta, z, pold, pnew, q, v[0]);
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0]);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
@@ -385,52 +365,142 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
   }
 }
 
+// Launched cooperatively (every CTA resident): the grid barrier between the
+// two phases is bounded and, should it ever give up, the solve ends flagged
+// as broken down instead of waiting.  Each thread takes its nodes
+// n0, n0 + stride, ... four (FP32) or two (FP64) at a time with all their
+// loads issued before any use (the partial sums keep that node order).
 template <typename T>
-__global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __restrict__ minv,
-                                                         typename Vec4<T>::type* __restrict__ x,
-                                                         typename Vec4<T>::type* __restrict__ r,
-                                                         typename Vec4<T>::type* __restrict__ z,
-                                                         const typename Vec4<T>::type* __restrict__ p,
-                                                         const typename Vec4<T>::type* __restrict__ q,
-                                                         double* partials, PcgScalars* sc) {
+__global__ void __launch_bounds__(256, 2) pcg_update_kernel(int nnd, const T* __restrict__ minv,
+                                                            typename Vec4<T>::type* __restrict__ x,
+                                                            typename Vec4<T>::type* __restrict__ r,
+                                                            typename Vec4<T>::type* __restrict__ z,
+                                                            typename Vec4<T>::type* __restrict__ p,
+                                                            const typename Vec4<T>::type* __restrict__ q,
+                                                            double* partials, PcgScalars* sc, int* status) {
   using V = typename Vec4<T>::type;
+  constexpr int U = sizeof(T) == 4 ? 4 : 2;  // within 128 registers: two CTAs per SM
+  __shared__ double totals[2];
   if (((volatile PcgScalars*)sc)->done) return;
   const T alpha = T(sc->alpha);
+  const double rz_old = sc->rz;  // read before the barrier: CTA 0 replaces it after
+  const int stride = gridDim.x * blockDim.x;
+  const int n0 = blockIdx.x * blockDim.x + threadIdx.x;
   Acc<T> v[2];
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gridDim.x * blockDim.x) {
-    const V pn = p[n], qn = q[n];
-    V xn = x[n], rn = r[n];
-    xn.x += alpha * pn.x;
-    xn.y += alpha * pn.y;
-    xn.z += alpha * pn.z;
-    rn.x -= alpha * qn.x;
-    rn.y -= alpha * qn.y;
-    rn.z -= alpha * qn.z;
-    T zx, zy, zz;
-    apply_minv<T>(minv, n, rn.x, rn.y, rn.z, zx, zy, zz);
-    x[n] = xn;
-    r[n] = rn;
-    z[n] = mk<V, T>(zx, zy, zz);
-    v[0].add_prod(rn.x, zx);
-    v[0].add_prod(rn.y, zy);
-    v[0].add_prod(rn.z, zz);
-    v[1].add_prod(rn.x, rn.x);
-    v[1].add_prod(rn.y, rn.y);
-    v[1].add_prod(rn.z, rn.z);
+  for (int base = n0; base < nnd; base += U * stride) {
+    V pn[U], qn[U], xn[U], rn[U];
+    T B[U][9];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = base + u * stride;
+      if (n < nnd) {
+        pn[u] = p[n];
+        qn[u] = q[n];
+        xn[u] = x[n];
+        rn[u] = r[n];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) B[u][k] = minv[(long long)n * 9 + k];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = base + u * stride;
+      if (n < nnd) {
+        xn[u].x += alpha * pn[u].x;
+        xn[u].y += alpha * pn[u].y;
+        xn[u].z += alpha * pn[u].z;
+        rn[u].x -= alpha * qn[u].x;
+        rn[u].y -= alpha * qn[u].y;
+        rn[u].z -= alpha * qn[u].z;
+        const T zx = B[u][0] * rn[u].x + B[u][1] * rn[u].y + B[u][2] * rn[u].z;
+        const T zy = B[u][3] * rn[u].x + B[u][4] * rn[u].y + B[u][5] * rn[u].z;
+        const T zz = B[u][6] * rn[u].x + B[u][7] * rn[u].y + B[u][8] * rn[u].z;
+        x[n] = xn[u];
+        r[n] = rn[u];
+        z[n] = mk<V, T>(zx, zy, zz);
+        v[0].add_prod(rn[u].x, zx);
+        v[0].add_prod(rn[u].y, zy);
+        v[0].add_prod(rn[u].z, zz);
+        v[1].add_prod(rn[u].x, rn[u].x);
+        v[1].add_prod(rn[u].y, rn[u].y);
+        v[1].add_prod(rn[u].z, rn[u].z);
+      }
+    }
   }
-  double tot[2];
-  if (last_block_total<T, 2>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
+  {
+    double bt[2];
+    block_total<T, 2>(v, bt);
+    if (threadIdx.x == 0) {
+      partials[blockIdx.x] = bt[0];
+      partials[gridDim.x + blockIdx.x] = bt[1];
+    }
+  }
+  if (!grid_barrier(&sc->bar_count, kBarrierLimit)) {
+    if (threadIdx.x == 0) {
+      atomicOr(status, kStatusWaitTimeout);
+      sc->fail = 5;
+      atomicExch(&sc->done, 2);
+    }
+    return;
+  }
+  // every CTA forms the same totals from the partials, in the same order
+  // (one warp: lane-strided sums, then a fixed shuffle tree)
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll 4
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+      s0 += ((volatile double*)partials)[b];
+      s1 += ((volatile double*)partials)[gridDim.x + b];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if (lane == 0) {
+      totals[0] = s0;
+      totals[1] = s1;
+    }
+  }
+  __syncthreads();
+  const double rz = totals[0], rr = totals[1];
+  const double beta_d = rz / rz_old;
+  const T beta = T(beta_d);
+  // next search direction, in place: p = z + beta p
+  for (int base = n0; base < nnd; base += U * stride) {
+    V zn[U], pn[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = base + u * stride;
+      if (n < nnd) {
+        zn[u] = z[n];
+        pn[u] = p[n];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = base + u * stride;
+      if (n < nnd)
+        p[n] = mk<V, T>(zn[u].x + beta * pn[u].x, zn[u].y + beta * pn[u].y, zn[u].z + beta * pn[u].z);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     const int it = sc->iters + 1;
     sc->iters = it;
-    sc->beta = tot[0] / sc->rz;
-    sc->rz = tot[0];
-    sc->rr = tot[1];
-    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
-      sc->done = 2;
+    sc->beta = beta_d;
+    sc->rz = rz;
+    sc->rr = rr;
+    int done = 0;
+    if (!isfinite(rz) || !isfinite(rr)) {
       sc->fail = 4;
+      done = 2;
+    } else if (rr <= sc->tol2 * sc->rr0) {
+      done = 1;
+    } else if (it >= sc->max_it) {
+      done = 3;
     }
-    else if (tot[1] <= sc->tol2 * sc->rr0) sc->done = 1;
-    else if (it >= sc->max_it) sc->done = 3;
+    if (done) atomicCAS(&sc->done, 0, done);  // a barrier failure elsewhere keeps its flag
   }
 }
 
@@ -487,15 +557,13 @@ int spmv_config(Context* c, Grids& g) {
   return g.stages == 3 ? spmv_config_n<T, 3>(c, g) : spmv_config_n<T, 2>(c, g);
 }
 template <typename T>
-void launch_spmv(Context* c, const Grids& g, const void* z, const void* pold, void* pnew) {
+void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc) {
   using V = typename Vec4<T>::type;
   const bool f32 = std::is_same<T, float>::value;
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);
-#define TG_SPMV_ARGS                                                                                         \
-  c->ntiles, off, blob, cap, (const V*)z, (const V*)pold, (V*)pnew, (V*)c->d_q, c->d_partials, c->d_pcg, \
-      c->d_status
+#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status
   if (g.warp_release) {
     if (g.stages == 3)
       pcg_spmv_wr_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
@@ -509,6 +577,31 @@ void launch_spmv(Context* c, const Grids& g, const void* z, const void* pold, vo
   }
 #undef TG_SPMV_ARGS
 }
+
+// The vector update as a cooperative launch (its grid barrier needs every
+// CTA resident; the grid is clamped to what fits at once).
+template <typename T>
+cudaError_t launch_update(Context* c, int grid, const T* minv, void* x, void* r, void* z, void* p, const void* q,
+                          double* partials, PcgScalars* sc) {
+  using V = typename Vec4<T>::type;
+  int per_sm = 0;
+  const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_update_kernel<T>, 256, 0);
+  if (oe != cudaSuccess) return oe;
+  grid = std::max(1, std::min(grid, kNumSMs * per_sm));  // every CTA resident at once
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, pcg_update_kernel<T>, c->nnd, minv, (V*)x, (V*)r, (V*)z, (V*)p, (const V*)q,
+                            partials, sc, c->d_status);
+}
+
 Grids grids(const Context* c) {
   Grids g;
   g.spmv = 0;
@@ -520,7 +613,6 @@ Grids grids(const Context* c) {
 
 template <typename T>
 int capture_chunk(Context* c, const T* minv) {
-  using V = typename Vec4<T>::type;
   Grids g = grids(c);
   {
     const int sc = spmv_config<T>(c, g);
@@ -528,15 +620,18 @@ int capture_chunk(Context* c, const T* minv) {
   }
   cudaGraph_t graph;
   if (!ok(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return TG_ERR_CUDA;
-  static_assert(kChunk % 2 == 0, "p buffers alternate within a chunk");
-  for (int k = 0; k < kChunk; ++k) {
-    V* pold = (V*)(k % 2 == 0 ? c->d_p : c->d_p1);
-    V* pnew = (V*)(k % 2 == 0 ? c->d_p1 : c->d_p);
-    launch_spmv<T>(c, g, c->d_z, pold, pnew);
-    pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z, pnew,
-                                                      (const V*)c->d_q, c->d_partials, c->d_pcg);
+  cudaError_t le = cudaSuccess;
+  for (int k = 0; k < kChunk && le == cudaSuccess; ++k) {
+    launch_spmv<T>(c, g, c->d_p, c->d_q, c->d_partials, c->d_pcg);
+    le = cudaGetLastError();
+    if (le == cudaSuccess)
+      le = launch_update<T>(c, g.vec, minv, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_partials, c->d_pcg);
   }
-  if (!ok(c, cudaStreamEndCapture(c->stream, &graph), "end capture")) return TG_ERR_CUDA;
+  const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+  if (!ok(c, le, "capture launch") || !ok(c, ee, "end capture")) {
+    if (ee == cudaSuccess) cudaGraphDestroy(graph);
+    return TG_ERR_CUDA;
+  }
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
   cudaError_t e = cudaGraphInstantiate(&c->pcg_graph, graph, 0);
@@ -548,7 +643,7 @@ template <typename T>
 int ensure_vectors(Context* c, int precision) {
   using V = typename Vec4<T>::type;
   if (c->pcg_vec_precision == precision) return TG_OK;
-  for (void** pp : {&c->d_x, &c->d_r, &c->d_z, &c->d_p, &c->d_p1, &c->d_q}) {
+  for (void** pp : {&c->d_x, &c->d_r, &c->d_z, &c->d_p, &c->d_q}) {
     if (*pp) dfree(c, *pp);
     V* v = nullptr;
     if (!dalloc(c, &v, (size_t)c->nnd)) return TG_ERR_OOM;
@@ -577,8 +672,8 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
   pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, d_rhs, c->d_mask, minv, c->d_partials, c->d_pcg);
   c->launches++;
   pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, d_rhs, c->d_mask, minv, (V*)c->d_x, (V*)c->d_r,
-                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_p1, (V*)c->d_q, c->d_partials,
-                                                  c->d_pcg, rel_tol, max_it);
+                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials, c->d_pcg,
+                                                  rel_tol, max_it);
   c->launches++;
   if (!ok(c, cudaGetLastError(), "pcg_init_kernel")) return TG_ERR_CUDA;
   if (c->pcg_graph_key != key || !c->pcg_graph) {
@@ -602,7 +697,8 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
   if (h.done == 1) return TG_OK;
   if (h.done == 2) {
     static const char* why[] = {"", "non-finite initial residual", "p.Ap <= 0 (indefinite operator)",
-                                "non-finite p.Ap", "non-finite r.z or r.r", "staged tile wait timed out"};
+                                "non-finite p.Ap", "non-finite r.z or r.r",
+                                "staged tile or grid barrier wait timed out"};
     c->err = std::string("PCG breakdown: ") + why[h.fail >= 1 && h.fail <= 5 ? h.fail : 0] + " at iteration " +
              std::to_string(h.iters);
     return TG_ERR_NAN;
@@ -710,7 +806,7 @@ int launch_gather_solution(Context* c, double* d_eq) {
 
 // Average device time of standalone launches of the two PCG kernels on the
 // current tangent, with the scalars pinned so every launch does the same work
-// (beta = alpha = 0: q = A z, p = z; x, r unchanged).
+// (alpha = 0: x and r unchanged; the product is q = A p).
 template <typename T>
 int time_pcg_t(Context* c, int which, int reps, double* ms) {
   using V = typename Vec4<T>::type;
@@ -726,8 +822,8 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
   pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, c->d_R, c->d_mask, minv, c->d_partials, c->d_pcg);
   c->launches++;
   pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, c->d_R, c->d_mask, minv, (V*)c->d_x, (V*)c->d_r,
-                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_p1, (V*)c->d_q, c->d_partials,
-                                                  c->d_pcg, 1e-30, 1 << 30);
+                                                  (V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials, c->d_pcg,
+                                                  1e-30, 1 << 30);
   c->launches++;
   PcgScalars t;
   std::memset(&t, 0, sizeof(t));
@@ -741,11 +837,11 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
     cudaMemcpyAsync(c->d_pcg, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream);
     cudaEventRecord(a, c->stream);
     if (which == 0)
-      launch_spmv<T>(c, g, c->d_z, c->d_p, c->d_p1);
-    else
-      pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z,
-                                                        (const V*)c->d_p1, (const V*)c->d_q, c->d_partials,
-                                                        c->d_pcg);
+      launch_spmv<T>(c, g, c->d_p, c->d_q, c->d_partials, c->d_pcg);
+    else if (!ok(c, launch_update<T>(c, g.vec, minv, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_partials,
+                                     c->d_pcg),
+                 "pcg_update_kernel"))
+      s = TG_ERR_CUDA;
     cudaEventRecord(b, c->stream);
     c->launches++;
     cudaEventSynchronize(b);
@@ -756,6 +852,7 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   *ms = total / reps;
+  if (s) return s;
   return ok(c, cudaGetLastError(), "time_pcg_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
@@ -773,7 +870,7 @@ template <typename T>
 int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
                     int max_it, int precond, int* iters, double* rel_res) {
   using V = typename Vec4<T>::type;
-  // scratch layout: scalars | partials | rhs (nodal FP64) | x r z p p1 q
+  // scratch layout: scalars | partials | rhs (nodal FP64) | x r z p q
   unsigned char* cur = scratch;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(cur);
   cur += kScratchScalarBytes;
@@ -781,12 +878,12 @@ int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigne
   cur += kScratchPartialBytes;
   double4_32a* rhs = reinterpret_cast<double4_32a*>(cur);
   cur += sizeof(double4_32a) * (size_t)c->nnd;
-  V* vec[6];
-  for (int k = 0; k < 6; ++k) {
+  V* vec[5];
+  for (int k = 0; k < 5; ++k) {
     vec[k] = reinterpret_cast<V*>(cur);
     cur += sizeof(V) * (size_t)c->nnd;
   }
-  V *x = vec[0], *r = vec[1], *z = vec[2], *p = vec[3], *p1 = vec[4], *q = vec[5];
+  V *x = vec[0], *r = vec[1], *z = vec[2], *p = vec[3], *q = vec[4];
   // what must start at zero: the scalars (last-block counters) and the nodal
   // right-hand side (prescribed slots are never written by the scatter)
   if (!ok(c, cudaMemsetAsync(sc, 0, sizeof(PcgScalars), c->stream), "memset") ||
@@ -799,27 +896,18 @@ int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigne
   if (s) return s;
   const T* minv_base = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
   const T* minv = minv_base + (precond == TG_PRECOND_BLOCK_JACOBI ? (long long)c->nnd * 9 : 0);
-  const bool f32 = std::is_same<T, float>::value;
-  const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
-  const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
-  const int cap = blob_cap<T>(c);
+  g.warp_release = 0;  // the CTA-barrier product
   pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, rhs, c->d_mask, minv, partials, sc);
-  pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, rhs, c->d_mask, minv, x, r, z, p, p1, q, partials, sc,
+  pcg_init_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, rhs, c->d_mask, minv, x, r, z, p, q, partials, sc,
                                                   rel_tol, max_it);
   c->launches += 2;
   if (!ok(c, cudaGetLastError(), "pcg init")) return TG_ERR_CUDA;
   const int max_chunks = max_it / kChunk + 2;
   for (int ch = 0; ch < max_chunks; ++ch) {
     for (int k = 0; k < kChunk; ++k) {
-      V* pold = k % 2 == 0 ? p : p1;
-      V* pnew = k % 2 == 0 ? p1 : p;
-      if (g.stages == 3)
-        pcg_spmv_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, z, pold, pnew, q,
-                                                                       partials, sc, c->d_status);
-      else
-        pcg_spmv_kernel<T, 2><<<g.spmv, 256, g.spmv_smem, c->stream>>>(c->ntiles, off, blob, cap, z, pold, pnew, q,
-                                                                       partials, sc, c->d_status);
-      pcg_update_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, minv, x, r, z, pnew, q, partials, sc);
+      launch_spmv<T>(c, g, p, q, partials, sc);
+      if (!ok(c, launch_update<T>(c, g.vec, minv, x, r, z, p, q, partials, sc), "pcg_update_kernel"))
+        return TG_ERR_CUDA;
     }
     c->launches += 2 * kChunk;
     if (!ok(c, cudaGetLastError(), "pcg chunk") ||
@@ -849,7 +937,7 @@ int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigne
 
 size_t pcg_scratch_bytes(const Context* c) {
   const size_t v = c->tangent_precision == TG_MIXED ? sizeof(float4) : sizeof(double4_32a);
-  return kScratchScalarBytes + kScratchPartialBytes + (sizeof(double4_32a) + 6 * v) * (size_t)c->nnd;
+  return kScratchScalarBytes + kScratchPartialBytes + (sizeof(double4_32a) + 5 * v) * (size_t)c->nnd;
 }
 
 int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,

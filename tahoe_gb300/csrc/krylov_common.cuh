@@ -171,5 +171,36 @@ __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier
 
 constexpr int kWaitLimit = 1 << 18;  // polls before a staged tile is declared lost
 
+// ---- grid-wide barrier of a cooperative launch ---------------------------
+constexpr int kBarrierLimit = 1 << 24;  // polls before a grid barrier is declared broken
+
+// Every CTA of a cooperative launch (all resident at once) adds one to a
+// counter that only grows (reset to zero when a solve starts, so it stays far
+// below 2^32) and polls it until it reaches the end of this launch's group of
+// gridDim arrivals.  Bounded: after `limit` polls a CTA stops waiting and the
+// call returns false (the caller records the failure); it never spins forever.
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, int limit) {
+  __shared__ int met;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // this CTA's partial sums before its arrival
+    const unsigned int old = atomicAdd(count, 1u);
+    const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
+    int ok = 1;
+    for (int i = 0;; ++i) {
+      unsigned int cur;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
+      if (cur >= target) break;
+      if (i >= limit) {
+        ok = 0;
+        break;
+      }
+    }
+    met = ok;
+  }
+  __syncthreads();
+  return met != 0;
+}
+
 }  // namespace
 }  // namespace tg

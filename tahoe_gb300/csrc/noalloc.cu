@@ -17,7 +17,7 @@ namespace {
 
 constexpr int kNoAllocMaxNodes = 32768;
 constexpr size_t kNoAllocScratchBytes = 8u << 20;  // 8 MiB per device
-static_assert(tg::kScratchScalarBytes + tg::kScratchPartialBytes + (32 + 6 * 32) * (size_t)kNoAllocMaxNodes <=
+static_assert(tg::kScratchScalarBytes + tg::kScratchPartialBytes + (32 + 5 * 32) * (size_t)kNoAllocMaxNodes <=
                   kNoAllocScratchBytes,
               "scratch too small for the stated node limit");
 

@@ -48,6 +48,7 @@ struct PcgScalars {
   int iters;
   int max_it;
   unsigned int count_a, count_b;  // last-block-done counters
+  unsigned int bar_count;  // arrivals at the vector update's grid barrier (reset per solve)
   int fail;  // breakdown cause: 1 init non-finite, 2 p.q <= 0, 3 p.q non-finite, 4 update non-finite
 };
 
@@ -150,8 +151,7 @@ struct Context {
   void* d_x = nullptr;  // float4 or double4_32a per node (solution du)
   void* d_r = nullptr;
   void* d_z = nullptr;
-  void* d_p = nullptr;   // search direction, double-buffered with d_p1
-  void* d_p1 = nullptr;
+  void* d_p = nullptr;   // search direction (updated in place by the vector update)
   void* d_q = nullptr;
   int pcg_vec_precision = -1;
   PcgScalars* d_pcg = nullptr;

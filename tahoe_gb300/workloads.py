@@ -63,17 +63,24 @@ def c3(nx=96, ny=96, nz=48, nsteps=40, add=None):
 
 
 def spmv_bytes(nnzb, nnd, s_val):
-    """Algorithmic bytes of one fused PCG SpMV launch on the node-block CSR:
-    nine values + one column index per block, row pointers, the gathered z
-    and p_old vectors once each, p_new and q written (vectors padded to 4
-    lanes)."""
+    """Algorithmic bytes of one PCG SpMV launch on the node-block CSR: nine
+    values + one column index per block, row pointers, the gathered p vector
+    once, q written (vectors padded to 4 lanes)."""
     s_vec = 4 * s_val
-    return nnzb * (9 * s_val + 4) + (nnd + 1) * 4 + 2 * nnd * s_vec + 2 * nnd * s_vec
+    return nnzb * (9 * s_val + 4) + (nnd + 1) * 4 + nnd * s_vec + nnd * s_vec
 
 
 def assembly_bytes(nel, nnzb, nnd, s_val):
-    """Algorithmic bytes of one assembly launch: element blocks (36 x 9 values
-    per element) read once, the 64 contribution codes per element and their
-    segment pointers, the block values written once, the preconditioner
-    inverses written."""
-    return nel * 36 * 9 * s_val + nel * 64 * 4 + (nnzb + 1) * 4 + nnzb * 9 * s_val + nnzb * 4 + nnd * 18 * s_val
+    """Algorithmic bytes of one assembly launch: element blocks (36 blocks of
+    3 rows padded to 4 values per element) read once, the 64 contribution
+    codes per element and their segment pointers, the column indices, the
+    block values written once, the preconditioner inverses written."""
+    return nel * 36 * 12 * s_val + nel * 64 * 4 + (nnzb + 1) * 4 + nnzb * 9 * s_val + nnzb * 4 + nnd * 18 * s_val
+
+
+def update_bytes(nnd, s_val):
+    """Algorithmic bytes of one PCG vector update: p, q, x, r and the 3x3
+    preconditioner block read, x, r, z and the next p written (vectors padded
+    to 4 lanes)."""
+    s_vec = 4 * s_val
+    return nnd * (4 * s_vec + 9 * s_val) + nnd * 4 * s_vec
