@@ -528,13 +528,19 @@ int spmv_config_n(Context* c, Grids& g) {
     return TG_ERR_CAPACITY;
   }
   auto kern = c->spmv_warp_release ? pcg_spmv_wr_kernel<T, NST> : pcg_spmv_kernel<T, NST>;
-  // both variants get the attribute (the scratch-vector solve always uses
-  // the CTA-barrier kernel)
-  if (!ok(c, cudaFuncSetAttribute(pcg_spmv_kernel<T, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)g.spmv_smem), "smem attribute") ||
-      !ok(c, cudaFuncSetAttribute(pcg_spmv_wr_kernel<T, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)g.spmv_smem), "smem attribute"))
-    return TG_ERR_CUDA;
+  // Both variants get the attribute (the scratch-vector solve always uses the
+  // CTA-barrier kernel).  The attribute belongs to the function, not to this
+  // context, and contexts with other meshes may configure and launch from
+  // other threads at the same time, so it is always set to the largest
+  // dynamic size the device allows (one value for every caller) rather than
+  // to this mesh's ring.
+  for (auto f : {pcg_spmv_kernel<T, NST>, pcg_spmv_wr_kernel<T, NST>}) {
+    cudaFuncAttributes fa;
+    if (!ok(c, cudaFuncGetAttributes(&fa, f), "function attributes") ||
+        !ok(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
+            "smem attribute"))
+      return TG_ERR_CUDA;
+  }
   int per_sm = 0;
   if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, g.spmv_smem), "occupancy"))
     return TG_ERR_CUDA;

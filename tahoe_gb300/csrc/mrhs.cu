@@ -418,8 +418,13 @@ int mrhs_config(Context* c, size_t smem, int* grid) {
     c->err = "multi-vector SpMV tile ring does not fit in shared memory";
     return TG_ERR_CAPACITY;
   }
-  if (!ok(c, cudaFuncSetAttribute(mrhs_spmv_kernel<T, NST, kNR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem),
+  // the attribute belongs to the function and other contexts may launch it
+  // from other threads: always the device's largest dynamic size (one value
+  // for every caller), not this mesh's ring
+  cudaFuncAttributes fa;
+  if (!ok(c, cudaFuncGetAttributes(&fa, mrhs_spmv_kernel<T, NST, kNR>), "function attributes") ||
+      !ok(c, cudaFuncSetAttribute(mrhs_spmv_kernel<T, NST, kNR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin - (int)fa.sharedSizeBytes),
           "smem attribute"))
     return TG_ERR_CUDA;
   int per_sm = 0;
