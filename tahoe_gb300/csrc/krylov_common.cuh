@@ -177,15 +177,16 @@ constexpr int kBarrierLimit = 1 << 24;  // polls before a grid barrier is declar
 // Every CTA of a cooperative launch (all resident at once) adds one to a
 // counter that only grows (reset to zero when a solve starts, so it stays far
 // below 2^32) and polls it until it reaches the end of this launch's group of
-// gridDim arrivals.  Bounded: after `limit` polls a CTA stops waiting and the
+// arrivals (one per CTA of the grid).  Bounded: after `limit` polls a CTA stops waiting and the
 // call returns false (the caller records the failure); it never spins forever.
 __device__ __forceinline__ bool grid_barrier(unsigned int* count, int limit) {
   __shared__ int met;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();  // this CTA's partial sums before its arrival
+    const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
     const unsigned int old = atomicAdd(count, 1u);
-    const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
+    const unsigned int target = (old / nb + 1u) * nb;
     int ok = 1;
     for (int i = 0;; ++i) {
       unsigned int cur;

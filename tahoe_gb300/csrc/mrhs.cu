@@ -80,6 +80,7 @@ struct MScalars {
   int done;  // 1 all converged, 2 breakdown / non-finite, 3 iteration limit
   int iters, max_it, fail;
   unsigned count_a, count_b;
+  unsigned bar_count;  // arrivals at the update's grid barrier (reset per solve)
 };
 
 template <typename T, int NR>
@@ -118,8 +119,8 @@ __global__ void __launch_bounds__(256) mrhs_init_kernel(int nnd, const double4_3
                                                         const uint8_t* __restrict__ mask, const T* __restrict__ minv,
                                                         typename Vec4<T>::type* x, typename Vec4<T>::type* r,
                                                         typename Vec4<T>::type* z, typename Vec4<T>::type* p,
-                                                        typename Vec4<T>::type* p1, typename Vec4<T>::type* q,
-                                                        double* partials, MScalars<NR>* sc, double tol, int max_it) {
+                                                        typename Vec4<T>::type* q, double* partials,
+                                                        MScalars<NR>* sc, double tol, int max_it) {
   using V = typename Vec4<T>::type;
   const int g = blockIdx.y;
   Acc<T> v[2 * kGS];  // r.z then r.r of the group's right-hand sides
@@ -141,8 +142,7 @@ __global__ void __launch_bounds__(256) mrhs_init_kernel(int nnd, const double4_3
       x[i] = zero;
       r[i] = mk<V, T>(rx, ry, rz);
       z[i] = mk<V, T>(zx, zy, zz);
-      p[i] = zero;
-      p1[i] = zero;
+      p[i] = mk<V, T>(zx, zy, zz);  // first direction p = z
       q[i] = zero;
       v[j].add_prod(rx, zx);
       v[j].add_prod(ry, zy);
@@ -171,29 +171,27 @@ __global__ void __launch_bounds__(256) mrhs_init_kernel(int nnd, const double4_3
     sc->max_it = max_it;
     sc->iters = 0;
     sc->count_a = 0u;
+    sc->bar_count = 0u;
     sc->fail = bad ? 1 : 0;
     sc->done = bad ? 2 : (any ? 0 : 1);
   }
 }
 
-// q_k = A p_new_k for all k, with p_new_k = z_k + beta_k p_old_k formed at
-// every gathered node; the same tile ring as the single-vector product.
+// q_k = A p_k for all k; the same tile ring as the single-vector product.
+// Each lane takes its row's blocks two at a time with both neighbours'
+// gathers in flight before the arithmetic.
 template <typename T, int NST, int NR>
 __global__ void __launch_bounds__(256) mrhs_spmv_kernel(int nnd, int ntiles, const long long* __restrict__ blob_off,
                                                         const unsigned char* __restrict__ blob, int cap,
-                                                        const typename Vec4<T>::type* __restrict__ z,
-                                                        const typename Vec4<T>::type* __restrict__ pold,
-                                                        typename Vec4<T>::type* __restrict__ pnew,
+                                                        const typename Vec4<T>::type* __restrict__ p,
                                                         typename Vec4<T>::type* __restrict__ q, double* partials,
                                                         MScalars<NR>* sc, int* status) {
   using V = typename Vec4<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
-  __shared__ T sbeta[NR];
   if (((volatile MScalars<NR>*)sc)->done) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  if (threadIdx.x < NR) sbeta[threadIdx.x] = T(sc->beta[threadIdx.x]);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NST; ++k) mbar_init(&bars[k], 1);
@@ -241,8 +239,6 @@ __global__ void __launch_bounds__(256) mrhs_spmv_kernel(int nnd, int ntiles, con
     const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
 #pragma unroll
     for (int g = 0; g < kNG; ++g) {
-      const T b0 = sbeta[g * kGS], b1 = sbeta[g * kGS + 1], b2 = sbeta[g * kGS + 2];
-      const T bg[kGS] = {b0, b1, b2};
       for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
         const bool live = li < nrows;
         const int I = r0 + li;
@@ -251,22 +247,31 @@ __global__ void __launch_bounds__(256) mrhs_spmv_kernel(int nnd, int ntiles, con
         for (int jj = 0; jj < kGS; ++jj) a[jj][0] = a[jj][1] = a[jj][2] = T(0);
         const int e0 = live ? rp[li] : 0;
         const int e1 = live ? rp[li + 1] : 0;
-        for (int j = e0 + sub; j < e1; j += 8) {
-          const int J = cl[j];
-          const T* vv = pl + j;
-          T mv[9];
-#pragma unroll
-          for (int i = 0; i < 9; ++i) mv[i] = vv[i * ps];
-          const long long o = vidx(nnd, J, g * kGS);
-          const V* zj = z + o;
-          const V* pj = pold + o;
+        for (int j = e0 + sub; j < e1; j += 16) {
+          const int jb = j + 8;
+          const bool two = jb < e1;
+          const long long oa = vidx(nnd, cl[j], g * kGS);
+          const long long ob = two ? vidx(nnd, cl[jb], g * kGS) : oa;
+          V pa[kGS], pb[kGS];
 #pragma unroll
           for (int jj = 0; jj < kGS; ++jj) {
-            const V zz = zj[jj], pp = pj[jj];
-            const T x = zz.x + bg[jj] * pp.x, y = zz.y + bg[jj] * pp.y, w = zz.z + bg[jj] * pp.z;
-            a[jj][0] += mv[0] * x + mv[1] * y + mv[2] * w;
-            a[jj][1] += mv[3] * x + mv[4] * y + mv[5] * w;
-            a[jj][2] += mv[6] * x + mv[7] * y + mv[8] * w;
+            pa[jj] = p[oa + jj];
+            pb[jj] = p[ob + jj];
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            if (h == 1 && !two) break;
+            const T* vv = pl + (h == 0 ? j : jb);
+            T mv[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) mv[i] = vv[i * ps];
+#pragma unroll
+            for (int jj = 0; jj < kGS; ++jj) {
+              const V pp = h == 0 ? pa[jj] : pb[jj];
+              a[jj][0] += mv[0] * pp.x + mv[1] * pp.y + mv[2] * pp.z;
+              a[jj][1] += mv[3] * pp.x + mv[4] * pp.y + mv[5] * pp.z;
+              a[jj][2] += mv[6] * pp.x + mv[7] * pp.y + mv[8] * pp.z;
+            }
           }
         }
 #pragma unroll
@@ -283,13 +288,11 @@ __global__ void __launch_bounds__(256) mrhs_spmv_kernel(int nnd, int ntiles, con
           for (int jj = 0; jj < kGS; ++jj)
             if (jj == sub) {
               const long long i = vidx(nnd, I, g * kGS + jj);
-              const V zi = z[i], pi = pold[i];
-              const V pn = mk<V, T>(zi.x + bg[jj] * pi.x, zi.y + bg[jj] * pi.y, zi.z + bg[jj] * pi.z);
+              const V pi = p[i];
               q[i] = mk<V, T>(a[jj][0], a[jj][1], a[jj][2]);
-              pnew[i] = pn;
-              v[g * kGS + jj].add_prod(pn.x, a[jj][0]);
-              v[g * kGS + jj].add_prod(pn.y, a[jj][1]);
-              v[g * kGS + jj].add_prod(pn.z, a[jj][2]);
+              v[g * kGS + jj].add_prod(pi.x, a[jj][0]);
+              v[g * kGS + jj].add_prod(pi.y, a[jj][1]);
+              v[g * kGS + jj].add_prod(pi.z, a[jj][2]);
             }
         }
       }
@@ -322,22 +325,52 @@ __global__ void __launch_bounds__(256) mrhs_spmv_kernel(int nnd, int ntiles, con
   }
 }
 
+// Totals of group g's 2*kGS partial sums (r.z of its right-hand sides, then
+// r.r) over the gx CTAs of its grid row: one warp, lane-strided sums and a
+// fixed shuffle tree, so every CTA that forms them gets the same bits.
+// Valid on lane 0.
+__device__ __forceinline__ void group_totals(const double* partials, int gx, int g, double (&tot)[2 * kGS]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < 2 * kGS; ++j) {
+    double s = 0.0;
+    for (int b = lane; b < gx; b += 32) s += ((volatile const double*)partials)[((long long)g * 2 * kGS + j) * gx + b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    tot[j] = s;
+  }
+}
+
+// x_k += alpha_k p_k, r_k -= alpha_k q_k, z_k = M^-1 r_k; then, after a
+// bounded grid barrier (cooperative launch: every CTA resident), p_k = z_k +
+// beta_k p_k in place, every CTA forming its group's beta from the partials in
+// the same order.  A right-hand side that is converged (or converges now) gets
+// beta = 0 and, in the next product, alpha = 0: it stays frozen.
 template <typename T, int NR>
 __global__ void __launch_bounds__(256) mrhs_update_kernel(int nnd, const T* __restrict__ minv,
                                                           typename Vec4<T>::type* __restrict__ x,
                                                           typename Vec4<T>::type* __restrict__ r,
                                                           typename Vec4<T>::type* __restrict__ z,
-                                                          const typename Vec4<T>::type* __restrict__ p,
+                                                          typename Vec4<T>::type* __restrict__ p,
                                                           const typename Vec4<T>::type* __restrict__ q,
-                                                          double* partials, MScalars<NR>* sc) {
+                                                          double* partials, MScalars<NR>* sc, int* status) {
   using V = typename Vec4<T>::type;
+  __shared__ double sbeta[kGS];
   if (((volatile MScalars<NR>*)sc)->done) return;
   const int g = blockIdx.y;
+  const int gx = gridDim.x;
   T alpha[kGS];
+  double rz_old[kGS];
+  int active[kGS];
 #pragma unroll
-  for (int j = 0; j < kGS; ++j) alpha[j] = T(sc->alpha[g * kGS + j]);
+  for (int j = 0; j < kGS; ++j) {
+    alpha[j] = T(sc->alpha[g * kGS + j]);
+    rz_old[j] = sc->rz[g * kGS + j];  // read before the barrier: CTA (0,0) replaces them after
+    active[j] = sc->active[g * kGS + j];
+  }
+  const double tol2 = sc->tol2;
   Acc<T> v[2 * kGS];
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gridDim.x * blockDim.x) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gx * blockDim.x) {
     const long long i0 = vidx(nnd, n, g * kGS);
 #pragma unroll
     for (int j = 0; j < kGS; ++j) {
@@ -363,33 +396,85 @@ __global__ void __launch_bounds__(256) mrhs_update_kernel(int nnd, const T* __re
       v[kGS + j].add_prod(rn.z, rn.z);
     }
   }
-  double tot[kNG * 2 * kGS];
-  if (last_block_total_groups<T, 2 * kGS, kNG>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
-    const int it = sc->iters + 1;
-    sc->iters = it;
-    int any = 0;
-    for (int k = 0; k < NR; ++k) {
-      if (!sc->active[k]) {
-        sc->beta[k] = 0.0;  // frozen: p_new = z, and alpha stays 0
-        continue;
-      }
-      const double rzk = tot[(k / kGS) * 2 * kGS + (k % kGS)], rrk = tot[(k / kGS) * 2 * kGS + kGS + (k % kGS)];
-      if (!isfinite(rzk) || !isfinite(rrk)) {
-        sc->done = 2;
-        sc->fail = 4;
-        return;
-      }
-      sc->beta[k] = rzk / sc->rz[k];
-      sc->rz[k] = rzk;
-      sc->rr[k] = rrk;
-      if (rrk <= sc->tol2 * sc->rr0[k]) {
-        sc->active[k] = 0;
-        sc->beta[k] = 0.0;
-      }
-      any |= sc->active[k];
+  {
+    double bt[2 * kGS];
+    block_total<T, 2 * kGS>(v, bt);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int j = 0; j < 2 * kGS; ++j) partials[((long long)g * 2 * kGS + j) * gx + blockIdx.x] = bt[j];
+  }
+  if (!grid_barrier(&sc->bar_count, kBarrierLimit)) {
+    if (threadIdx.x == 0) {
+      atomicOr(status, kStatusWaitTimeout);
+      sc->fail = 5;
+      atomicExch(&sc->done, 2);
     }
-    if (!any) sc->done = 1;
-    else if (it >= sc->max_it) sc->done = 3;
+    return;
+  }
+  if (threadIdx.x < 32) {
+    double tot[2 * kGS];
+    group_totals(partials, gx, g, tot);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int j = 0; j < kGS; ++j) {
+        const double rzk = tot[j], rrk = tot[kGS + j];
+        double beta = 0.0;
+        if (active[j] && isfinite(rzk) && isfinite(rrk) && !(rrk <= tol2 * sc->rr0[g * kGS + j]))
+          beta = rzk / rz_old[j];
+        sbeta[j] = beta;
+      }
+  }
+  __syncthreads();
+  T beta[kGS];
+#pragma unroll
+  for (int j = 0; j < kGS; ++j) beta[j] = T(sbeta[j]);
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnd; n += gx * blockDim.x) {
+    const long long i0 = vidx(nnd, n, g * kGS);
+#pragma unroll
+    for (int j = 0; j < kGS; ++j) {
+      const V zn = z[i0 + j], pn = p[i0 + j];
+      p[i0 + j] = mk<V, T>(zn.x + beta[j] * pn.x, zn.y + beta[j] * pn.y, zn.z + beta[j] * pn.z);
+    }
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 32) {
+    // the scalars of every right-hand side, from the same totals
+    double tot[kNG][2 * kGS];
+#pragma unroll
+    for (int gg = 0; gg < kNG; ++gg) group_totals(partials, gx, gg, tot[gg]);
+    if (threadIdx.x == 0) {
+      const int it = sc->iters + 1;
+      sc->iters = it;
+      int any = 0, bad = 0;
+      for (int k = 0; k < NR; ++k) {
+        if (!sc->active[k]) {
+          sc->beta[k] = 0.0;
+          continue;
+        }
+        const double rzk = tot[k / kGS][k % kGS], rrk = tot[k / kGS][kGS + (k % kGS)];
+        if (!isfinite(rzk) || !isfinite(rrk)) {
+          bad = 1;
+          continue;
+        }
+        sc->beta[k] = rzk / sc->rz[k];
+        sc->rz[k] = rzk;
+        sc->rr[k] = rrk;
+        if (rrk <= sc->tol2 * sc->rr0[k]) {
+          sc->active[k] = 0;
+          sc->beta[k] = 0.0;
+        }
+        any |= sc->active[k];
+      }
+      int done = 0;
+      if (bad) {
+        sc->fail = 4;
+        done = 2;
+      } else if (!any) {
+        done = 1;
+      } else if (it >= sc->max_it) {
+        done = 3;
+      }
+      if (done) atomicCAS(&sc->done, 0, done);  // a barrier failure elsewhere keeps its flag
+    }
   }
 }
 
@@ -457,34 +542,48 @@ int mrhs_solve_t(Context* c, const double4_32a* d_b, const double4_32a* d_v, dou
   int s = mrhs_config<T, 2>(c, smem, &grid);
   if (s) return s;
   const int vgrid = std::min((c->nnd + 255) / 256, kNumSMs * 2);            // scale pass (1-D)
-  const int ugrid = std::min((c->nnd + 255) / 256, kNumSMs * 4);            // per group (2-D rows)
+  // the update is a cooperative launch: its kNG grid rows together fit at once
+  int upd_per_sm = 0;
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&upd_per_sm, mrhs_update_kernel<T, kNR>, 256, 0),
+          "occupancy"))
+    return TG_ERR_CUDA;
+  const int ugrid = std::max(1, std::min((c->nnd + 255) / 256, kNumSMs * upd_per_sm / kNG));  // per group row
   const size_t npart = (size_t)std::max({(long long)grid * kNR, (long long)vgrid * kNR, (long long)ugrid * kNR * 2});
   const size_t nv = (size_t)c->nnd * kNR;
-  V *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *p1 = nullptr, *q = nullptr;
+  V *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
   S* sc = nullptr;
   double* part = nullptr;
   cudaStream_t st = c->stream;
   bool good = ok(c, cudaMallocAsync((void**)&part, sizeof(double) * npart, st), "alloc");
-  for (V** pp : {&x, &r, &z, &p, &p1, &q}) good = good && ok(c, cudaMallocAsync((void**)pp, sizeof(V) * nv, st), "alloc");
+  for (V** pp : {&x, &r, &z, &p, &q}) good = good && ok(c, cudaMallocAsync((void**)pp, sizeof(V) * nv, st), "alloc");
   good = good && ok(c, cudaMallocAsync((void**)&sc, sizeof(S), st), "alloc");
   if (!good) return TG_ERR_OOM;
   good = ok(c, cudaMemsetAsync(sc, 0, sizeof(S), st), "memset");
   if (good) {
     mrhs_scale_kernel<T, kNR><<<vgrid, 256, 0, st>>>(c->nnd, d_b, c->d_mask, minv, part, sc);
-    mrhs_init_kernel<T, kNR><<<dim3(ugrid, kNG), 256, 0, st>>>(c->nnd, d_b, c->d_mask, minv, x, r, z, p, p1, q, part,
-                                                              sc, rel_tol, max_it);
+    mrhs_init_kernel<T, kNR><<<dim3(ugrid, kNG), 256, 0, st>>>(c->nnd, d_b, c->d_mask, minv, x, r, z, p, q, part, sc,
+                                                              rel_tol, max_it);
     c->launches += 2;
     good = ok(c, cudaGetLastError(), "mrhs init");
   }
   S h;
   std::memset(&h, 0, sizeof(h));
   for (int k = 0; good && k * kPollEvery <= max_it + 2 * kPollEvery; ++k) {
-    for (int j = 0; j < kPollEvery; ++j) {
-      V* pold = (j % 2 == 0) ? p : p1;
-      V* pnew = (j % 2 == 0) ? p1 : p;
-      mrhs_spmv_kernel<T, 2, kNR><<<grid, 256, smem, st>>>(c->nnd, c->ntiles, off, blob, cap, z, pold, pnew, q,
-                                                           part, sc, c->d_status);
-      mrhs_update_kernel<T, kNR><<<dim3(ugrid, kNG), 256, 0, st>>>(c->nnd, minv, x, r, z, pnew, q, part, sc);
+    for (int j = 0; j < kPollEvery && good; ++j) {
+      mrhs_spmv_kernel<T, 2, kNR><<<grid, 256, smem, st>>>(c->nnd, c->ntiles, off, blob, cap, p, q, part, sc,
+                                                           c->d_status);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(ugrid, kNG);
+      cfg.blockDim = dim3(256);
+      cfg.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      good = ok(c, cudaLaunchKernelEx(&cfg, mrhs_update_kernel<T, kNR>, c->nnd, minv, x, r, z, p, (const V*)q, part,
+                                      sc, c->d_status),
+                "mrhs update");
     }
     c->launches += 2 * kPollEvery;
     good = ok(c, cudaGetLastError(), "mrhs iterate") &&
@@ -497,7 +596,7 @@ int mrhs_solve_t(Context* c, const double4_32a* d_b, const double4_32a* d_v, dou
     c->launches++;
     good = ok(c, cudaGetLastError(), "mrhs combine");
   }
-  for (void* ptr : {(void*)x, (void*)r, (void*)z, (void*)p, (void*)p1, (void*)q, (void*)sc, (void*)part})
+  for (void* ptr : {(void*)x, (void*)r, (void*)z, (void*)p, (void*)q, (void*)sc, (void*)part})
     if (ptr) cudaFreeAsync(ptr, st);
   if (!ok(c, cudaStreamSynchronize(st), "sync") || !good) return TG_ERR_CUDA;
   if (iters) *iters = h.iters;
@@ -507,7 +606,8 @@ int mrhs_solve_t(Context* c, const double4_32a* d_b, const double4_32a* d_v, dou
   if (worst_rel) *worst_rel = worst;
   if (h.done == 2) {
     static const char* why[] = {"", "non-finite initial residual", "p.Ap <= 0 (indefinite operator)",
-                                "p.Ap not finite", "non-finite update", "staged tile copy timed out"};
+                                "p.Ap not finite", "non-finite update",
+                                "staged tile copy or grid barrier wait timed out"};
     c->err = std::string("multi-vector PCG breakdown: ") + why[(h.fail >= 0 && h.fail <= 5) ? h.fail : 0];
     return TG_ERR_NAN;
   }
