@@ -44,6 +44,10 @@ void free_all(Context* c) {
   if (c->ev_a) cudaEventDestroy(c->ev_a);
   if (c->ev_b) cudaEventDestroy(c->ev_b);
   c->ev_a = c->ev_b = nullptr;
+  for (cudaEvent_t& e : c->ev_poll) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
@@ -240,7 +244,9 @@ int tg_create(tg_context** out, int device) {
     cudaGetLastError();
   }
   if (set_device(c) || !ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
-      !ok(c, cudaMallocHost((void**)&c->h_pcg, sizeof(PcgScalars)), "pinned") ||
+      !ok(c, cudaMallocHost((void**)&c->h_pcg, 2 * sizeof(PcgScalars)), "pinned") ||
+      !ok(c, cudaEventCreateWithFlags(&c->ev_poll[0], cudaEventDisableTiming), "event") ||
+      !ok(c, cudaEventCreateWithFlags(&c->ev_poll[1], cudaEventDisableTiming), "event") ||
       !ok(c, cudaMallocHost((void**)&c->h_resid, sizeof(ResidScalars)), "pinned") ||
       !ok(c, cudaMallocHost((void**)&c->h_status, sizeof(int)), "pinned")) {
     free_all(c);

@@ -687,16 +687,27 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
     if (s) return s;
     c->pcg_graph_key = key;
   }
+  // The scalars after each chunk are copied into alternating pinned mirrors;
+  // the host checks a chunk's flag while the next chunk already runs, so the
+  // GPU never idles for the round trip.  A chunk queued after convergence
+  // costs only kernels that return at once.
   const int max_chunks = max_it / kChunk + 2;
+  int last = 0;
   for (int k = 0; k < max_chunks; ++k) {
     if (!ok(c, cudaGraphLaunch(c->pcg_graph, c->stream), "graph launch")) return TG_ERR_CUDA;
     c->launches += 2 * kChunk;
-    if (!ok(c, cudaMemcpyAsync(c->h_pcg, c->d_pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c->stream), "copy"))
+    last = k & 1;
+    if (!ok(c, cudaMemcpyAsync(&c->h_pcg[last], c->d_pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c->stream),
+            "copy") ||
+        !ok(c, cudaEventRecord(c->ev_poll[last], c->stream), "event"))
       return TG_ERR_CUDA;
-    if (!ok(c, cudaStreamSynchronize(c->stream), "pcg sync")) return TG_ERR_CUDA;
-    if (c->h_pcg->done) break;
+    if (k > 0) {
+      if (!ok(c, cudaEventSynchronize(c->ev_poll[last ^ 1]), "pcg poll")) return TG_ERR_CUDA;
+      if (c->h_pcg[last ^ 1].done) break;
+    }
   }
-  const PcgScalars& h = *c->h_pcg;
+  if (!ok(c, cudaStreamSynchronize(c->stream), "pcg sync")) return TG_ERR_CUDA;
+  const PcgScalars& h = c->h_pcg[last];
   if (iters) *iters = h.iters;
   if (rel_res) *rel_res = h.rr0 > 0 ? std::sqrt(h.rr / h.rr0) : 0.0;
   c->have_du = true;

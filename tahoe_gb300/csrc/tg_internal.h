@@ -159,7 +159,8 @@ struct Context {
   int partials_cap = 0;
   ResidScalars* d_resid = nullptr;
   int* d_status = nullptr;
-  PcgScalars* h_pcg = nullptr;       // pinned mirror
+  PcgScalars* h_pcg = nullptr;       // pinned mirrors [2]: chunk scalars alternate between them
+  cudaEvent_t ev_poll[2] = {nullptr, nullptr};  // arrival of each mirror's copy
   ResidScalars* h_resid = nullptr;   // pinned mirror
   int* h_status = nullptr;           // pinned mirror
   double4_32a* d_du_last = nullptr;      // FP64 update (nnd)
