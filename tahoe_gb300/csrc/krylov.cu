@@ -12,7 +12,7 @@
 // repeatable, no floating-point atomics) and compute alpha / beta and the
 // convergence flag on the device.  Iterations run in chunks captured once in
 // a CUDA graph; kernels return immediately once the flag is set, and the host
-// polls the flag between chunks.
+// reads each chunk's flag while the next chunk runs.
 //
 // Vectors are stored per node, padded to 4 lanes (float4 in the mixed form,
 // double4_32a in the plain FP64 form).  Dot products and norms accumulate in
