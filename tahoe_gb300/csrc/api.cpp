@@ -159,6 +159,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
   c->d_geo = nullptr;
+  c->d_xyz = nullptr;
   c->d_blob32 = c->d_blob64 = nullptr;
   c->nseg = 0;
   c->d_seg_node = c->d_seg_elem = nullptr;
@@ -501,30 +502,30 @@ int tg_pattern_build(tg_context* c, int upper_only, int* row_ptr, int* col_idx, 
   return TG_OK;
 }
 
+// The caller's (x, y, z) array is copied as it is (directly by DMA when the
+// caller's memory is pinned) into a device staging array and re-laid out
+// into the padded nodal vector on the device.
 int tg_set_displacement(tg_context* c, const double* u) {
   if (!c || !u || c->nnd <= 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
-  std::vector<double4_32a> h(c->nnd);
-  for (int n = 0; n < c->nnd; ++n) h[n] = make_double4_32a(u[n * 3], u[n * 3 + 1], u[n * 3 + 2], 0.0);
-  return ok(c, cudaMemcpyAsync(c->d_u, h.data(), sizeof(double4_32a) * c->nnd, cudaMemcpyHostToDevice, c->stream), "u") &&
-                 ok(c, cudaStreamSynchronize(c->stream), "sync")
-             ? TG_OK
-             : TG_ERR_CUDA;
+  if (!c->d_xyz && !dalloc(c, &c->d_xyz, (size_t)c->nnd * 3)) return TG_ERR_OOM;
+  if (!ok(c, cudaMemcpyAsync(c->d_xyz, u, sizeof(double) * 3 * c->nnd, cudaMemcpyHostToDevice, c->stream), "u"))
+    return TG_ERR_CUDA;
+  const int s = launch_xyz_to_nodal(c, c->d_xyz, c->d_u);
+  if (s) return s;
+  return ok(c, cudaStreamSynchronize(c->stream), "sync") ? TG_OK : TG_ERR_CUDA;
 }
 
 int tg_get_displacement(tg_context* c, double* u) {
   if (!c || !u || c->nnd <= 0) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
-  std::vector<double4_32a> h(c->nnd);
-  if (!ok(c, cudaMemcpyAsync(h.data(), c->d_u, sizeof(double4_32a) * c->nnd, cudaMemcpyDeviceToHost, c->stream), "u") ||
-      !ok(c, cudaStreamSynchronize(c->stream), "sync"))
-    return TG_ERR_CUDA;
-  for (int n = 0; n < c->nnd; ++n) {
-    u[n * 3] = h[n].x;
-    u[n * 3 + 1] = h[n].y;
-    u[n * 3 + 2] = h[n].z;
-  }
-  return TG_OK;
+  if (!c->d_xyz && !dalloc(c, &c->d_xyz, (size_t)c->nnd * 3)) return TG_ERR_OOM;
+  const int s = launch_nodal_to_xyz(c, c->d_u, c->d_xyz);
+  if (s) return s;
+  return ok(c, cudaMemcpyAsync(u, c->d_xyz, sizeof(double) * 3 * c->nnd, cudaMemcpyDeviceToHost, c->stream), "u") &&
+                 ok(c, cudaStreamSynchronize(c->stream), "sync")
+             ? TG_OK
+             : TG_ERR_CUDA;
 }
 
 int tg_set_prescribed(tg_context* c, int n, const int* idx, const double* val) {

@@ -149,6 +149,21 @@ __global__ void apply_update_kernel(int nnd, const V* __restrict__ du, const Pcg
   u[n] = x;
 }
 
+__global__ void xyz_to_nodal_kernel(int nnd, const double* __restrict__ xyz, double4_32a* __restrict__ u) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnd) return;
+  u[n] = make_double4_32a(xyz[3LL * n], xyz[3LL * n + 1], xyz[3LL * n + 2], 0.0);
+}
+
+__global__ void nodal_to_xyz_kernel(int nnd, const double4_32a* __restrict__ u, double* __restrict__ xyz) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnd) return;
+  const double4_32a v = u[n];
+  xyz[3LL * n] = v.x;
+  xyz[3LL * n + 1] = v.y;
+  xyz[3LL * n + 2] = v.z;
+}
+
 __global__ void gather_eq_kernel(int neq, const int* __restrict__ slot, const double4_32a* __restrict__ nodal,
                                  double* __restrict__ eq) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -238,6 +253,18 @@ int launch_apply_update(Context* c) {
     apply_update_kernel<double4_32a><<<grid, 256, 0, c->stream>>>(c->nnd, (const double4_32a*)c->d_x, c->d_pcg, c->d_u);
   c->launches++;
   return ok(c, cudaGetLastError(), "apply_update_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_xyz_to_nodal(Context* c, const double* d_xyz, double4_32a* d_nodal) {
+  xyz_to_nodal_kernel<<<(c->nnd + 255) / 256, 256, 0, c->stream>>>(c->nnd, d_xyz, d_nodal);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "xyz_to_nodal_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+int launch_nodal_to_xyz(Context* c, const double4_32a* d_nodal, double* d_xyz) {
+  nodal_to_xyz_kernel<<<(c->nnd + 255) / 256, 256, 0, c->stream>>>(c->nnd, d_nodal, d_xyz);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "nodal_to_xyz_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
 int launch_gather_eq(Context* c, const double4_32a* d_nodal, double* d_eq) {

@@ -125,6 +125,7 @@ struct Context {
   float* d_minv32 = nullptr;    // 18*nnd: Jacobi then block-Jacobi
   double* d_minv64 = nullptr;
   double* d_geo = nullptr;      // 25 planes over nel*8 points: dN/dX (3x8), w det J (residual)
+  double* d_xyz = nullptr;      // nnd*3: staging of caller (x, y, z) nodal arrays
   float* d_Ke32 = nullptr;      // nel*432: 36 upper node-pair blocks, rows padded to 4
   double* d_Ke64 = nullptr;
   int tangent_precision = -1;   // precision of the last tangent
@@ -275,6 +276,8 @@ int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out);
 int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs, bool zero_base = false, int nvec = 1);
 int launch_diff(Context* c, const double4_32a* a, const double4_32a* b, double4_32a* out);
 int launch_gather_eq(Context* c, const double4_32a* d_nodal, double* d_eq);
+int launch_xyz_to_nodal(Context* c, const double* d_xyz, double4_32a* d_nodal);  // 3 -> padded 4 per node
+int launch_nodal_to_xyz(Context* c, const double4_32a* d_nodal, double* d_xyz);
 int launch_scatter_eq(Context* c, const double* d_eq, double4_32a* d_nodal);
 
 }  // namespace tg

@@ -214,8 +214,12 @@ class Context:
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
         self._chk(self.L.tg_set_displacement(self.h, _d(u)), "tg_set_displacement")
 
-    def get_u(self):
-        u = np.zeros(self.nnd * 3)
+    def get_u(self, out=None):
+        """Displacements (nnd, 3); written into `out` (a contiguous float64
+        array of nnd*3 values, e.g. in pinned memory) when given."""
+        u = np.zeros(self.nnd * 3) if out is None else out.reshape(-1)
+        if u.dtype != np.float64 or u.size != self.nnd * 3 or not u.flags.c_contiguous:
+            raise ValueError("get_u: out must be a contiguous float64 array of nnd*3 values")
         self._chk(self.L.tg_get_displacement(self.h, _d(u)), "tg_get_displacement")
         return u.reshape(-1, 3)
 
