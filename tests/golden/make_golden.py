@@ -36,6 +36,10 @@ DECKS = [
      ["benchmark/beam.Newton.io0.run"]),
     ("beam_bbar", "level.0/3D.elastostatic/beam.B_bar.xml",
      ["benchmark/beam.B_bar.io0.run"]),
+    ("mat01_ssstvenant_cube", "level.1/material.solid/3D/material.01/mat.1.a.xml",
+     ["benchmark/mat.1.a.io0.run"]),
+    ("mat02_fsstvenant_cube", "level.1/material.solid/3D/material.02/mat.2.a.xml",
+     ["benchmark/mat.2.a.io0.run"]),
 ]
 
 

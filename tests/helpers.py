@@ -10,7 +10,8 @@ from tahoe_gb300.meshgen import BoxMesh
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GOLDEN_NAMES = ["mat08_j2_cube", "mat24_hookean_cube", "mat05_simo_cube", "traction_a_cube",
-                "beam_newton_totlag", "beam_newton_updlag", "beam_bbar"]
+                "beam_newton_totlag", "beam_newton_updlag", "beam_bbar", "mat01_ssstvenant_cube",
+                "mat02_fsstvenant_cube"]
 
 
 def load_fixture(name):
