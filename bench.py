@@ -14,12 +14,14 @@ lower is better).  Inputs stay resident in HBM; the block-CSR matrix (about
 290 MB) is larger than the 129 MB L2, so no flush is needed between steps.
 
 `e2e` repeats the step through the C ABI with host buffers: displacement
-uploaded from host memory, residual at the step start, the iteration, and the
-displacement read back, all inside the timed region.
+uploaded from pinned host memory, residual at the step start, the iteration,
+and the displacement read back into pinned host memory, all inside the timed
+region.
 
 --impl reference times the reference algorithm on the host cores instead
 (the CPU oracle restatement: the reference's own build needs its CMake
-system), on a bounded sample of the same workload.
+system, generated headers and expat, so it is not compiled here), on a
+bounded sample of the same workload.
 
 Multi-GPU: independent replicas (the single-mesh path has a real halo
 exchange that is not built); --gpus N under torchrun runs N replicas.
