@@ -2,8 +2,8 @@
  * CPU oracle for the Tahoe implicit hex8 solid path -- TEST INFRASTRUCTURE.
  *
  * A plain FP64 restatement of the reference algorithms, written for clarity
- * rather than speed.  It is the checker for the CUDA library: only tests,
- * the smoke check and the benchmark's CPU-baseline leg use it.  Each routine
+ * rather than speed.  The CUDA library's results are tested against it:
+ * only tests, the smoke check and the benchmark's CPU-baseline leg use it.  Each routine
  * names the reference function it restates (paths relative to the Tahoe
  * source tree).
  */

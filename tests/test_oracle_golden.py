@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's own golden outputs (regression-suite
-.run files extracted into tests/golden).  Pins the oracle before it is used as
-the checker for the CUDA path."""
+.run files extracted into tests/golden).  Pins the oracle before the CUDA path
+is tested against it."""
 import numpy as np
 import pytest
 
