@@ -167,10 +167,39 @@ def _parse_deck(path):
     mat_holder = list(blk.find("small_strain_material_3D") if blk.find("small_strain_material_3D") is not None
                       else blk.find("large_strain_material_3D"))[0]
     d["material"] = parse_material(mat_holder)
-    sol = root.find("nonlinear_solver")
-    d["solver"] = {"rel_tol": float(sol.get("rel_tolerance")), "abs_tol": float(sol.get("abs_tolerance")),
-                   "max_its": int(sol.get("max_iterations")), "div_tol": float(sol.get("divergence_tolerance"))}
+    sol = solver_element(root)
+    d["solver"] = {"rel_tol": float(sol.get("rel_tolerance", "1.0e-12")),
+                   "abs_tol": float(sol.get("abs_tolerance", "1.0e-12")),
+                   "max_its": int(sol.get("max_iterations", "1" if sol.tag.startswith("linear") else "25")),
+                   "div_tol": float(sol.get("divergence_tolerance", "1.0e+10")),
+                   "type": sol.tag, "matrix": solver_matrix(sol)}
     return d
+
+
+# Solver names of the reference's solver factory (SolverT_factory.cpp:18-28).
+# On the GPU path every one of them is served by the GPU Newton driver with
+# the GPU global matrix (block CSR, PCG): the converged field is the same,
+# so the deck's tolerances and iteration limits are kept and only the
+# algorithm that reaches the field changes.
+SOLVER_TYPES = ("linear_solver", "nonlinear_solver", "newton_krylov_solver", "PCG_solver", "nonlinear_solver_LS",
+                "linear_solver_RS")
+
+
+def solver_element(root):
+    for name in SOLVER_TYPES:
+        el = root.find(name)
+        if el is not None:
+            return el
+    raise ValueError("deck has no solver (one of %s)" % ", ".join(SOLVER_TYPES))
+
+
+def solver_matrix(sol):
+    """Name of the global matrix chosen under the solver (profile_matrix,
+    diagonal_matrix, SPOOLES_matrix, ...; SolverT.cpp:577-700), or None."""
+    for child in sol:
+        if child.tag.endswith("_matrix"):
+            return child.tag
+    return None
 
 
 def parse_material(m):
@@ -239,7 +268,7 @@ class Deck:
                      int(k.get("schedule", "1"))) for k in fld.findall("force_BC")]
         self.tractions = d["tractions"]
         self.solver = d["solver"]
-        sol = root.find("nonlinear_solver")
+        sol = solver_element(root)
         self.quick_solve_iter = int(sol.get("quick_solve_iter", "6"))
         self.quick_solve_count = int(sol.get("quick_solve_count", "3"))
 

@@ -40,6 +40,12 @@ DECKS = [
      ["benchmark/mat.1.a.io0.run"]),
     ("mat02_fsstvenant_cube", "level.1/material.solid/3D/material.02/mat.2.a.xml",
      ["benchmark/mat.2.a.io0.run"]),
+    # the same beam with the other solver / matrix choices of the deck
+    ("beam_pcg_diagonal", "level.0/3D.elastostatic/beam.PCG.xml", ["benchmark/beam.PCG.io0.run"]),
+    ("beam_pcg_profile", "level.0/3D.elastostatic/beam.PCG.K.xml", ["benchmark/beam.PCG.K.io0.run"]),
+    ("beam_quasi_newton", "level.0/3D.elastostatic/beam.quasi-Newton.xml", ["benchmark/beam.quasi-Newton.io0.run"]),
+    ("beam_newton_totlag_store", "level.0/3D.elastostatic/beam.Newton.TotLag.store.xml",
+     ["benchmark/beam.Newton.TotLag.store.io0.run"]),
 ]
 
 

@@ -12,6 +12,10 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GOLDEN_NAMES = ["mat08_j2_cube", "mat24_hookean_cube", "mat05_simo_cube", "traction_a_cube",
                 "beam_newton_totlag", "beam_newton_updlag", "beam_bbar", "mat01_ssstvenant_cube",
                 "mat02_fsstvenant_cube"]
+# the beam with the deck's other solver / matrix choices (nonlinear PCG with a
+# diagonal or profile matrix, quasi-Newton, stored shape functions): the
+# reference's outputs of the same field reached by other algorithms
+SOLVER_CHOICE_NAMES = ["beam_pcg_diagonal", "beam_pcg_profile", "beam_quasi_newton", "beam_newton_totlag_store"]
 
 
 def load_fixture(name):

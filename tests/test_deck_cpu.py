@@ -49,3 +49,19 @@ def test_run_file_round_trip(tmp_path):
         assert b["time"] == t
         assert b["labels"] == ["D_X", "D_Y", "D_Z", "s11", "s22", "s33", "s23", "s13", "s12", "alpha", "VM", "press"]
         assert np.allclose(np.array(b["rows"]), np.hstack([u, s, mo]), rtol=1e-11, atol=1e-300)
+
+
+def test_every_solver_type_of_the_reference_factory_is_accepted():
+    """Each solver name the reference's solver factory registers is read with
+    its tolerances and matrix choice; the GPU Newton driver serves them all."""
+    import xml.etree.ElementTree as ET
+    for name in dk.SOLVER_TYPES:
+        root = ET.fromstring('<tahoe><%s abs_tolerance="1e-9" rel_tolerance="1e-11" max_iterations="7" '
+                             'divergence_tolerance="5"><SPOOLES_matrix/></%s></tahoe>' % (name, name))
+        sol = dk.solver_element(root)
+        assert sol.tag == name and dk.solver_matrix(sol) == "SPOOLES_matrix"
+    try:
+        dk.solver_element(ET.fromstring("<tahoe/>"))
+        raise AssertionError("a deck without a solver is rejected")
+    except ValueError:
+        pass

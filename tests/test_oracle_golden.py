@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle.pyoracle import J2_PLASTIC, J2_RESET, model_from_fixture
-from tests.helpers import GOLDEN_NAMES, golden_displacements, load_fixture, rel_err
+from tests.helpers import GOLDEN_NAMES, SOLVER_CHOICE_NAMES, golden_displacements, load_fixture, rel_err
 
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
@@ -94,3 +94,24 @@ def test_oracle_pcg_matches_direct_solve():
         for j in range(bindx[r], bindx[r + 1]):
             A[r, bindx[j]] = A[bindx[j], r] = val[j]
     assert np.allclose(A @ x, R, rtol=0, atol=1e-12 * np.abs(R).max())
+
+
+@pytest.mark.parametrize("name", SOLVER_CHOICE_NAMES)
+def test_oracle_newton_reaches_the_field_of_other_solver_choices(name):
+    """Decks that select nonlinear PCG (diagonal or profile matrix),
+    quasi-Newton or stored shape functions: full Newton reaches the same
+    displacements and output stresses, within the deck's own solver tolerance
+    (rel 1e-12 on the residual; the golden files print 13 digits)."""
+    fx = load_fixture(name)
+    sv = fx["solver"]
+    assert sv["type"] in ("nonlinear_solver", "PCG_solver") and sv["matrix"] in ("diagonal_matrix", "profile_matrix")
+    m = model_from_fixture(fx)
+    status, uh, its, cuts, sh = m.run_cuts(fx["nsteps"], fx["dt"], sv["rel_tol"], sv["abs_tol"], 25, sv["div_tol"], 0,
+                                           want_stress=True)
+    assert status == 0 and cuts == 0
+    for step, ref in golden_displacements(fx).items():
+        assert rel_err(uh[step], ref) < 1e-10, (name, step)
+    for o in fx["outputs"]:
+        step = int(round(o["time"] / fx["dt"])) - 1
+        ref = np.array(o["rows"])[:, o["labels"].index("s11"):o["labels"].index("s12") + 1]
+        assert rel_err(sh[step], ref) < 1e-10, (name, step)
