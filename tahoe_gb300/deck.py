@@ -202,6 +202,16 @@ def solver_matrix(sol):
     return None
 
 
+def _e_nu(en):
+    """Young's modulus and Poisson's ratio of an E_and_nu entry, rejected as
+    IsotropicT::Set_E_nu rejects them (IsotropicT.cpp:32-44): E < 0 or nu
+    outside [-1, 0.5]."""
+    E, nu = float(en.get("Young_modulus")), float(en.get("Poisson_ratio"))
+    if E < 0.0 or nu > 0.5 or nu < -1.0:
+        raise ValueError("E_and_nu out of range: E=%g nu=%g" % (E, nu))
+    return E, nu
+
+
 def parse_material(m):
     name = m.tag
     en = m.find("E_and_nu")
@@ -218,21 +228,24 @@ def parse_material(m):
                     C[j][i] = float(v)
         return {"kind": "ss_hookean", "C": C}
     if name == "small_strain_StVenant":
-        return {"kind": "ss_hookean", "E": float(en.get("Young_modulus")), "nu": float(en.get("Poisson_ratio"))}
+        E, nu = _e_nu(en)
+        return {"kind": "ss_hookean", "E": E, "nu": nu}
     if name == "small_strain_StVenant_J2":
         lf = m.find("linear_function")
-        return {"kind": "ss_j2", "E": float(en.get("Young_modulus")), "nu": float(en.get("Poisson_ratio")),
+        E, nu = _e_nu(en)
+        return {"kind": "ss_j2", "E": E, "nu": nu,
                 "a": float(lf.get("a")), "b": float(lf.get("b")),
                 "elastic_iterations": int(m.get("elastic_iterations", "0"))}
     if name == "Simo_isotropic":
         if en is not None:
-            E, nu = float(en.get("Young_modulus")), float(en.get("Poisson_ratio"))
+            E, nu = _e_nu(en)
             mu = 0.5 * E / (1.0 + nu)
             lam = 2.0 * mu * nu / (1.0 - 2.0 * nu)
             return {"kind": "fs_simo", "mu": mu, "kappa": lam + 2.0 / 3.0 * mu}
         return {"kind": "fs_simo", "mu": float(bs.get("shear_modulus")), "kappa": float(bs.get("bulk_modulus"))}
     if name == "large_strain_StVenant":
-        return {"kind": "fs_stvenant", "E": float(en.get("Young_modulus")), "nu": float(en.get("Poisson_ratio"))}
+        E, nu = _e_nu(en)
+        return {"kind": "fs_stvenant", "E": E, "nu": nu}
     raise ValueError("unsupported material " + name)
 
 

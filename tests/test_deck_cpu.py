@@ -65,3 +65,25 @@ def test_every_solver_type_of_the_reference_factory_is_accepted():
         raise AssertionError("a deck without a solver is rejected")
     except ValueError:
         pass
+
+
+def test_isotropic_constants_follow_the_reference_unit_tests():
+    """The relations the reference's tests/materials/test_IsotropicT.cpp
+    checks: mu = E/(2(1+nu)), lambda = 2 mu nu/(1-2nu), E = 9 kappa mu /
+    (3 kappa + mu); negative E and nu above 0.5 rejected."""
+    import xml.etree.ElementTree as ET
+    simo = dk.parse_material(ET.fromstring(
+        '<Simo_isotropic><E_and_nu Young_modulus="200.0e9" Poisson_ratio="0.3"/></Simo_isotropic>'))
+    mu = 200.0e9 / (2.0 * 1.3)
+    lam = 2.0 * mu * 0.3 / (1.0 - 0.6)
+    assert abs(simo["mu"] - mu) <= 1.0
+    assert abs(simo["kappa"] - (lam + 2.0 / 3.0 * mu)) <= 1.0
+    E = 9.0 * simo["kappa"] * simo["mu"] / (3.0 * simo["kappa"] + simo["mu"])
+    assert abs(E - 200.0e9) <= 1.0e3
+    for E_, nu_ in ((-1.0, 0.3), (100.0, 0.6)):
+        try:
+            dk.parse_material(ET.fromstring('<small_strain_StVenant><E_and_nu Young_modulus="%g" '
+                                            'Poisson_ratio="%g"/></small_strain_StVenant>' % (E_, nu_)))
+            raise AssertionError("E=%g nu=%g accepted" % (E_, nu_))
+        except ValueError:
+            pass
