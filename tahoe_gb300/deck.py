@@ -202,6 +202,20 @@ def solver_matrix(sol):
     return None
 
 
+def _modulus_6x6(c):
+    """The 6x6 modulus of a modulus_6x6 entry (C_i_j attributes, 1-based,
+    mirrored when copy_symmetric is true)."""
+    C = [[0.0] * 6 for _ in range(6)]
+    for k, v in c.attrib.items():
+        mm = re.match(r"C_(\d)_(\d)", k)
+        if mm:
+            i, j = int(mm.group(1)) - 1, int(mm.group(2)) - 1
+            C[i][j] = float(v)
+            if c.get("copy_symmetric", "false") == "true":
+                C[j][i] = float(v)
+    return C
+
+
 def _e_nu(en):
     """Young's modulus and Poisson's ratio of an E_and_nu entry, rejected as
     IsotropicT::Set_E_nu rejects them (IsotropicT.cpp:32-44): E < 0 or nu
@@ -217,16 +231,7 @@ def parse_material(m):
     en = m.find("E_and_nu")
     bs = m.find("bulk_and_shear")
     if name == "small_strain_Hookean":
-        c = m.find("modulus_6x6")
-        C = [[0.0] * 6 for _ in range(6)]
-        for k, v in c.attrib.items():
-            mm = re.match(r"C_(\d)_(\d)", k)
-            if mm:
-                i, j = int(mm.group(1)) - 1, int(mm.group(2)) - 1
-                C[i][j] = float(v)
-                if c.get("copy_symmetric", "false") == "true":
-                    C[j][i] = float(v)
-        return {"kind": "ss_hookean", "C": C}
+        return {"kind": "ss_hookean", "C": _modulus_6x6(m.find("modulus_6x6"))}
     if name == "small_strain_StVenant":
         E, nu = _e_nu(en)
         return {"kind": "ss_hookean", "E": E, "nu": nu}
@@ -245,6 +250,19 @@ def parse_material(m):
         return {"kind": "fs_simo", "mu": float(bs.get("shear_modulus")), "kappa": float(bs.get("bulk_modulus"))}
     if name == "large_strain_StVenant":
         E, nu = _e_nu(en)
+        return {"kind": "fs_stvenant", "E": E, "nu": nu}
+    if name == "large_strain_Hookean":
+        # FDHookeanMatT (FDHookeanMatT.cpp:39-55): S = C : E(Green), pushed
+        # forward: the St.Venant-Kirchhoff law; an isotropic modulus is
+        # lambda = C_12, mu = C_44
+        C = _modulus_6x6(m.find("modulus_6x6"))
+        lam, mu = C[0][1], C[3][3]
+        iso = [[(lam + 2.0 * mu if i == j else lam) if i < 3 and j < 3 else (mu if i == j else 0.0)
+                for j in range(6)] for i in range(6)]
+        if any(abs(C[i][j] - iso[i][j]) > 1e-12 * max(abs(lam), abs(mu)) for i in range(6) for j in range(6)):
+            raise ValueError("large_strain_Hookean: only an isotropic modulus_6x6 is supported")
+        E = mu * (3.0 * lam + 2.0 * mu) / (lam + mu)
+        nu = lam / (2.0 * (lam + mu))
         return {"kind": "fs_stvenant", "E": E, "nu": nu}
     raise ValueError("unsupported material " + name)
 

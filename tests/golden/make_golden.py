@@ -40,6 +40,8 @@ DECKS = [
      ["benchmark/mat.1.a.io0.run"]),
     ("mat02_fsstvenant_cube", "level.1/material.solid/3D/material.02/mat.2.a.xml",
      ["benchmark/mat.2.a.io0.run"]),
+    ("mat25_fshookean_cube", "level.1/material.solid/3D/material.25/mat.25.a.xml",
+     ["benchmark/mat.25.a.io0.run.ps0000", "benchmark/mat.25.a.io0.run.ps0001"]),
     # the same beam with the other solver / matrix choices of the deck
     ("beam_pcg_diagonal", "level.0/3D.elastostatic/beam.PCG.xml", ["benchmark/beam.PCG.io0.run"]),
     ("beam_pcg_profile", "level.0/3D.elastostatic/beam.PCG.K.xml", ["benchmark/beam.PCG.K.io0.run"]),

@@ -87,3 +87,18 @@ def test_isotropic_constants_follow_the_reference_unit_tests():
             raise AssertionError("E=%g nu=%g accepted" % (E_, nu_))
         except ValueError:
             pass
+
+
+def test_large_strain_hookean_reads_as_st_venant_or_is_rejected():
+    """An isotropic modulus_6x6 (C11 = lambda + 2 mu, C12 = lambda, C44 = mu)
+    becomes the St.Venant-Kirchhoff material; any other modulus is refused."""
+    import xml.etree.ElementTree as ET
+    iso = ('<large_strain_Hookean><modulus_6x6 C_1_1="30.0" C_1_2="10.0" C_1_3="10.0" C_2_2="30.0" C_2_3="10.0" '
+           'C_3_3="30.0" C_4_4="10.0" C_5_5="10.0" C_6_6="10.0" copy_symmetric="true"/></large_strain_Hookean>')
+    m = dk.parse_material(ET.fromstring(iso))
+    assert m == {"kind": "fs_stvenant", "E": 25.0, "nu": 0.25}
+    try:
+        dk.parse_material(ET.fromstring(iso.replace('C_4_4="10.0"', 'C_4_4="12.0"')))
+        raise AssertionError("anisotropic modulus accepted")
+    except ValueError:
+        pass

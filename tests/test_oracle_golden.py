@@ -5,10 +5,11 @@ import numpy as np
 import pytest
 
 from oracle.pyoracle import J2_PLASTIC, J2_RESET, model_from_fixture
-from tests.helpers import GOLDEN_NAMES, SOLVER_CHOICE_NAMES, golden_displacements, load_fixture, rel_err
+from tests.helpers import (GOLDEN_NAMES, ORACLE_EXTRA_NAMES, SOLVER_CHOICE_NAMES, golden_displacements, load_fixture,
+                           rel_err)
 
 
-@pytest.mark.parametrize("name", GOLDEN_NAMES)
+@pytest.mark.parametrize("name", GOLDEN_NAMES + ORACLE_EXTRA_NAMES)
 def test_oracle_reproduces_golden_displacements(name):
     fx = load_fixture(name)
     m = model_from_fixture(fx)
@@ -20,7 +21,7 @@ def test_oracle_reproduces_golden_displacements(name):
         assert rel_err(uh[step], ref) < 1e-11, (name, step)
 
 
-@pytest.mark.parametrize("name", GOLDEN_NAMES)
+@pytest.mark.parametrize("name", GOLDEN_NAMES + ORACLE_EXTRA_NAMES)
 def test_oracle_nodal_stress_matches_golden(name):
     """Output stresses (integration-point Cauchy stress extrapolated to the
     nodes and averaged over elements) against the .run files' s11..s12."""
