@@ -286,6 +286,15 @@ struct KBC {
   int node, dof;
   double value;
   bool scheduled;
+  int torsion = -1;  /* >= 0: the dof follows torsion controller [torsion] */
+};
+/* TorsionKBCT (TorsionKBCT.cpp:39-99, 148-180): the nodes turn rigidly about
+ * an axis through `point` by theta = rate * t; the two dofs across the axis
+ * are prescribed, the one along it is free. */
+struct Torsion {
+  int axis;
+  double rate;
+  double point[3];
 };
 struct Force {
   int node, dof;
@@ -306,6 +315,7 @@ struct Model {
   std::vector<Material> mats;
   std::vector<double> sx, sy; /* schedule */
   std::vector<KBC> kbc;
+  std::vector<Torsion> torsions;
   std::vector<Force> forces;
   std::vector<Traction> tractions;
   int nthreads = 1;
@@ -882,6 +892,20 @@ int orc_set_schedule(void* m, int n, const double* x, const double* y) {
   M->sy.assign(y, y + n);
   return 0;
 }
+int orc_add_torsion(void* m, int axis, double rate, const double* point, int nnodes, const int* nodes) {
+  Model* M = static_cast<Model*>(m);
+  if (axis < 0 || axis > 2 || nnodes < 0) return -1;
+  const int t = (int)M->torsions.size();
+  M->torsions.push_back({axis, rate, {point[0], point[1], point[2]}});
+  const int across[3][2] = {{1, 2}, {2, 0}, {0, 1}};  /* the dofs turned about each axis */
+  for (int i = 0; i < nnodes; ++i)
+    for (int j = 0; j < 2; ++j) {
+      KBC k{nodes[i], across[axis][j], 0.0, false};
+      k.torsion = t;
+      M->kbc.push_back(k);
+    }
+  return 0;
+}
 int orc_add_kbc(void* m, int node, int dof, double value, int scheduled) {
   static_cast<Model*>(m)->kbc.push_back({node, dof, value, scheduled != 0});
   return 0;
@@ -945,6 +969,42 @@ int orc_pcg(void* m, const double* val, const double* b, double* x, double tol, 
   return pcg(*M, val, b, x, tol, maxit, relres);
 }
 
+/* Prescribed displacements at the start of the step ending at time t
+ * (FieldT::InitStep): schedule x value for ordinary cards; for torsion cards
+ * the rigid turn of the node's initial position (TorsionKBCT::InitStep), the
+ * in-plane radius vector rotated by theta = rate * t about the axis. */
+static void apply_kbc(Model& M, double t) {
+  const double sc = M.schedule(t);
+  for (const KBC& k : M.kbc) {
+    double v = k.scheduled ? sc * k.value : 0.0;
+    if (k.torsion >= 0) {
+      const Torsion& T = M.torsions[k.torsion];
+      double a[3] = {0.0, 0.0, 0.0};
+      a[T.axis] = 1.0;
+      const double* X = &M.X[(size_t)k.node * 3];
+      double d[3], r[3];
+      for (int i = 0; i < 3; ++i) d[i] = X[i] - T.point[i];
+      const double along = d[0] * a[0] + d[1] * a[1] + d[2] * a[2];
+      for (int i = 0; i < 3; ++i) r[i] = d[i] - along * a[i];
+      const double rad = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      v = 0.0;
+      if (std::fabs(rad) > 1.0e-12) {
+        const double th = T.rate * t;
+        double e1[3], e2[3];
+        for (int i = 0; i < 3; ++i) e1[i] = r[i] / rad;
+        e2[0] = a[1] * e1[2] - a[2] * e1[1];
+        e2[1] = a[2] * e1[0] - a[0] * e1[2];
+        e2[2] = a[0] * e1[1] - a[1] * e1[0];
+        /* new position: the foot on the axis plus the turned radius */
+        const int i = k.dof;
+        const double x = (X[i] - r[i]) + rad * std::cos(th) * e1[i] + rad * std::sin(th) * e2[i];
+        v = x - X[i];
+      }
+    }
+    M.u[(size_t)k.node * 3 + k.dof] = v;
+  }
+}
+
 /* NLSolver::Solve (NLSolver.cpp:57-262) + ExitIteration (:675-755) over load
  * steps; prescribed displacements applied at step start (FieldT::InitStep);
  * J2 history closed after each converged step (ContinuumElementT::CloseStep). */
@@ -956,8 +1016,7 @@ int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int 
   std::vector<double> R(n), du(n), val(M->bindx.size());
   for (int step = 1; step <= nsteps; ++step) {
     double t = step * dt;
-    double sc = M->schedule(t);
-    for (const KBC& k : M->kbc) M->u[k.node * 3 + k.dof] = k.scheduled ? sc * k.value : 0.0;
+    apply_kbc(*M, t);
     int iteration = -1;
     if (form(*M, M->u.data(), t, iteration, R.data(), nullptr)) return step;
     double err0 = 0;
@@ -1035,8 +1094,7 @@ int newton_step(Model* M, double t, double rel_tol, double abs_tol, int max_its,
                 double lin_tol, int* its_out) {
   const int n = M->neq;
   std::vector<double> R(n), du(n), val(M->bindx.size());
-  const double sc = M->schedule(t);
-  for (const KBC& k : M->kbc) M->u[k.node * 3 + k.dof] = k.scheduled ? sc * k.value : 0.0;
+  apply_kbc(*M, t);
   int iteration = -1, its = 0;
   *its_out = 0;
   if (form(*M, M->u.data(), t, iteration, R.data(), nullptr)) return 1;

@@ -50,6 +50,9 @@ int orc_set_material(void* m, int block, int kind, const double* p, int np);
 int orc_set_element_blocks(void* m, const int* block_of_element);
 int orc_set_schedule(void* m, int npts, const double* x, const double* y);
 int orc_add_kbc(void* m, int node, int dof, double value, int scheduled);
+/* rigid turn of `nodes` about coordinate axis `axis` (0..2) through `point`,
+ * theta = rate * t (TorsionKBCT) */
+int orc_add_torsion(void* m, int axis, double rate, const double* point, int nnodes, const int* nodes);
 int orc_add_force(void* m, int node, int dof, double value);
 int orc_add_traction(void* m, int elem, int facet, const double* t3);
 int orc_set_threads(void* m, int nthreads);

@@ -35,6 +35,7 @@ def lib():
             ("orc_set_element_blocks", [_ip]),
             ("orc_set_schedule", [ctypes.c_int, _dp, _dp]),
             ("orc_add_kbc", [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+            ("orc_add_torsion", [ctypes.c_int, ctypes.c_double, _dp, ctypes.c_int, _ip]),
             ("orc_add_force", [ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             ("orc_add_traction", [ctypes.c_int, ctypes.c_int, _dp]),
             ("orc_set_threads", [ctypes.c_int]),
@@ -125,6 +126,14 @@ class OracleModel:
 
     def add_kbc(self, node, dof, value=0.0, scheduled=False):
         lib().orc_add_kbc(self.h, int(node), int(dof), float(value), int(bool(scheduled)))
+
+    def add_torsion(self, axis, rate, point, nodes):
+        """Rigid turn of `nodes` about coordinate axis `axis` (0..2) through
+        `point` by rate * t (the reference's torsion controller)."""
+        pt = np.ascontiguousarray(point, dtype=np.float64)
+        nd = np.ascontiguousarray(nodes, dtype=np.int32)
+        if lib().orc_add_torsion(self.h, int(axis), float(rate), _d(pt), len(nd), _i(nd)) != 0:
+            raise ValueError("torsion axis must be 0, 1 or 2")
 
     def add_force(self, node, dof, value):
         lib().orc_add_force(self.h, int(node), int(dof), float(value))
@@ -243,6 +252,8 @@ def model_from_fixture(fx, threads=1):
     m.set_schedule(fx["schedule"])
     for n, d, v, s in fx["kbc"]:
         m.add_kbc(n, d, v, s)
+    for axis, rate, px, py, pz, nodes in fx.get("torsion", []):
+        m.add_torsion(axis, rate, [px, py, pz], nodes)
     for n, d, v in fx.get("forces", []):
         m.add_force(n, d, v)
     for row in fx.get("tractions", []):

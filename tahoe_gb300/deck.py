@@ -154,6 +154,14 @@ def _parse_deck(path):
                 for k in fld.findall("kinematic_BC")]
     d["fbc"] = [{"dof": int(k.get("dof")) - 1, "set": int(k.get("node_ID")),
                  "value": float(k.get("value", "0.0"))} for k in fld.findall("force_BC")]
+    # torsion controller (TorsionKBCT.cpp:139-160): rigid turn of node sets
+    # about a coordinate axis through a point, angle rotation_rate * t
+    d["torsion"] = []
+    for t in fld.findall("torsion"):
+        pt = t.find("point_on_axis")
+        d["torsion"].append({"axis": int(t.get("rotation_axis")) - 1, "rate": float(t.get("rotation_rate")),
+                             "point": [float(pt.get("x_1")), float(pt.get("x_2")), float(pt.get("x_3"))],
+                             "sets": [int(v.get("value")) for v in t.findall("node_ID_list/String")]})
     el = list(root.find("element_list"))[0]
     d["element"] = el.tag
     d["strain_displacement"] = el.get("strain_displacement", "standard")
@@ -298,6 +306,7 @@ class Deck:
         self.fbc = [(int(k.get("dof")) - 1, int(k.get("node_ID")), float(k.get("value", "0.0")),
                      int(k.get("schedule", "1"))) for k in fld.findall("force_BC")]
         self.tractions = d["tractions"]
+        self.torsion = d["torsion"]
         self.solver = d["solver"]
         sol = solver_element(root)
         self.quick_solve_iter = int(sol.get("quick_solve_iter", "6"))
@@ -309,6 +318,8 @@ class Deck:
 
     def model(self, device=0):
         """The deck as a GPU SolidModel (not yet set up)."""
+        if self.torsion:
+            raise ValueError("torsion boundary controller: not on the GPU step loop")
         m = SolidModel(self.X, self.conn, self.formulation, self.material, device=device,
                        strain_displacement=self.strain_displacement)
         for k, pts in self.schedules.items():

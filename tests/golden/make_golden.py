@@ -48,6 +48,10 @@ DECKS = [
     ("beam_quasi_newton", "level.0/3D.elastostatic/beam.quasi-Newton.xml", ["benchmark/beam.quasi-Newton.io0.run"]),
     ("beam_newton_totlag_store", "level.0/3D.elastostatic/beam.Newton.TotLag.store.xml",
      ["benchmark/beam.Newton.TotLag.store.io0.run"]),
+    # finite rotations: one end of two stacked cubes turned about z (y) by
+    # the torsion controller, the other end pinned
+    ("torsion_z", "level.2/torsion/torsion.z.xml", ["benchmark/torsion.z.io0.run"]),
+    ("torsion_y", "level.2/torsion/torsion.y.xml", ["benchmark/torsion.y.io0.run"]),
 ]
 
 
@@ -66,6 +70,10 @@ def make(ref_root):
         for k in d["kbc"]:
             for n in nodesets[k["set"]]:
                 kbc.append([n, k["dof"], k["value"], int(k["scheduled"])])
+        torsion = []
+        for t in d["torsion"]:
+            nodes = sorted({n for ns in t["sets"] for n in nodesets[ns]})
+            torsion.append([t["axis"], t["rate"]] + t["point"] + [nodes])
         forces = []
         for f in d["fbc"]:
             for n in nodesets[f["set"]]:
@@ -86,7 +94,7 @@ def make(ref_root):
             "formulation": form,
             "X": X, "conn": conn,
             "material": d["material"],
-            "kbc": kbc, "forces": forces, "tractions": tractions,
+            "kbc": kbc, "forces": forces, "tractions": tractions, "torsion": torsion,
             "schedule": d["schedule"], "nsteps": d["nsteps"], "dt": d["dt"],
             "solver": d["solver"],
             "outputs": outputs,

@@ -16,10 +16,10 @@ GOLDEN_NAMES = ["mat08_j2_cube", "mat24_hookean_cube", "mat05_simo_cube", "tract
 # diagonal or profile matrix, quasi-Newton, stored shape functions): the
 # reference's outputs of the same field reached by other algorithms
 SOLVER_CHOICE_NAMES = ["beam_pcg_diagonal", "beam_pcg_profile", "beam_quasi_newton", "beam_newton_totlag_store"]
-# decks read into the same materials under another name (large_strain_Hookean
-# with an isotropic modulus is the St.Venant-Kirchhoff law), pinned on the
-# oracle
-ORACLE_EXTRA_NAMES = ["mat25_fshookean_cube"]
+# decks pinned on the oracle only: a material read under another name
+# (large_strain_Hookean with an isotropic modulus is the St.Venant-Kirchhoff
+# law) and finite rotations driven by the torsion boundary controller
+ORACLE_EXTRA_NAMES = ["mat25_fshookean_cube", "torsion_z", "torsion_y"]
 
 
 def load_fixture(name):

@@ -102,3 +102,25 @@ def test_large_strain_hookean_reads_as_st_venant_or_is_rejected():
         raise AssertionError("anisotropic modulus accepted")
     except ValueError:
         pass
+
+
+def test_torsion_controller_is_read_and_refused_by_the_gpu_step_loop(tmp_path):
+    """A deck with the reference's torsion controller: the axis, rate, point
+    and node sets are read (the oracle runs it); the GPU step loop refuses
+    it explicitly rather than dropping the rotation."""
+    import shutil
+    with open(os.path.join(DECKS, "cube8_j2.xml")) as f:
+        xml = f.read()
+    shutil.copy(os.path.join(DECKS, "cube8.geom"), tmp_path / "cube8.geom")
+    tors = ('<torsion rotation_axis="3" rotation_rate="0.5"><point_on_axis x_1="0.5" x_2="0.5" x_3="0.0"/>'
+            '<node_ID_list><String value="2"/></node_ID_list></torsion>')
+    xml = xml.replace("</field>", tors + "</field>", 1)
+    path = tmp_path / "torsion.xml"
+    path.write_text(xml)
+    d = dk.Deck(str(path))
+    assert d.torsion == [{"axis": 2, "rate": 0.5, "point": [0.5, 0.5, 0.0], "sets": [2]}]
+    try:
+        d.model()
+        raise AssertionError("torsion deck accepted by the GPU step loop")
+    except ValueError:
+        pass
