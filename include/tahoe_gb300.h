@@ -159,8 +159,11 @@ int tg_apply_update(tg_context* ctx);
  * partial sums and scalars live in one static device array of 8 MiB held by
  * every GPU that loads the library, which limits the mesh to 32,768 nodes
  * (larger meshes get TG_ERR_CAPACITY).  The first call on a device looks up
- * that array's address, so make it before any stream capture.  All calls on a
- * device share the array: calls that overlap on the GPU race. */
+ * that array's address, so make it before any stream capture; the address is
+ * cached per device for the life of the process and assumes the device's
+ * primary context (do not call it after cudaDeviceReset or under another
+ * driver context).  All calls on a device share the array: calls that overlap
+ * on the GPU race. */
 int tg_pcg_solve_noalloc(tg_context* ctx, const double* rhs_device, double* du_device, double rel_tol, int max_it,
                          int precond, int* iterations, double* rel_res);
 

@@ -34,6 +34,7 @@ void free_device(Context* c) {
   // the caller's timer events outlive mesh changes (a timed region may
   // cover composing a batch mesh)
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
+  c->ckpt_valid = false;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
   for (void* p : c->allocations) cudaFreeAsync(p, c->stream);
@@ -49,6 +50,7 @@ void free_all(Context* c) {
     e = nullptr;
   }
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
+  c->ckpt_valid = false;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
   for (void* p : c->allocations) cudaFreeAsync(p, c->stream);
@@ -244,7 +246,9 @@ int tg_create(tg_context** out, int device) {
     }
     cudaGetLastError();
   }
-  if (set_device(c) || !ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
+  if (set_device(c) ||
+      !ok(c, cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device), "multiprocessor count") ||
+      !ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
       !ok(c, cudaMallocHost((void**)&c->h_pcg, 2 * sizeof(PcgScalars)), "pinned") ||
       !ok(c, cudaEventCreateWithFlags(&c->ev_poll[0], cudaEventDisableTiming), "event") ||
       !ok(c, cudaEventCreateWithFlags(&c->ev_poll[1], cudaEventDisableTiming), "event") ||

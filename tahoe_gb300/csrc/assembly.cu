@@ -205,7 +205,7 @@ __global__ void blob_structure_kernel(int ntiles, const int* __restrict__ tile_r
 
 int launch_blob_structure(Context* c, int precision) {
   const bool f32 = precision == TG_MIXED;
-  const int grid = std::min(c->ntiles, kNumSMs * 16);
+  const int grid = std::min(c->ntiles, c->num_sms * 16);
   blob_structure_kernel<<<std::max(grid, 1), 128, 0, c->stream>>>(c->ntiles, c->d_tile_row, c->d_rowptr, c->d_col,
                                                                   f32 ? c->d_blob_off32 : c->d_blob_off64,
                                                                   f32 ? 4 : 8, f32 ? c->d_blob32 : c->d_blob64);
@@ -225,7 +225,7 @@ int launch_assemble(Context* c, int precision) {
           "occupancy"))
     return TG_ERR_CUDA;
   int grid = (c->nnd + warps_per_block - 1) / warps_per_block;
-  grid = std::max(1, std::min(grid, kNumSMs * std::max(per_sm, 1)));
+  grid = std::max(1, std::min(grid, c->num_sms * std::max(per_sm, 1)));
   if (precision == TG_MIXED)
     assemble_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_col, c->d_contrib_ptr,
                                                         c->d_contrib, c->d_Ke32, c->d_mask, c->d_blob32,

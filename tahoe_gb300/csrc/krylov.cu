@@ -548,7 +548,7 @@ int spmv_config_n(Context* c, Grids& g) {
     c->err = "SpMV tile does not fit in shared memory";
     return TG_ERR_CAPACITY;
   }
-  g.spmv = std::max(1, std::min(c->ntiles, kNumSMs * per_sm));
+  g.spmv = std::max(1, std::min(c->ntiles, c->num_sms * per_sm));
   g.warp_release = c->spmv_warp_release;
   return TG_OK;
 }
@@ -593,7 +593,7 @@ cudaError_t launch_update(Context* c, int grid, const T* minv, void* x, void* r,
   int per_sm = 0;
   const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_update_kernel<T>, 256, 0);
   if (oe != cudaSuccess) return oe;
-  grid = std::max(1, std::min(grid, kNumSMs * per_sm));  // every CTA resident at once
+  grid = std::max(1, std::min(grid, c->num_sms * per_sm));  // every CTA resident at once
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(256);
@@ -613,7 +613,7 @@ Grids grids(const Context* c) {
   g.spmv = 0;
   g.spmv_smem = 0;
   g.stages = 8;
-  g.vec = std::min((c->nnd + 255) / 256, kNumSMs * 2);
+  g.vec = std::min((c->nnd + 255) / 256, c->num_sms * 2);
   return g;
 }
 
@@ -792,7 +792,7 @@ __global__ void gather_solution_kernel(int neq, const int* __restrict__ slot, co
 int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs, bool zero_base, int nvec) {
   const double4_32a* base = zero_base ? nullptr : c->d_R;
   Grids g = grids(c);
-  const dim3 grid(std::min((c->nnd + 7) / 8, kNumSMs * 8), nvec);
+  const dim3 grid(std::min((c->nnd + 7) / 8, c->num_sms * 8), nvec);
   if (c->tangent_precision == TG_MIXED)
     lift_rhs_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, c->d_row_tile, c->d_blob_off32,
                                                          c->d_blob32, d_v, base, d_rhs);

@@ -520,7 +520,7 @@ int mrhs_config(Context* c, size_t smem, int* grid) {
     c->err = "multi-vector SpMV does not fit on an SM";
     return TG_ERR_CAPACITY;
   }
-  *grid = std::max(1, std::min(c->ntiles, kNumSMs * per_sm));
+  *grid = std::max(1, std::min(c->ntiles, c->num_sms * per_sm));
   return TG_OK;
 }
 
@@ -541,13 +541,13 @@ int mrhs_solve_t(Context* c, const double4_32a* d_b, const double4_32a* d_v, dou
   const size_t smem = 2 * (size_t)cap;
   int s = mrhs_config<T, 2>(c, smem, &grid);
   if (s) return s;
-  const int vgrid = std::min((c->nnd + 255) / 256, kNumSMs * 2);            // scale pass (1-D)
+  const int vgrid = std::min((c->nnd + 255) / 256, c->num_sms * 2);            // scale pass (1-D)
   // the update is a cooperative launch: its kNG grid rows together fit at once
   int upd_per_sm = 0;
   if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&upd_per_sm, mrhs_update_kernel<T, kNR>, 256, 0),
           "occupancy"))
     return TG_ERR_CUDA;
-  const int ugrid = std::max(1, std::min((c->nnd + 255) / 256, kNumSMs * upd_per_sm / kNG));  // per group row
+  const int ugrid = std::max(1, std::min((c->nnd + 255) / 256, c->num_sms * upd_per_sm / kNG));  // per group row
   const size_t npart = (size_t)std::max({(long long)grid * kNR, (long long)vgrid * kNR, (long long)ugrid * kNR * 2});
   const size_t nv = (size_t)c->nnd * kNR;
   V *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;

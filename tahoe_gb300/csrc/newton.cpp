@@ -365,6 +365,9 @@ int tg_state_load(tg_context* c, const void* buf, long long bytes) {
     off += (q.bytes + 15) / 16 * 16;
   }
   c->have_du = false;
+  // the device snapshot predates the loaded state: a rollback must not bring
+  // it back (the caller checkpoints again once the residual is formed)
+  c->ckpt_valid = false;
   return ok(c, cudaStreamSynchronize(c->stream), "sync") ? TG_OK : TG_ERR_CUDA;
 }
 
@@ -697,14 +700,19 @@ int tg_checkpoint(tg_context* c) {
   if (!c->d_u_ckpt && (!dalloc(c, &c->d_u_ckpt, (size_t)c->nnd) || !dalloc(c, &c->d_R_ckpt, (size_t)c->nnd)))
     return TG_ERR_OOM;
   const size_t n = sizeof(double4_32a) * c->nnd;
-  return ok(c, cudaMemcpyAsync(c->d_u_ckpt, c->d_u, n, cudaMemcpyDeviceToDevice, c->stream), "ckpt") &&
-                 ok(c, cudaMemcpyAsync(c->d_R_ckpt, c->d_R, n, cudaMemcpyDeviceToDevice, c->stream), "ckpt")
-             ? TG_OK
-             : TG_ERR_CUDA;
+  if (!ok(c, cudaMemcpyAsync(c->d_u_ckpt, c->d_u, n, cudaMemcpyDeviceToDevice, c->stream), "ckpt") ||
+      !ok(c, cudaMemcpyAsync(c->d_R_ckpt, c->d_R, n, cudaMemcpyDeviceToDevice, c->stream), "ckpt"))
+    return TG_ERR_CUDA;
+  c->ckpt_valid = true;
+  return TG_OK;
 }
 
 int tg_rollback(tg_context* c) {
-  if (!c || !c->d_u_ckpt) return TG_ERR_ARG;
+  if (!c) return TG_ERR_ARG;
+  if (!c->d_u_ckpt || !c->ckpt_valid) {
+    c->err = "tg_rollback: no checkpoint of the current state (take one with tg_checkpoint)";
+    return TG_ERR_ARG;
+  }
   const size_t n = sizeof(double4_32a) * c->nnd;
   return ok(c, cudaMemcpyAsync(c->d_u, c->d_u_ckpt, n, cudaMemcpyDeviceToDevice, c->stream), "rollback") &&
                  ok(c, cudaMemcpyAsync(c->d_R, c->d_R_ckpt, n, cudaMemcpyDeviceToDevice, c->stream), "rollback")

@@ -30,7 +30,10 @@ void* g_addr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch array for the current device.  The host-side
 // name g_pcg_scratch is only a stand-in, so the address is looked up once per
-// device (with that device current) and cached.
+// device (with that device current) and cached.  The cache assumes the
+// device's primary context for the life of the process (the runtime API's
+// context): after a cudaDeviceReset, or when the caller makes another driver
+// context current, the cached address no longer names the array.
 int scratch_address(tg::Context* c, void** out) {
   if (c->device < 0 || c->device >= kMaxDevices) {
     c->err = "device index out of range for the no-allocation scratch table";

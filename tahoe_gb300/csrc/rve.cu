@@ -179,7 +179,7 @@ int launch_macro_combine(Context* c, const double4_32a* d_v, double4_32a* d_w) {
 
 int launch_segment_macro(Context* c, const double4_32a* d_w, int kL, int ncols, const double* d_vol0,
                          double* d_out) {
-  const dim3 grid(std::min(c->nseg, kNumSMs * 16), ncols);
+  const dim3 grid(std::min(c->nseg, c->num_sms * 16), ncols);
   if (c->tangent_precision == TG_MIXED)
     segment_macro_kernel<float><<<grid, 256, 0, c->stream>>>(c->nseg, c->d_seg_elem, c->d_conn, c->d_X, c->nnd,
                                                              c->d_Ke32, d_w, kL, d_vol0, d_out);
@@ -191,13 +191,13 @@ int launch_segment_macro(Context* c, const double4_32a* d_w, int kL, int ncols, 
 }
 
 int launch_segment_norms(Context* c, int nseg, const int* d_node_off, double* d_out) {
-  segment_norms_kernel<<<std::min(nseg, kNumSMs * 16), 256, 0, c->stream>>>(nseg, d_node_off, c->d_R, d_out);
+  segment_norms_kernel<<<std::min(nseg, c->num_sms * 16), 256, 0, c->stream>>>(nseg, d_node_off, c->d_R, d_out);
   c->launches++;
   return ok(c, cudaGetLastError(), "segment_norms_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
 int launch_segment_stress(Context* c, int nseg, const int* d_elem_off, double* d_out) {
-  segment_stress_kernel<<<std::min(nseg, kNumSMs * 16), 256, 0, c->stream>>>(nseg, d_elem_off, c->d_conn, c->d_X,
+  segment_stress_kernel<<<std::min(nseg, c->num_sms * 16), 256, 0, c->stream>>>(nseg, d_elem_off, c->d_conn, c->d_X,
                                                                               c->nnd, c->d_fint, d_out);
   c->launches++;
   return ok(c, cudaGetLastError(), "segment_stress_kernel") ? TG_OK : TG_ERR_CUDA;

@@ -13,7 +13,6 @@
 namespace tg {
 
 constexpr int kMaxBlocks = 4;      // material blocks per element group
-constexpr int kNumSMs = 152;       // GB300
 constexpr int kSlots = 36;         // upper-triangle node-pair blocks of a hex8 element
 // A staged 3x3 element block is three 4-value rows (the 4th value is zero
 // padding), so a row is one 16-byte (FP32) or 32-byte (FP64) aligned vector.
@@ -69,6 +68,7 @@ struct DevBuf {
 
 struct Context {
   int device = 0;
+  int num_sms = 1;  // multiprocessors of the device (grid sizing), queried at creation
   cudaStream_t stream = nullptr;
   std::string err;
   long long launches = 0;
@@ -181,6 +181,7 @@ struct Context {
   // step-start snapshot (tg_checkpoint / tg_rollback)
   double4_32a* d_u_ckpt = nullptr;
   double4_32a* d_R_ckpt = nullptr;
+  bool ckpt_valid = false;  // cleared when the state is replaced (tg_state_load, new mesh)
   // caller timer (tg_timer_start / tg_timer_stop)
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
 

@@ -10,7 +10,7 @@ tests/golden/:
   * the nodal results of every output step (from the committed ``.run`` /
     ``.run.psNNNN`` golden files of the reference suite).
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT   (the reference source tree)
 """
 import json
 import os
@@ -105,4 +105,6 @@ def make(ref_root):
 
 
 if __name__ == "__main__":
-    make(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference source tree>")
+    make(sys.argv[1])

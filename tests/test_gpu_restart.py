@@ -51,3 +51,19 @@ def test_mismatched_image_refused():
     image[0] ^= 0xFF
     with pytest.raises(lib.TahoeError):
         m.ctx.state_load(bytes(image))
+
+
+def test_rollback_after_load_is_refused():
+    """A device snapshot taken before tg_state_load predates the loaded state:
+    rolling back to it after the load is refused until a new checkpoint."""
+    d = dk.Deck(DECK)
+    m = d.model()
+    _run(m, d, 1, 1)
+    image = m.ctx.state_save()
+    m.ctx.checkpoint()
+    m.ctx.state_load(image)
+    with pytest.raises(lib.TahoeError) as e:
+        m.ctx.rollback()
+    assert e.value.code == -1
+    m.ctx.checkpoint()
+    m.ctx.rollback()
