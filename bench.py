@@ -1,27 +1,38 @@
 """Benchmark of the GB300 hex8 implicit path.
 
-Workload (configuration 2 of the benchmark set): total-Lagrangian compressible
-neo-Hookean block, 64^3 hex8 (274,625 nodes, 823,875 dofs), mu=1, kappa=10,
-interior nodes jittered +-0.2h (seed 0), bottom fixed, top compressed 1% in the
-first of 10 load steps.  Synthetic, seeded input (no dataset exists).
+Headline workload (configuration 2 of the benchmark set): total-Lagrangian
+compressible neo-Hookean block, 64^3 hex8 (274,625 nodes, 823,875 dofs),
+mu=1, kappa=10, interior nodes jittered +-0.2h (seed 0), bottom fixed, top
+compressed 1% in the first of 10 load steps.  Synthetic, seeded input (no
+dataset exists).
 
-A timed step is one Newton iteration of that load step: FP32 element tangent
-+ deterministic block-CSR assembly + Jacobi PCG (FP32 vectors, FP64 dots) to
-the inner tolerance + update + FP64 element residual and norm.  Every step
-starts from the same device snapshot of the step-start state, so the K steps
-do identical work.  The metric is the Newton-step time (ms per iteration,
-lower is better).  Inputs stay resident in HBM; the block-CSR matrix (about
-290 MB) is larger than the 129 MB L2, so no flush is needed between steps.
+A timed step is one Newton iteration of that load step from its start state
+(the prescribed-increment predictor's): FP32 element tangent + deterministic
+block-CSR assembly + Jacobi PCG (the reference's diagonal_matrix; FP32
+vectors, FP64 dots) to the inner tolerance 1e-4 + update + FP64 element
+residual and norm.  Every step starts from the same device snapshot, so the K
+steps do identical work.  The metric is the Newton-step time (ms per
+iteration, lower is better).  Inputs stay resident in HBM; the block-CSR
+matrix (about 290 MB) is larger than the 129 MB L2, so no flush is needed
+between steps.
 
 `e2e` repeats the step through the C ABI with host buffers: displacement
 uploaded from pinned host memory, residual at the step start, the iteration,
 and the displacement read back into pinned host memory, all inside the timed
 region.
 
---impl reference times the reference algorithm on the host cores instead
-(the CPU oracle restatement: the reference's own build needs its CMake
-system, generated headers and expat, so it is not compiled here), on a
-bounded sample of the same workload.
+The same line carries the other halves of the metric, each measured in this
+run: C1 (16^3 small-strain elastic cube, one static step), the full 10-step
+C2 load history in both precision forms, the C4 batch of 4,096 RVEs (RVE
+solves/s, mixed vs FP64, with the SpMV roofline on the batch mesh) and a short
+C5 served stream (p50/p99 beside the plain FP64 one-at-a-time solve).
+
+--impl reference runs the reference algorithm on the host cores: the CPU
+oracle restatement of the path (the reference's own build needs its CMake
+system over the whole library, so it is not compiled here), one complete
+Newton iteration of the same workload per step -- tangent + MSR assembly
+(serial, as the reference's AssembleLHS), Jacobi CG to the same 1e-4 on all
+host threads, update, residual -- from the same predictor start state.
 
 Multi-GPU: independent replicas (the single-mesh path has a real halo
 exchange that is not built); --gpus N under torchrun runs N replicas.
@@ -41,23 +52,17 @@ sys.path.insert(0, ROOT)
 
 LIN_TOL = 1e-4          # inner PCG relative tolerance (inexact Newton)
 NEWTON_TOL = 1e-8       # outer relative tolerance on the FP64 residual
-C2_PCG_ITERS_FP64 = None  # filled from the run when available
+C2_T = 1.0              # load step 1 of 10 (schedule 0 -> 1 over t = 0..10)
 
 
-def profiled_traffic(precision_mixed):
-    """DRAM bytes per SpMV launch from the committed ncu summary of this
-    workload (profiles/pcg_spmv_c2_64cubed.md), or None."""
-    if not precision_mixed:
-        return None
-    path = os.path.join(ROOT, "profiles", "pcg_spmv_c2_64cubed.md")
-    try:
-        with open(path) as f:
-            for ln in f:
-                if ln.startswith("traffic_bytes_per_launch:"):
-                    return int(ln.split(":")[1])
-    except OSError:
-        pass
-    return None
+def c2_config(nel, nnd, neq, precond, ws):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": "C2: 64^3 hex8 total-Lagrangian Simo neo-Hookean (mu=1, kappa=10), jitter 0.2h seed 0, "
+                        "load step 1/10 from the predictor state, one Newton iteration (inner %s-PCG rel tol %g)"
+                        % ("block-Jacobi" if precond == "block" else "Jacobi", LIN_TOL),
+            "nel": int(nel), "nodes": int(nnd), "dofs": int(3 * nnd), "equations": int(neq),
+            "precond": precond, "parallelism": "replicas x%d" % ws,
+            "l2": "inputs larger than L2 (assembled matrix about 290 MB FP32 block CSR on the GPU)"}
 
 
 def peaks():
@@ -170,18 +175,33 @@ def pinned_pair(n):
         return np.empty(n), np.empty(n), "pageable"
 
 
-def setup_c2(device, precision):
+def profiled_traffic(name):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary profiles/<name>, or None.  The figure is
+    the capture's, not a measurement of this run."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    return int(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def setup_c2(device, precision, precond):
     from tahoe_gb300 import workloads
     mesh, model, run = workloads.c2(add=None)
     model.device = device
     model.setup()
     # load step 1: prescribed increment through the linearised predictor
-    model.apply_step(1.0, (precision, 0, LIN_TOL))
+    pred_its = model.apply_step(C2_T, (precision, precond, LIN_TOL))
     ctx = model.ctx
     ctx.set_iteration(-1)
     ctx.residual(want_vector=False)
     ctx.checkpoint()
-    return mesh, model, ctx
+    return mesh, model, ctx, pred_its
 
 
 def one_iteration(ctx, precision, lin_tol, precond=0):
@@ -190,25 +210,102 @@ def one_iteration(ctx, precision, lin_tol, precond=0):
     return ctx.newton_iteration(precision=precision, precond=precond, lin_rel_tol=lin_tol, lin_max_it=20000)
 
 
-def cpu_baseline(mesh, gpu_pcg_iters, threads, n_pcg=10):
-    """Oracle port timed on the host cores: one residual + tangent + MSR
-    assembly pass over all elements and n_pcg Jacobi-PCG iterations on the
-    assembled system, extrapolated to the GPU's inner iteration count."""
+def cpu_newton_port(threads, steps, warmup, n=64):
+    """The oracle port of the C2 Newton iteration on the host cores: mesh,
+    equations and MSR structure, the predictor to the step-1 start state (not
+    timed), then per step one complete Newton iteration from that state --
+    tangent + MSR assembly, Jacobi CG to LIN_TOL on `threads` threads, update,
+    residual -- timed with the wall clock."""
     from oracle.pyoracle import OracleModel
     from tahoe_gb300 import workloads
-    _, om, _ = workloads.c2(add=lambda X, conn, form, mat: OracleModel(X, conn, form, mat, threads=threads))
-    u = np.zeros((mesh.nnd, 3))
-    top = mesh.face_nodes(2, 1)
-    u[top, 2] = -0.01
-    om.equations()
     t0 = time.perf_counter()
-    R, val, bindx = om.form(u, 1.0, -1, want_K=True)
-    t_form = time.perf_counter() - t0
+    mesh, om, _ = workloads.c2(n=n, add=lambda X, conn, form, mat: OracleModel(X, conn, form, mat, threads=threads))
+    _, neq = om.equations()
+    pred_its = om.predict(C2_T, LIN_TOL)
+    u0 = om.get_u()
+    setup_s = time.perf_counter() - t0
+    times, parts, its = [], [], []
+    for k in range(warmup + steps):
+        om.set_u(u0)
+        om.residual(C2_T, -1)
+        t0 = time.perf_counter()
+        n_its, nrm, tm = om.newton_iteration(C2_T, -1, LIN_TOL)
+        dt = time.perf_counter() - t0
+        if k >= warmup:
+            times.append(dt)
+            parts.append(tm)
+            its.append(n_its)
+    parts = np.mean(np.array(parts), axis=0)
+    return {"ms": 1e3 * float(np.mean(times)), "ms_steps": [round(1e3 * t, 1) for t in times],
+            "pcg_iterations": its, "predictor_pcg_iterations": pred_its, "setup_s": round(setup_s, 2),
+            "phase_s": {"tangent_and_assembly": round(float(parts[0]), 3), "pcg": round(float(parts[1]), 3),
+                        "residual": round(float(parts[2]), 3)},
+            "nel": mesh.nel, "nnd": mesh.nnd, "neq": neq}
+
+
+def cpu_sample_text(r, threads):
+    return ("oracle port, one complete C2 Newton iteration per step from the step-1 predictor state: tangent + "
+            "serial MSR assembly (%.2f s, element formation on %d threads), Jacobi CG to %g on %d threads "
+            "(%s iterations, %.2f s), update, residual (%.2f s); mean of %d timed steps"
+            % (r["phase_s"]["tangent_and_assembly"], threads, LIN_TOL, threads,
+               "/".join(str(i) for i in sorted(set(r["pcg_iterations"]))), r["phase_s"]["pcg"],
+               r["phase_s"]["residual"], len(r["ms_steps"])))
+
+
+def c2_history(model, precond):
+    """The full 10-step C2 load history from the undeformed state in both
+    forms: Newton / PCG iterations per step, device time, and the mixed form's
+    displacement error against the FP64 form at every step end."""
+    from tahoe_gb300 import lib
+    ctx = model.ctx
+    out, hist = {}, {}
+    for name, p in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
+        ctx.set_u(np.zeros((model.X.shape[0], 3)))
+        ctx.timer_start()
+        h, reps = model.run(10, 1.0, rel_tol=NEWTON_TOL, abs_tol=0.0, max_iterations=20, div_tol=10.0, precision=p,
+                            precond=precond, lin_rel_tol=LIN_TOL, lin_max_it=20000, predictor=True)
+        ms = ctx.timer_stop()
+        hist[name] = h
+        newton = [r.iterations for r in reps]
+        out[name] = {"ms": round(ms, 1), "newton_per_step": newton, "pcg_per_step": [r.pcg_iterations for r in reps],
+                     "ms_per_newton_iteration": round(ms / max(sum(newton), 1), 3)}
+    err = [float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(hist["mixed"], hist["fp64"])]
+    out["u_rel_err_mixed_vs_fp64_per_step"] = [float("%.3g" % e) for e in err]
+    out["note"] = "pcg_per_step excludes the predictor's iterations; ms covers predictors and Newton"
+    return out
+
+
+def c1_step():
+    """C1: 16^3 small-strain Hookean cube, 1 MPa traction, one static step,
+    PCG-Jacobi to 1e-10, both forms; the oracle port's time for the same
+    step on the host (single thread, as the reference's implicit path)."""
+    from oracle.pyoracle import OracleModel
+    from tahoe_gb300 import lib, workloads
+    res, u = {}, {}
+    for name, p in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
+        mesh, m, run = workloads.c1()
+        m.setup()
+        m.ctx.timer_start()
+        # FP64: one Newton iteration with PCG to 1e-10 (the configuration's
+        # solver); mixed: inexact Newton (FP32 PCG to 1e-4) to the same
+        # 1e-10 on the FP64 residual
+        h, reps = m.run(1, 1.0, rel_tol=1e-10, abs_tol=0.0, max_iterations=10, precision=p,
+                        precond=lib.PRECOND_JACOBI, lin_rel_tol=1e-10 if p == lib.FP64 else LIN_TOL,
+                        lin_max_it=20000)
+        ms = m.ctx.timer_stop()
+        u[name] = h[-1]
+        res[name] = {"ms": round(ms, 3), "newton_iterations": reps[0].iterations,
+                     "pcg_iterations": reps[0].pcg_iterations}
+        m.ctx.close()
+    _, om, _ = workloads.c1(add=lambda X, conn, form, mat: OracleModel(X, conn, form, mat, threads=1))
     t0 = time.perf_counter()
-    om.pcg(val, R, 1e-30, n_pcg)
-    t_pcg = (time.perf_counter() - t0) / n_pcg
-    ms = 1e3 * (t_form + gpu_pcg_iters * t_pcg)
-    return ms, t_form, t_pcg
+    st, uh, its = om.run(1, 1.0, 1e-10, 0.0, 10, 10.0, 1, 1e-10)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    res["u_rel_err_mixed_vs_fp64"] = float(np.abs(u["mixed"] - u["fp64"]).max() / np.abs(u["fp64"]).max())
+    res["cpu_baseline"] = {"value": round(cpu_ms, 1), "unit": "ms/static step", "cores": 1, "kind": "port",
+                           "sample": "oracle port, the whole static step (Newton + serial Jacobi CG to 1e-10)"}
+    res["config"] = "C1: 16^3 hex8 small-strain Hookean (E 200e3, nu 0.3), z=0 fixed, 1 MPa traction on z=1"
+    return res
 
 
 def run_ours(args):
@@ -216,7 +313,7 @@ def run_ours(args):
     from tahoe_gb300 import lib, workloads
     prec = lib.MIXED if args.precision == "mixed" else lib.FP64
     precond = lib.PRECOND_BLOCK_JACOBI if args.precond == "block" else lib.PRECOND_JACOBI
-    mesh, model, ctx = setup_c2(local, prec)
+    mesh, model, ctx, pred_its = setup_c2(local, prec, precond)
     tuning = None
     if not args.no_tune:
         # launch shapes picked by the autotuner on this mesh and state
@@ -227,10 +324,8 @@ def run_ours(args):
                                              "cached", "spmv_sweep")}
 
     # warm-up (also captures the PCG graph)
-    its_seen = []
     for _ in range(max(args.warmup, 1)):
-        nrm, its = one_iteration(ctx, prec, LIN_TOL, precond)
-        its_seen.append(its)
+        one_iteration(ctx, prec, LIN_TOL, precond)
 
     sampler = ClockSampler(local)
     barrier(ws)
@@ -292,26 +387,6 @@ def run_ours(args):
         other_rooflines[name] = {"bound": "hbm", "achieved": round(a, 1), "peak": peak, "unit": "GB/s",
                                  "frac": round(a / peak, 4), "algorithmic_bytes": int(b), "ms_per_launch": round(t, 5)}
 
-    # full load step to NEWTON_TOL in both forms: Newton iterations, time, agreement
-    extra = {}
-    if not args.quick:
-        res = {}
-        for name, p in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
-            ctx.rollback()
-            ctx.timer_start()
-            rc, rep = ctx.newton(rel_tol=NEWTON_TOL, abs_tol=0.0, div_tol=10.0, max_iterations=20, precision=p,
-                                 precond=precond, lin_rel_tol=LIN_TOL, lin_max_it=20000, check=False)
-            ms = ctx.timer_stop()
-            res[name] = (ctx.get_u().copy(), rep, ms, rc)
-        uf, um = res["fp64"][0], res["mixed"][0]
-        extra = {
-            "load_step": {k: {"ms": round(v[2], 3), "newton_iterations": v[1].iterations,
-                              "pcg_iterations": v[1].pcg_iterations, "status": v[3],
-                              "ms_per_newton_iteration": round(v[2] / max(v[1].iterations, 1), 3)}
-                          for k, v in res.items()},
-            "rel_err_mixed_vs_fp64": float(np.abs(um - uf).max() / np.abs(uf).max()),
-        }
-
     line = {
         "metric": "Newton-step time",
         "value": round(ms_step, 4),
@@ -325,20 +400,19 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "fp32 tangent+PCG, fp64 residual/dots" if prec == lib.MIXED else "fp64",
         "data": "synthetic (seeded 64^3 jittered hex8 block)",
-        "config": {"workload": "C2: 64^3 hex8 total-Lagrangian Simo neo-Hookean (mu=1, kappa=10), jitter 0.2h seed 0, "
-                               "load step 1/10, one Newton iteration (inner %s-PCG rel tol %g)"
-                               % ("block-Jacobi" if args.precond == "block" else "Jacobi", LIN_TOL),
-                   "nel": mesh.nel, "nodes": nnd, "dofs": nnd * 3, "equations": ctx.neq, "block_nnz": nnzb,
-                   "scalar_nnz": int(nnzb * 9), "parallelism": "replicas x%d" % ws,
-                   "l2": "inputs larger than L2 (block CSR %.0f MB)" % (nnzb * (9 * s_val + 4) / 1e6)},
+        "config": c2_config(mesh.nel, nnd, ctx.neq, args.precond, ws),
+        "block_nnz": int(nnzb), "scalar_nnz": int(nnzb * 9),
         "pcg_iterations_per_step": float(np.mean(pcg_its)),
+        "predictor_pcg_iterations": pred_its,
         "elements_assembled_per_s": round(elements_per_s, 1),
         "kernel_ms": {"pcg_spmv": round(t_spmv, 5), "pcg_update": round(t_upd, 5), "tangent": round(t_tan, 4),
                       "assembly": round(t_asm, 4), "residual": round(t_res, 4)},
         "roofline": {"kernel": "pcg_spmv_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "algorithmic_bytes": int(bytes_spmv), "traffic": profiled_traffic(prec == lib.MIXED),
-                     "traffic_source": "ncu dram__bytes_read.sum+dram__bytes_write.sum, profiles/pcg_spmv_c2_64cubed.md"},
+                     "algorithmic_bytes": int(bytes_spmv),
+                     "traffic": profiled_traffic("pcg_spmv_c2_64cubed.md") if prec == lib.MIXED else None,
+                     "traffic_source": "committed ncu capture of this kernel on this workload "
+                                       "(profiles/pcg_spmv_c2_64cubed.md), not measured in this run"},
         "other_rooflines": other_rooflines,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/Newton iteration", "h2d_bytes_per_step": nnd * 24,
                 "d2h_bytes_per_step": nnd * 24, "host_memory": host_mem},
@@ -346,48 +420,50 @@ def run_ours(args):
         "tuning": tuning,
         "clocks": clocks,
     }
-    line.update(extra)
+    if not args.quick and ws == 1:
+        # the metric's other halves, measured in this run (device timers)
+        t_extra = time.perf_counter()
+        line["c2_load_history"] = c2_history(model, precond)
+        model.ctx.close()
+        line["c1"] = c1_step()
+        line["c4"] = c4_batch(args.rves, args.c4_precond, with_cpu=False, macro=True)
+        line["c5"] = c5_trace(args, rates=[args.c5_rate], requests=args.c5_requests,
+                              plain_requests=args.c5_plain_requests)
+        line["extras_wall_s"] = round(time.perf_counter() - t_extra, 1)
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        # the reference's CPU path is Jacobi-PCG (diagonal_matrix): its
-        # iteration count is the GPU path's Jacobi count on this workload
-        n_cpu = float(np.mean(pcg_its)) if args.precond == "jacobi" else float(args.ref_pcg_iters)
-        cms, t_form, t_pcg = cpu_baseline(mesh, n_cpu, threads)
-        line["cpu_baseline"] = {
-            "value": round(cms, 1), "unit": "ms/Newton iteration", "cores": threads, "kind": "port",
-            "sample": "oracle: one residual+tangent+MSR assembly pass over all %d elements (%.2f s, %d threads) and "
-                      "10 serial Jacobi-PCG iterations on the MSR system (%.1f ms each), extrapolated to %.0f inner "
-                      "Jacobi iterations" % (mesh.nel, t_form, threads, t_pcg * 1e3, n_cpu)}
+        r = cpu_newton_port(threads, steps=2, warmup=1)
+        line["cpu_baseline"] = {"value": round(r["ms"], 1), "unit": "ms/Newton iteration", "cores": threads,
+                                "kind": "port", "sample": cpu_sample_text(r, threads)}
     if rank == 0:
         print(json.dumps(line))
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the same Newton iteration on all
+    host threads, one complete iteration per step (nothing extrapolated)."""
     ws, rank, local = dist_init()
     if rank != 0:
         return
-    from tahoe_gb300.meshgen import BoxMesh
-    mesh = BoxMesh(64, 64, 64, jitter=0.2, seed=0)
     threads = os.cpu_count() or 1
-    n_its = args.ref_pcg_iters
-    times = []
-    for k in range(args.warmup + args.steps):
-        ms, t_form, t_pcg = cpu_baseline(mesh, n_its, threads, n_pcg=5)
-        if k >= args.warmup:
-            times.append(ms)
-    v = float(np.mean(times))
+    t_run = time.perf_counter()
+    r = cpu_newton_port(threads, steps=args.steps, warmup=args.warmup)
+    v = r["ms"]
     line = {
         "impl": "reference", "metric": "Newton-step time", "value": round(v, 1), "unit": "ms/Newton iteration",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 1),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
         "data": "synthetic (seeded 64^3 jittered hex8 block)",
-        "config": {"workload": "C2: 64^3 hex8 total-Lagrangian Simo neo-Hookean (mu=1, kappa=10), jitter 0.2h seed 0, "
-                               "load step 1/10, one Newton iteration (inner Jacobi-PCG rel tol %g)" % LIN_TOL},
+        "config": c2_config(r["nel"], r["nnd"], r["neq"], args.precond, ws),
+        "pcg_iterations_per_step": float(np.mean(r["pcg_iterations"])),
+        "ms_steps": r["ms_steps"],
         "cpu_baseline": {"value": round(v, 1), "unit": "ms/Newton iteration", "cores": threads, "kind": "port",
-                         "sample": "per step: residual+tangent+MSR assembly over all elements + 5 Jacobi-PCG "
-                                   "iterations, extrapolated to %d inner iterations" % n_its},
+                         "sample": cpu_sample_text(r, threads)},
         "e2e": {"value": round(v, 1), "unit": "ms/Newton iteration", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_s": r["setup_s"], "wall_s": round(time.perf_counter() - t_run, 1),
     }
+    if args.precond != "jacobi":
+        line["note"] = "the port's CG is Jacobi (the reference's diagonal_matrix) whatever --precond says"
     print(json.dumps(line))
 
 
@@ -418,45 +494,51 @@ def rve_cpu_sample(sizes_all, threads, seed=0):
     return mean, per_n
 
 
-def run_c4(args):
+def c4_batch(count, precond_name, with_cpu=False, macro=True):
     """Configuration 4: a batch of independent RVEs solved together.  The
     timed batch covers composing the batch mesh from the resident templates,
-    the affine predictor, Newton to 1e-8 per RVE and the averaged stresses."""
+    the affine predictor, Newton to 1e-8 per RVE and the averaged stresses;
+    the consistent macro tangent is timed separately."""
     from tahoe_gb300 import lib, rve
-    ns, Fs = rve.sample_batch(args.rves, seed=0)
+    ns, Fs = rve.sample_batch(count, seed=0)
     t0 = time.perf_counter()
     c = lib.Context(0)
     res = rve.ResidentRVEs(c)
     for n in np.unique(ns):
         res.template_id(n)
     t_setup = time.perf_counter() - t0
-    precond = lib.PRECOND_BLOCK_JACOBI if args.precond == "block" else lib.PRECOND_JACOBI
+    precond = lib.PRECOND_BLOCK_JACOBI if precond_name == "block" else lib.PRECOND_JACOBI
     out = {}
+    wn, wF = ns[:64], Fs[:64]
     for name, prec in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
-        res.solve(ns, Fs, precision=prec, precond=precond)  # warm-up: pools, graphs
+        res.solve(wn, wF, precision=prec, precond=precond)  # warm-up: pools
         c.timer_start()
         rc, rep, rel, P = res.solve(ns, Fs, precision=prec, precond=precond)
         ms = c.timer_stop()
         out[name] = dict(ms=ms, rc=rc, newton=rep.iterations, pcg=rep.pcg_iterations, worst_rel=float(rel.max()),
                          P=P, ms_tangent=rep.ms_tangent, ms_solve=rep.ms_solve, ms_residual=rep.ms_residual)
-        # consistent macro tangent of every RVE at the converged state
-        c.timer_start()
-        Cm, cits = c.macro_tangent(np.ones(len(ns)), precision=prec, precond=precond, lin_rel_tol=1e-7)
-        out[name].update(C=Cm, ms_macro=c.timer_stop(), macro_pcg=cits)
-    b = argparse.Namespace(nel=c.nel, nnd=c.nnd)
-    c.tangent(lib.MIXED)
-    roof = spmv_roofline(c, lib.MIXED)
+        if macro:
+            # consistent macro tangent of every RVE at the converged state
+            c.timer_start()
+            Cm, cits = c.macro_tangent(np.ones(len(ns)), precision=prec, precond=precond, lin_rel_tol=1e-7)
+            out[name].update(C=Cm, ms_macro=c.timer_stop(), macro_pcg=cits)
+        if name == "mixed":
+            c.tangent(lib.MIXED)
+            roof = spmv_roofline(c, lib.MIXED)
+            roof["on"] = "the composed batch mesh (%d nodes, %d block nonzeros)" % (c.nnd, c.block_nnz)
+            geo = dict(elements=int(c.nel), nodes=int(c.nnd), dofs=int(3 * c.nnd), equations=int(c.neq),
+                       block_nnz=int(c.block_nnz))
+    c.close()
     Pm, Pf = out["mixed"]["P"], out["fp64"]["P"]
     err = float(np.abs(Pm - Pf).max() / np.abs(Pf).max())
     per_rve = np.abs(Pm - Pf).reshape(len(ns), -1).max(axis=1) / np.abs(Pf).reshape(len(ns), -1).max(axis=1)
     line = {
         "metric": "RVE solves/s", "value": round(len(ns) / (out["mixed"]["ms"] * 1e-3), 1), "unit": "RVE/s",
         "higher_is_better": True, "n_gpus": 1,
-        "config": {"workload": "C4: %d independent RVEs, n x n x n hex8 unit cubes, n ~ U{4..16} (seed 0), two-phase "
-                               "Simo neo-Hookean (mu 1/10, kappa 10/100, inclusion r=0.3 by centroid), affine BC from "
-                               "F = I + 0.05 S, linear predictor then Newton to 1e-8 per RVE" % len(ns),
-                   "elements": int(b.nel), "nodes": int(b.nnd), "dofs": int(3 * b.nnd), "equations": int(c.neq),
-                   "block_nnz": int(c.block_nnz)},
+        "config": dict(workload="C4: %d independent RVEs, n x n x n hex8 unit cubes, n ~ U{4..16} (seed 0), two-phase "
+                                "Simo neo-Hookean (mu 1/10, kappa 10/100, inclusion r=0.3 by centroid), affine BC "
+                                "from F = I + 0.05 S, linear predictor then Newton to 1e-8 per RVE, %s-PCG 1e-4"
+                                % (len(ns), "block-Jacobi" if precond_name == "block" else "Jacobi"), **geo),
         "batch_ms": {k: round(v["ms"], 2) for k, v in out.items()},
         "solves_per_s": {k: round(len(ns) / (v["ms"] * 1e-3), 1) for k, v in out.items()},
         "newton_iterations": {k: v["newton"] for k, v in out.items()},
@@ -466,31 +548,37 @@ def run_c4(args):
         "worst_rve_rel_residual": {k: v["worst_rel"] for k, v in out.items()},
         "status": {k: v["rc"] for k, v in out.items()},
         "P_rel_err_mixed_vs_fp64": err,
-        "macro_tangent_ms": {k: round(v["ms_macro"], 2) for k, v in out.items()},
-        "macro_tangent_pcg_iterations": {k: v["macro_pcg"] for k, v in out.items()},
-        "macro_tangent_rel_err_mixed_vs_fp64": float(np.abs(out["mixed"]["C"] - out["fp64"]["C"]).max() /
-                                                     np.abs(out["fp64"]["C"]).max()),
         "P_rel_err_mixed_vs_fp64_worst_rve": float(per_rve.max()),
         "template_setup_s": round(t_setup, 3),
         "roofline": roof,
-        "precond": args.precond,
+        "precond": precond_name,
     }
-    if not args.no_cpu:
+    if macro:
+        line["macro_tangent_ms"] = {k: round(v["ms_macro"], 2) for k, v in out.items()}
+        line["macro_tangent_pcg_iterations"] = {k: v["macro_pcg"] for k, v in out.items()}
+        line["macro_tangent_rel_err_mixed_vs_fp64"] = float(np.abs(out["mixed"]["C"] - out["fp64"]["C"]).max() /
+                                                            np.abs(out["fp64"]["C"]).max())
+        line["solves_per_s_with_macro_tangent"] = {
+            k: round(len(ns) / ((v["ms"] + v["ms_macro"]) * 1e-3), 1) for k, v in out.items()}
+    if with_cpu:
         threads = os.cpu_count() or 1
         mean, per_n = rve_cpu_sample(ns, threads)
         line["cpu_baseline"] = {"value": round(threads / mean, 2), "unit": "RVE/s", "cores": threads, "kind": "port",
                                 "sample": "oracle (Newton + Jacobi-PCG 1e-4, FP64) on one RVE per size n=4..16, "
                                           "single-threaded; batch rate = pool of %d independent processes at the "
                                           "size-weighted mean %.3f s per RVE" % (threads, mean)}
-    print(json.dumps(line))
+    return line
 
 
-def run_c5(args):
+def run_c4(args):
+    print(json.dumps(c4_batch(args.rves, args.c4_precond, with_cpu=not args.no_cpu, macro=True)))
+
+
+def c5_trace(args, rates, requests, plain_requests):
     """Configuration 5: a Poisson stream of RVE requests served with
     continuous batching over several lanes (mixed precision), beside the plain
     one-at-a-time FP64 GPU solve of the same requests."""
     from tahoe_gb300 import lib, serve
-    rates = [float(r) for r in args.rates.split(",")]
     import torch
     free, _ = torch.cuda.mem_get_info(0)
     budget = 0.5 * free
@@ -504,9 +592,9 @@ def run_c5(args):
     plain.run(wa[:2], wn[:2], wF[:2])
     sweep = []
     for i, rate in enumerate(rates):
-        arr, ns, Fs = serve.sample_requests(args.requests, rate, seed=i)
+        arr, ns, Fs = serve.sample_requests(requests, rate, seed=i)
         res = srv.run(arr, ns, Fs)
-        k = min(args.plain_requests, len(ns))
+        k = min(plain_requests, len(ns))
         ref = plain.run(arr[:k], ns[:k], Fs[:k])
         both = (res["status"][:k] == 0) & (ref["status"] == 0)
         d = np.abs(res["P"][:k] - ref["P"]).reshape(k, -1).max(axis=1) / \
@@ -536,7 +624,7 @@ def run_c5(args):
     srv.close()
     plain.close()
     top = max(sweep, key=lambda r: r["solves_per_s"])
-    line = {
+    return {
         "metric": "served RVE solves/s", "value": top["solves_per_s"], "unit": "RVE/s", "higher_is_better": True,
         "n_gpus": 1,
         "config": {"workload": "C5: Poisson stream of RVE requests, n log-uniform in {4..24}, two-phase Simo "
@@ -547,7 +635,11 @@ def run_c5(args):
         "sweep": sweep,
         "roofline": roof,
     }
-    print(json.dumps(line))
+
+
+def run_c5(args):
+    rates = [float(r) for r in args.rates.split(",")]
+    print(json.dumps(c5_trace(args, rates, args.requests, args.plain_requests)))
 
 
 def run_c3(args):
@@ -590,10 +682,11 @@ def run_c3(args):
         # allocate (also in intermediate Newton iterations)
         yielding, alloc = (fl == 0) | (fl == 3), fl != lib.J2_UNALLOCATED
         if name == "mixed":
-            flags_ref["final"] = (yielding, alloc)
+            flags_ref["final"] = (yielding, alloc, fl)
         else:
             rec["mismatch"].append(int((yielding != flags_ref["final"][0]).sum()))
             rec["alloc_mismatch"] = int((alloc != flags_ref["final"][1]).sum())
+            rec["raw_mismatch"] = int((fl != flags_ref["final"][2]).sum())
         u_last[name] = hist
         out[name] = rec
         c.close()
@@ -620,8 +713,13 @@ def run_c3(args):
         "flags_final": {k: v["flags_final"] for k, v in out.items()},
         "roofline": out["mixed"]["roofline"],
         "yielding_set_mismatch_final": f["mismatch"][0],
-        "active_set_bit_exact": f["mismatch"][0] == 0,
+        "yielding_set_bit_exact": f["mismatch"][0] == 0,
+        "raw_flag_array_mismatch_final": f["raw_mismatch"],
+        "raw_flag_array_bit_exact": f["raw_mismatch"] == 0,
         "allocated_points_mismatch_final": f["alloc_mismatch"],
+        "flags_note": "yielding set = points flagged plastic or reset at the last converged step; the raw flag "
+                      "array also records element allocation, which follows transient yields of intermediate "
+                      "Newton iterates and so the precision form's iterate path",
         "u_rel_err_mixed_vs_fp64_worst_step": float(max(
             np.abs(a - b).max() / max(np.abs(b).max(), 1e-300) for a, b in zip(u_last["mixed"], u_last["fp64"]))),
     }
@@ -656,13 +754,10 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the full load-step comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes, no autotuning")
-    ap.add_argument("--ref-pcg-iters", type=int, default=564,
-                    help="Jacobi-PCG iterations of the C2 Newton iteration to 1e-4 (the GPU path's Jacobi count) "
-                         "for the CPU arm's extrapolation")
     ap.add_argument("--kernel", choices=sorted(KERNELS), help="time standalone launches of one kernel only")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--n", type=int, default=64, help="mesh size per side for --kernel")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--c3-steps", type=int, default=40, help="C3 load steps to run (of 40)")
     ap.add_argument("--max-step-cuts", type=int, default=6, help="C3 load-step cuts allowed (TimeManagerT)")
     ap.add_argument("--quick-solve-iter", type=int, default=0,
@@ -673,10 +768,17 @@ def main():
     ap.add_argument("--plain-requests", type=int, default=200, help="C5 requests for the one-at-a-time arm")
     ap.add_argument("--lanes", type=int, default=4)
     ap.add_argument("--max-batch", type=int, default=1024)
-    ap.add_argument("--precond", default="block", choices=["jacobi", "block"],
-                    help="PCG preconditioner: block-Jacobi (3x3 node blocks) or Jacobi")
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "block"],
+                    help="PCG preconditioner: Jacobi (the reference's diagonal_matrix) or block-Jacobi (3x3 node "
+                         "blocks)")
+    ap.add_argument("--c4-precond", default="block", choices=["jacobi", "block"], help="C4 batch preconditioner")
+    ap.add_argument("--c5-rate", type=float, default=5000.0, help="C5 arrival rate of the default run's trace")
+    ap.add_argument("--c5-requests", type=int, default=1000, help="C5 requests of the default run's trace")
+    ap.add_argument("--c5-plain-requests", type=int, default=100, help="C5 one-at-a-time FP64 requests (default run)")
     args = ap.parse_args()
-    if args.workload == "c4" and args.impl == "ours":
+    if args.workload == "c1" and args.impl == "ours":
+        print(json.dumps(c1_step()))
+    elif args.workload == "c4" and args.impl == "ours":
         run_c4(args)
     elif args.workload == "c5" and args.impl == "ours":
         run_c5(args)

@@ -98,6 +98,13 @@ int tg_element_blocks(tg_context* ctx, const int* block_of_element);
  * symmetric pattern of MSRBuilderT::GenerateMSR, MSRBuilderT.cpp:134, with
  * the diagonal stored in-row).  Call with row_ptr == NULL to get *nnz. */
 int tg_pattern_build(tg_context* ctx, int upper_only, int* row_ptr, int* col_idx, long long* nnz);
+/* The same structure computed on the host from the mesh alone (no context,
+ * no GPU): the node graph of the connectivity (conn: nel*8, 0-based) that
+ * tg_mesh_upload builds, expanded over the equations `eqnos` (nnd*3) exactly
+ * as tg_pattern_build does -- MSRBuilderT::GenerateMSR (MSRBuilderT.cpp:134)
+ * over GraphT::MakeGraph's node graph.  Call with row_ptr == NULL to get *nnz. */
+int tg_pattern_build_host(int nnd, int nel, const int* conn, const int* eqnos, int upper_only, int* row_ptr,
+                          int* col_idx, long long* nnz);
 /* number of active equations / structural block nonzeros */
 int tg_sizes(const tg_context* ctx, int* neq, long long* block_nnz);
 

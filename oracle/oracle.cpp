@@ -10,6 +10,8 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -325,6 +327,8 @@ struct Model {
   std::vector<int> bindx; /* MSR upper (symmetric) */
   std::vector<J2Card> j2;
   std::vector<double> u; /* nnd*3 current */
+  std::vector<double> Rcur; /* residual at u (orc_residual / orc_newton_iteration) */
+  std::vector<double> Kval; /* MSR values of the last tangent of orc_newton_iteration */
 
   const Material& mat(int e) const { return mats[block.empty() ? 0 : block[e]]; }
   double schedule(double t) const { /* PiecewiseLinearT::function (:179-188) */
@@ -653,7 +657,8 @@ long msr_find(const std::vector<int>& bindx, int row, int col) {
  * SolidElementT::ElementRHSDriver / ElementLHSDriver with assembly of
  * MSRMatrixT::Assemble (symmetric, MSRMatrixT.cpp:96-143).  Element
  * formation is spread over M.nthreads threads; assembly is serial. */
-int form(Model& M, const double* u, double t, int iteration, double* R, double* val) {
+int form(Model& M, const double* u, double t, int iteration, double* R, double* val,
+         const double* v_nodal = nullptr, double* Kv = nullptr) {
   const int nth = std::max(1, M.nthreads);
   if (R) {
     std::vector<double> fext;
@@ -693,6 +698,19 @@ int form(Model& M, const double* u, double t, int iteration, double* R, double* 
           for (int p = 0; p < 24; ++p)
             if (eq[p] > 0) R[eq[p] - 1] -= buf[k].fint[p];
         } else {
+          if (Kv) {
+            /* the element tangent applied to a nodal vector, on the active
+             * rows (all columns: the coupling to prescribed dofs included) */
+            double ve[24];
+            for (int a = 0; a < 8; ++a)
+              for (int d = 0; d < 3; ++d) ve[a * 3 + d] = v_nodal[M.conn[e * 8 + a] * 3 + d];
+            for (int p = 0; p < 24; ++p) {
+              if (eq[p] <= 0) continue;
+              double a = 0.0;
+              for (int q = 0; q < 24; ++q) a += buf[k].Ke[p * 24 + q] * ve[q];
+              Kv[eq[p] - 1] += a;
+            }
+          }
           for (int p = 0; p < 24; ++p) {
             if (eq[p] <= 0) continue;
             for (int q = 0; q < 24; ++q) {
@@ -764,6 +782,170 @@ int pcg(const Model& M, const double* val, const double* b, double* x, double to
     for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
   }
   return -maxit;
+}
+
+/* Spin barrier of the oracle's worker threads (generation counter). */
+struct SpinBarrier {
+  std::atomic<int> count{0};
+  std::atomic<int> gen{0};
+  int n;
+  explicit SpinBarrier(int n_) : n(n_) {}
+  void wait() {
+    const int g = gen.load(std::memory_order_acquire);
+    if (count.fetch_add(1, std::memory_order_acq_rel) == n - 1) {
+      count.store(0, std::memory_order_relaxed);
+      gen.store(g + 1, std::memory_order_release);
+    } else {
+      while (gen.load(std::memory_order_acquire) == g) std::this_thread::yield();
+    }
+  }
+};
+
+/* The same Jacobi CG as pcg() on M.nthreads threads, for the CPU baseline
+ * and large oracle runs.  The rows are split into contiguous ranges of
+ * about equal stored length; the symmetric MSR product (MSRMatrixT::Multx,
+ * MSRMatrixT.cpp:385-420) runs per range, a row's transposed contributions
+ * to rows of later ranges going into a per-thread spill buffer that the
+ * owners of those rows add, in thread order, after a barrier.  Dot products
+ * are summed per thread and then over threads in a fixed order, so every
+ * thread takes the same decisions and the result does not depend on timing.
+ * Same stopping rule as pcg(): ||r|| / ||b|| < tol. */
+int pcg_mt(const Model& M, const double* val, const double* b, double* x, double tol, int maxit,
+           double* relres) {
+  const int n = M.neq;
+  const int nth = std::max(1, std::min(M.nthreads, n / 2048));
+  if (nth <= 1) return pcg(M, val, b, x, tol, maxit, relres);
+  const std::vector<int>& bx = M.bindx;
+  std::vector<int> lo(nth + 1, n);
+  {
+    const long long total = (long long)n + (bx[n] - bx[0]);
+    long long acc = 0;
+    int t = 1;
+    lo[0] = 0;
+    for (int r = 0; r < n && t < nth; ++r) {
+      acc += 1 + (bx[r + 1] - bx[r]);
+      if (acc * nth >= total * t) lo[t++] = r + 1;
+    }
+    for (; t < nth; ++t) lo[t] = n;
+  }
+  std::vector<int> spill_len(nth, 0);
+  for (int t = 0; t < nth; ++t) {
+    int hi = lo[t + 1];
+    for (int r = lo[t]; r < lo[t + 1]; ++r)
+      if (bx[r + 1] > bx[r]) hi = std::max(hi, bx[bx[r + 1] - 1] + 1);
+    spill_len[t] = hi - lo[t + 1];
+  }
+  std::vector<std::vector<double>> spill(nth);
+  for (int t = 0; t < nth; ++t) spill[t].assign(spill_len[t], 0.0);
+  std::vector<double> r(n), z(n), p(n), q(n), minv(n);
+  std::vector<double> part_a(nth), part_b(nth), part_c(nth);
+  SpinBarrier bar(nth);
+  int result = -maxit;
+  double rel_out = 0.0;
+  /* y = A v over the rows of thread t (spill of later rows kept aside) */
+  auto product = [&](int t, const double* v, double* y) {
+    const int a = lo[t], e = lo[t + 1];
+    std::vector<double>& sp = spill[t];
+    std::fill(sp.begin(), sp.end(), 0.0);
+    for (int i = a; i < e; ++i) y[i] = 0.0;
+    for (int i = a; i < e; ++i) {
+      const double vi = v[i];
+      double s_ = val[i] * vi;
+      for (int j = bx[i]; j < bx[i + 1]; ++j) {
+        const int c = bx[j];
+        const double w = val[j];
+        s_ += w * v[c];
+        if (c < e) y[c] += w * vi;
+        else sp[c - e] += w * vi;
+      }
+      y[i] += s_;
+    }
+  };
+  /* add the spills of earlier threads that fall on thread t's rows */
+  auto add_spills = [&](int t, double* y) {
+    const int a = lo[t], e = lo[t + 1];
+    for (int s2 = 0; s2 < t; ++s2) {
+      const int base = lo[s2 + 1], len = spill_len[s2];
+      const int i0 = std::max(a, base), i1 = std::min(e, base + len);
+      for (int i = i0; i < i1; ++i) y[i] += spill[s2][i - base];
+    }
+  };
+  auto total = [&](const std::vector<double>& part) {
+    double s_ = 0.0;
+    for (int t = 0; t < nth; ++t) s_ += part[t];
+    return s_;
+  };
+  auto worker = [&](int t) {
+    const int a = lo[t], e = lo[t + 1];
+    for (int i = a; i < e; ++i) minv[i] = 1.0 / val[i];
+    product(t, x, q.data());
+    bar.wait();
+    add_spills(t, q.data());
+    double bb = 0.0, rz_ = 0.0;
+    for (int i = a; i < e; ++i) {
+      r[i] = b[i] - q[i];
+      z[i] = minv[i] * r[i];
+      p[i] = z[i];
+      bb += b[i] * b[i];
+      rz_ += r[i] * z[i];
+    }
+    part_a[t] = bb;
+    part_b[t] = rz_;
+    bar.wait();
+    const double bn = std::sqrt(total(part_a));
+    double rz = total(part_b);
+    bar.wait();  /* part_a / part_b are rewritten below */
+    if (bn == 0.0) {
+      if (t == 0) {
+        result = 0;
+        rel_out = 0.0;
+      }
+      return;
+    }
+    for (int it = 1; it <= maxit; ++it) {
+      product(t, p.data(), q.data());
+      bar.wait();
+      add_spills(t, q.data());
+      double pq = 0.0;
+      for (int i = a; i < e; ++i) pq += p[i] * q[i];
+      part_c[t] = pq;
+      bar.wait();
+      const double alpha = rz / total(part_c);
+      double rr = 0.0, rzn = 0.0;
+      for (int i = a; i < e; ++i) {
+        x[i] += alpha * p[i];
+        r[i] -= alpha * q[i];
+        z[i] = minv[i] * r[i];
+        rr += r[i] * r[i];
+        rzn += r[i] * z[i];
+      }
+      part_a[t] = rr;
+      part_b[t] = rzn;
+      bar.wait();
+      const double rel = std::sqrt(total(part_a)) / bn;
+      const double rz_new = total(part_b);
+      if (t == 0) rel_out = rel;
+      if (rel < tol) {
+        if (t == 0) result = it;
+        return;
+      }
+      const double beta = rz_new / rz;
+      rz = rz_new;
+      for (int i = a; i < e; ++i) p[i] = z[i] + beta * p[i];
+      bar.wait();  /* p complete before the next product; totals read */
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nth; ++t) th.emplace_back(worker, t);
+  worker(0);
+  for (auto& w : th) w.join();
+  if (relres) *relres = rel_out;
+  return result;
+}
+
+/* Jacobi CG on the model's thread count (serial when it is 1). */
+int pcg_any(const Model& M, const double* val, const double* b, double* x, double tol, int maxit, double* relres) {
+  return M.nthreads > 1 ? pcg_mt(M, val, b, x, tol, maxit, relres) : pcg(M, val, b, x, tol, maxit, relres);
 }
 
 /* dense LU (partial pivoting) solve of the MSR system: stands in for the
@@ -966,7 +1148,92 @@ int orc_pcg(void* m, const double* val, const double* b, double* x, double tol, 
             double* relres) {
   Model* M = static_cast<Model*>(m);
   ensure_setup(*M);
-  return pcg(*M, val, b, x, tol, maxit, relres);
+  return pcg_any(*M, val, b, x, tol, maxit, relres);
+}
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static double norm2(const std::vector<double>& v) {
+  double a = 0.0;
+  for (double x : v) a += x * x;
+  return std::sqrt(a);
+}
+
+/* R = Fext - Fint at the held displacement (SolverT::Residual after
+ * FEManagerT::FormRHS), kept for the next orc_newton_iteration. */
+int orc_residual(void* m, double t, int iteration, double* norm) {
+  Model* M = static_cast<Model*>(m);
+  ensure_setup(*M);
+  M->Rcur.assign(M->neq, 0.0);
+  if (form(*M, M->u.data(), t, iteration, M->Rcur.data(), nullptr)) return -1;
+  if (norm) *norm = norm2(M->Rcur);
+  return 0;
+}
+
+/* One iteration of NLSolver::Solve's loop (NLSolver.cpp:137-188) from the
+ * held displacement and residual: tangent + MSR assembly, Jacobi CG to
+ * lin_tol, u += du, new residual (iteration + 1).  times[3] receives the
+ * seconds of the tangent pass, the CG and the residual pass. */
+int orc_newton_iteration(void* m, double t, int iteration, double lin_tol, int max_it, int* pcg_its, double* norm,
+                         double* times) {
+  Model* M = static_cast<Model*>(m);
+  ensure_setup(*M);
+  if ((int)M->Rcur.size() != M->neq) return -1;
+  const int n = M->neq;
+  M->Kval.assign(M->bindx.size(), 0.0);
+  double t0 = now_s();
+  if (form(*M, M->u.data(), t, iteration, nullptr, M->Kval.data())) return -1;
+  double t1 = now_s();
+  std::vector<double> du(n, 0.0);
+  const int its = pcg_any(*M, M->Kval.data(), M->Rcur.data(), du.data(), lin_tol, max_it, nullptr);
+  double t2 = now_s();
+  if (its < 0) return -2;
+  for (int i = 0; i < M->nnd * 3; ++i)
+    if (M->eqnos[i] > 0) M->u[i] += du[M->eqnos[i] - 1];
+  if (form(*M, M->u.data(), t, iteration + 1, M->Rcur.data(), nullptr)) return -1;
+  double t3 = now_s();
+  if (pcg_its) *pcg_its = its;
+  if (norm) *norm = norm2(M->Rcur);
+  if (times) {
+    times[0] = t1 - t0;
+    times[1] = t2 - t1;
+    times[2] = t3 - t2;
+  }
+  return 0;
+}
+
+static void apply_kbc(Model& M, double t);
+
+/* Prescribed-increment predictor of a load step (the GPU path's
+ * tg_predict_prescribed): with u at the last converged state and du_p the
+ * jump of the prescribed values to time t, solves
+ * K(u) du_f = R(u) - K(u) [du_p] on the free dofs (Jacobi CG to lin_tol),
+ * then sets u_p to the new values and u_f += du_f.  History is untouched. */
+int orc_predict(void* m, double t, double lin_tol, int max_it, int* pcg_its) {
+  Model* M = static_cast<Model*>(m);
+  ensure_setup(*M);
+  const int n = M->neq;
+  const std::vector<double> u_old = M->u;
+  apply_kbc(*M, t);
+  std::vector<double> dup(M->nnd * 3, 0.0);
+  for (int i = 0; i < M->nnd * 3; ++i)
+    if (M->eqnos[i] <= 0) dup[i] = M->u[i] - u_old[i];
+  const std::vector<double> u_new_p = M->u;
+  M->u = u_old;
+  std::vector<double> R(n, 0.0), Kv(n, 0.0), val(M->bindx.size(), 0.0);
+  if (form(*M, M->u.data(), t, -1, R.data(), val.data(), dup.data(), Kv.data())) return -1;
+  for (int i = 0; i < n; ++i) R[i] -= Kv[i];
+  std::vector<double> du(n, 0.0);
+  const int its = pcg_any(*M, val.data(), R.data(), du.data(), lin_tol, max_it, nullptr);
+  if (its < 0) return -2;
+  for (int i = 0; i < M->nnd * 3; ++i) {
+    if (M->eqnos[i] > 0) M->u[i] += du[M->eqnos[i] - 1];
+    else M->u[i] = u_new_p[i];
+  }
+  if (pcg_its) *pcg_its = its;
+  return 0;
 }
 
 /* Prescribed displacements at the start of the step ending at time t
@@ -1028,7 +1295,7 @@ int orc_run(void* m, int nsteps, double dt, double rel_tol, double abs_tol, int 
       if (form(*M, M->u.data(), t, iteration, nullptr, val.data())) return step;
       std::fill(du.begin(), du.end(), 0.0);
       int s = (solver == 0) ? dense_solve(*M, val.data(), R.data(), du.data())
-                            : (pcg(*M, val.data(), R.data(), du.data(), lin_tol, 100000, nullptr) < 0 ? -1 : 0);
+                            : (pcg_any(*M, val.data(), R.data(), du.data(), lin_tol, 100000, nullptr) < 0 ? -1 : 0);
       if (s) return step;
       for (int i = 0; i < M->nnd * 3; ++i)
         if (M->eqnos[i] > 0) M->u[i] += du[M->eqnos[i] - 1];
@@ -1106,7 +1373,7 @@ int newton_step(Model* M, double t, double rel_tol, double abs_tol, int max_its,
     if (form(*M, M->u.data(), t, iteration, nullptr, val.data())) return 1;
     std::fill(du.begin(), du.end(), 0.0);
     int s = (solver == 0) ? dense_solve(*M, val.data(), R.data(), du.data())
-                          : (pcg(*M, val.data(), R.data(), du.data(), lin_tol, 100000, nullptr) < 0 ? -1 : 0);
+                          : (pcg_any(*M, val.data(), R.data(), du.data(), lin_tol, 100000, nullptr) < 0 ? -1 : 0);
     if (s) return 1;
     for (int i = 0; i < M->nnd * 3; ++i)
       if (M->eqnos[i] > 0) M->u[i] += du[M->eqnos[i] - 1];

@@ -78,6 +78,18 @@ int orc_msr_multx(void* m, const double* val, const double* x, double* y);
 int orc_pcg(void* m, const double* val, const double* b, double* x, double rel_tol, int max_it,
             double* rel_res);
 
+/* R = Fext - Fint at the held displacement (kept for orc_newton_iteration). */
+int orc_residual(void* m, double t, int iteration, double* norm);
+/* One Newton iteration from the held displacement and residual: tangent +
+ * MSR assembly, Jacobi CG to lin_tol, u += du, new residual at
+ * iteration + 1 (*norm).  times (may be NULL): seconds of the tangent pass,
+ * the CG and the residual pass.  The CG runs on orc_set_threads threads. */
+int orc_newton_iteration(void* m, double t, int iteration, double lin_tol, int max_it, int* pcg_its, double* norm,
+                         double* times);
+/* Prescribed-increment predictor to time t: K(u) du_f = R(u) - K(u)[du_p]
+ * on the free dofs (Jacobi CG to lin_tol), then u_p = new values, u_f += du_f. */
+int orc_predict(void* m, double t, double lin_tol, int max_it, int* pcg_its);
+
 /* Newton (NLSolver) over nsteps load steps with time step dt.
  * solver: 0 dense Cholesky, 1 Jacobi PCG (lin_tol).  u_hist: nsteps*nnd*3
  * nodal displacements after each converged step; its_hist: Newton iterations

@@ -56,6 +56,9 @@ def lib():
             ("orc_get_u", [_dp]),
             ("orc_set_u", [_dp]),
             ("orc_close_step", []),
+            ("orc_residual", [ctypes.c_double, ctypes.c_int, _dp]),
+            ("orc_newton_iteration", [ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, _ip, _dp, _dp]),
+            ("orc_predict", [ctypes.c_double, ctypes.c_double, ctypes.c_int, _ip]),
         ]:
             f = getattr(L, name)
             f.restype = ctypes.c_int
@@ -244,6 +247,32 @@ class OracleModel:
 
     def close_step(self):
         lib().orc_close_step(self.h)
+
+    def residual(self, t, iteration=-1):
+        """||R|| at the held displacement; R is kept for newton_iteration."""
+        nrm = ctypes.c_double(0)
+        if lib().orc_residual(self.h, float(t), int(iteration), ctypes.byref(nrm)):
+            raise RuntimeError("oracle residual failed")
+        return nrm.value
+
+    def newton_iteration(self, t, iteration, lin_tol, max_it=100000):
+        """One Newton iteration from the held state: (CG iterations, new
+        ||R||, seconds of [tangent pass, CG, residual pass])."""
+        its = ctypes.c_int(0)
+        nrm = ctypes.c_double(0)
+        tm = np.zeros(3)
+        s = lib().orc_newton_iteration(self.h, float(t), int(iteration), float(lin_tol), int(max_it),
+                                       ctypes.byref(its), ctypes.byref(nrm), _d(tm))
+        if s:
+            raise RuntimeError("oracle Newton iteration failed (%d)" % s)
+        return its.value, nrm.value, tm
+
+    def predict(self, t, lin_tol, max_it=100000):
+        """Prescribed-increment predictor to time t; returns CG iterations."""
+        its = ctypes.c_int(0)
+        if lib().orc_predict(self.h, float(t), float(lin_tol), int(max_it), ctypes.byref(its)):
+            raise RuntimeError("oracle predictor failed")
+        return its.value
 
 
 def model_from_fixture(fx, threads=1):

@@ -482,27 +482,20 @@ int tg_sizes(const tg_context* c, int* neq, long long* nnzb) {
 int tg_pattern_build(tg_context* c, int upper_only, int* row_ptr, int* col_idx, long long* nnz) {
   if (!c || c->nnd <= 0) return TG_ERR_ARG;
   if (set_device(c) || ensure_host_mesh(c)) return TG_ERR_CUDA;
-  const int* eq = c->h_eqnos.data();
-  long long count = 0;
-  if (row_ptr) row_ptr[0] = 0;
-  int row = 0;
-  for (int I = 0; I < c->nnd; ++I)
-    for (int p = 0; p < 3; ++p) {
-      const int r = eq[I * 3 + p];
-      if (r <= 0) continue;
-      for (int k = c->h_rowptr[I]; k < c->h_rowptr[I + 1]; ++k) {
-        const int J = c->h_col[k];
-        for (int q = 0; q < 3; ++q) {
-          const int cc = eq[J * 3 + q];
-          if (cc <= 0 || (upper_only && cc < r)) continue;
-          if (col_idx) col_idx[count] = cc - 1;
-          ++count;
-        }
-      }
-      ++row;
-      if (row_ptr) row_ptr[row] = (int)count;
-    }
-  if (nnz) *nnz = count;
+  expand_pattern(c->nnd, c->h_eqnos.data(), c->h_rowptr, c->h_col, upper_only != 0, row_ptr, col_idx, nnz);
+  return TG_OK;
+}
+
+// The same structure from the mesh alone, on the host (no context, no GPU):
+// the node-block pattern tg_mesh_upload builds, expanded the same way.
+int tg_pattern_build_host(int nnd, int nel, const int* conn, const int* eqnos, int upper_only, int* row_ptr,
+                          int* col_idx, long long* nnz) {
+  if (nnd <= 0 || nel < 0 || !conn || !eqnos || !nnz) return TG_ERR_ARG;
+  for (long long k = 0; k < (long long)nel * 8; ++k)
+    if (conn[k] < 0 || conn[k] >= nnd) return TG_ERR_ARG;
+  std::vector<int> rowptr, col;
+  build_block_pattern(nnd, nel, conn, rowptr, col);
+  expand_pattern(nnd, eqnos, rowptr, col, upper_only != 0, row_ptr, col_idx, nnz);
   return TG_OK;
 }
 

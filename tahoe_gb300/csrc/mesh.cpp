@@ -103,4 +103,32 @@ void build_contrib_map(int nnd, int nel, const int* conn, const std::vector<int>
   for (size_t k = 0; k < dest.size(); ++k) contrib[fill[dest[k]]++] = (int)k;
 }
 
+// Scalar CSR over the active equations from the node-block pattern: row r
+// (equation r+1) lists the equations of the dofs of every node coupled to its
+// node, ascending, prescribed dofs left out (and, with upper_only, columns
+// below the diagonal).  row_ptr / col_idx may be NULL (count only).
+void expand_pattern(int nnd, const int* eq, const std::vector<int>& rowptr, const std::vector<int>& col,
+                    bool upper_only, int* row_ptr, int* col_idx, long long* nnz) {
+  long long count = 0;
+  if (row_ptr) row_ptr[0] = 0;
+  int row = 0;
+  for (int I = 0; I < nnd; ++I)
+    for (int p = 0; p < 3; ++p) {
+      const int r = eq[I * 3 + p];
+      if (r <= 0) continue;
+      for (int k = rowptr[I]; k < rowptr[I + 1]; ++k) {
+        const int J = col[k];
+        for (int q = 0; q < 3; ++q) {
+          const int cc = eq[J * 3 + q];
+          if (cc <= 0 || (upper_only && cc < r)) continue;
+          if (col_idx) col_idx[count] = cc - 1;
+          ++count;
+        }
+      }
+      ++row;
+      if (row_ptr) row_ptr[row] = (int)count;
+    }
+  if (nnz) *nnz = count;
+}
+
 }  // namespace tg

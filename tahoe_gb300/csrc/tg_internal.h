@@ -235,6 +235,8 @@ __host__ __device__ inline long long blob_tile_bytes(int nrows, int nb, int elem
   return 16 + 4LL * ceil4(nrows + 1) + 4LL * ceil4(nb) + 9LL * pstride * elem;
 }
 void build_node_elem(int nnd, int nel, const int* conn, std::vector<int>& ptr, std::vector<int>& list);
+void expand_pattern(int nnd, const int* eq, const std::vector<int>& rowptr, const std::vector<int>& col,
+                    bool upper_only, int* row_ptr, int* col_idx, long long* nnz);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----
 int launch_residual(Context* c);          // fint per element + gather + norm

@@ -58,6 +58,8 @@ _SIGS = {
     "tg_set_external_force": (ctypes.c_int, [_vp, _dp]),
     "tg_set_load_factor": (ctypes.c_int, [_vp, ctypes.c_double]),
     "tg_traction_forces": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _dp, _dp]),
+    "tg_pattern_build_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.c_int, _ip, _ip,
+                                             ctypes.POINTER(ctypes.c_longlong)]),
     "tg_set_iteration": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_form_residual": (ctypes.c_int, [_vp, _dp, _dp]),
     "tg_form_tangent": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -484,3 +486,24 @@ def traction_forces(X, conn, elems, facets, tractions):
     if rc != TG_OK:
         raise TahoeError(rc, "tg_traction_forces", "bad arguments")
     return f.reshape(-1, 3)
+
+
+def pattern_host(conn, eqnos, nnd, upper_only=False):
+    """Scalar CSR (row_ptr, col_idx) of the active equations computed on the
+    host from the mesh alone (tg_pattern_build_host; no GPU needed)."""
+    L = load()
+    conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 8)
+    eq = np.ascontiguousarray(eqnos, dtype=np.int32).reshape(-1)
+    nnz = ctypes.c_longlong(0)
+    rc = L.tg_pattern_build_host(int(nnd), conn.shape[0], _i(conn), _i(eq), int(upper_only), None, None,
+                                 ctypes.byref(nnz))
+    if rc != TG_OK:
+        raise TahoeError(rc, "tg_pattern_build_host", "bad arguments")
+    neq = int((eq > 0).sum())
+    rp = np.zeros(neq + 1, dtype=np.int32)
+    ci = np.zeros(nnz.value, dtype=np.int32)
+    rc = L.tg_pattern_build_host(int(nnd), conn.shape[0], _i(conn), _i(eq), int(upper_only), _i(rp), _i(ci),
+                                 ctypes.byref(nnz))
+    if rc != TG_OK:
+        raise TahoeError(rc, "tg_pattern_build_host", "bad arguments")
+    return rp, ci

@@ -66,3 +66,24 @@ def rel_err(a, b):
     b = np.asarray(b)
     s = max(np.abs(b).max(), 1e-300)
     return float(np.abs(a - b).max() / s)
+
+
+def oracle_rve(n, F):
+    """One RVE of side n under the affine boundary displacement (F - I) X,
+    solved by the oracle's Newton with its direct solve; returns the
+    displacements and the averaged first Piola stress from the reactions,
+    (1/V0) sum_{boundary a} f_a (x) X_a."""
+    from tahoe_gb300 import rve
+    t = rve.template(n)
+    o = OracleModel(t.X, t.conn, "total_lagrangian", [rve.MATRIX, rve.INCLUSION], blocks=t.blocks)
+    o.set_schedule([(0.0, 1.0)])
+    U = t.X @ (F - np.eye(3)).T
+    for a in t.boundary:
+        for d in range(3):
+            o.add_kbc(int(a), d, float(U[a, d]), True)
+    st, uh, its = o.run(1, 1.0, 1e-12, 1e-15, 20, 1e3, 0)
+    assert st == 0
+    u = uh[-1]
+    f = o.nodal_internal_force(u)
+    P = sum(np.outer(f[a], t.X[a]) for a in t.boundary) / t.vol
+    return u, P

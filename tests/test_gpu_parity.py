@@ -193,28 +193,35 @@ def test_pcg_solves_oracle_system():
         assert rel_err(du, x_o) < 1e-9
 
 
-def test_c1_linear_cube_matches_oracle_and_mixed_within_1e6():
-    """configuration 1 geometry at 8^3: traction load, FP64 vs oracle, mixed vs FP64"""
-    mesh = BoxMesh(8, 8, 8)
-    fixed = [(int(n), d) for n in mesh.face_nodes(2, 0) for d in range(3)]
-    el, fc = mesh.face_facets(2, 1)
-    o = oracle_for(mesh, "small_strain", HOOKE, fixed)
-    for e, f in zip(el, fc):
-        o.add_traction(e, f, [0.0, 0.0, 1.0])
+def test_c1_full_size_matches_oracle_and_mixed_within_1e6():
+    """configuration 1 at its full size (16^3 hex8, 14,739 dofs, traction
+    load, one static step): FP64 against the oracle's Newton with Jacobi CG to
+    1e-14 at 1e-9, mixed against FP64 at 1e-6"""
+    mesh, o, _ = workloads.c1(add=lambda X, conn, form, mat: OracleModel(X, conn, form, [mat], threads=8))
     st, uh, its = o.run(1, 1.0, 1e-12, 1e-14, 5, 10.0, 1, 1e-14)
     assert st == 0
     res = {}
     for prec in (lib.FP64, lib.MIXED):
-        g = SolidModel(mesh.X, mesh.conn, "small_strain", HOOKE)
-        for node, d in fixed:
-            g.add_kbc(node, d)
-        for e, f in zip(el, fc):
-            g.add_traction(e, f, [0.0, 0.0, 1.0])
+        _, g, _ = workloads.c1()
         hist, reps = g.run(1, 1.0, rel_tol=1e-12, abs_tol=1e-14, max_iterations=12, precision=prec,
-                           lin_rel_tol=1e-8 if prec == lib.MIXED else 1e-13)
+                           lin_rel_tol=1e-6 if prec == lib.MIXED else 1e-13, lin_max_it=20000)
         res[prec] = hist[-1]
+        g.ctx.close()
     assert rel_err(res[lib.FP64], uh[0]) < 1e-9
     assert rel_err(res[lib.MIXED], res[lib.FP64]) < 1e-6
+
+
+def test_context_pattern_at_c2_size_equals_host_build():
+    """the pattern a context builds for the full C2 mesh (tg_pattern_build)
+    is the host build's (tg_pattern_build_host, checked against the oracle at
+    this size in tests/test_pattern_cpu.py)"""
+    mesh, g, _ = workloads.c2()
+    g.setup()
+    for upper in (True, False):
+        rp, ci = g.ctx.pattern(upper_only=upper)
+        rph, cih = lib.pattern_host(mesh.conn, g.eqnos, mesh.nnd, upper_only=upper)
+        assert np.array_equal(rp, rph) and np.array_equal(ci, cih)
+    g.ctx.close()
 
 
 def test_c2_style_neo_hookean_steps_match_oracle():

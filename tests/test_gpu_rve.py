@@ -8,27 +8,10 @@ an RVE solved alone equal (1e-6) to the same RVE solved inside a batch.
 import numpy as np
 import pytest
 
-from oracle.pyoracle import OracleModel
 from tahoe_gb300 import lib, rve
-from tests.helpers import rel_err
+from tests.helpers import oracle_rve, rel_err
 
 pytestmark = pytest.mark.gpu
-
-
-def oracle_rve(n, F):
-    t = rve.template(n)
-    o = OracleModel(t.X, t.conn, "total_lagrangian", [rve.MATRIX, rve.INCLUSION], blocks=t.blocks)
-    o.set_schedule([(0.0, 1.0)])
-    U = t.X @ (F - np.eye(3)).T
-    for a in t.boundary:
-        for d in range(3):
-            o.add_kbc(int(a), d, float(U[a, d]), True)
-    st, uh, its = o.run(1, 1.0, 1e-12, 1e-15, 20, 1e3, 0)
-    assert st == 0
-    u = uh[-1]
-    f = o.nodal_internal_force(u)
-    P = sum(np.outer(f[a], t.X[a]) for a in t.boundary) / t.vol
-    return u, P
 
 
 @pytest.fixture(scope="module")

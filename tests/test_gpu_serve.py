@@ -1,12 +1,13 @@
 """Served RVE stream on the GPU: a Poisson trace through two lanes with
 continuous batching, mixed precision; every request's averaged first Piola
-stress equals (1e-6) the same RVE solved alone, one at a time, in FP64, and
-the lanes actually batched and overlapped."""
+stress equals (1e-6) the same RVE solved alone, one at a time, in FP64, a
+sample of the served requests equals (1e-6) the oracle's solve of the same
+RVE, and the lanes actually batched and overlapped."""
 import numpy as np
 import pytest
 
 from tahoe_gb300 import lib, rve, serve
-from tests.helpers import rel_err
+from tests.helpers import oracle_rve, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -29,6 +30,12 @@ def test_served_stream_equals_one_at_a_time_fp64():
     assert all(b[1] == 1 for b in ref["batches"])
     for r in range(len(ns)):
         assert rel_err(res["P"][r], ref["P"][r]) < 1e-6, (r, int(ns[r]))
+    # served results against the oracle (independent of both GPU paths): the
+    # first requests of each side length in the trace
+    picked = [int(np.nonzero(ns == n)[0][0]) for n in np.unique(ns)][:4]
+    for r in picked:
+        _, Po = oracle_rve(int(ns[r]), Fs[r])
+        assert rel_err(res["P"][r], Po) < 1e-6, (r, int(ns[r]))
 
 
 def test_lane_context_reused_across_batches():
