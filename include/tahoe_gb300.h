@@ -37,7 +37,7 @@ enum tg_status {
   TG_ERR_CAPACITY = -8        /* size above a fixed capacity */
 };
 
-enum tg_formulation { TG_SMALL_STRAIN = 0, TG_TOTAL_LAGRANGIAN = 1 };
+enum tg_formulation { TG_SMALL_STRAIN = 0, TG_TOTAL_LAGRANGIAN = 1, TG_UPDATED_LAGRANGIAN = 2 };
 enum tg_strain_displacement { TG_STRAIN_STANDARD = 0, TG_STRAIN_BBAR = 1 };
 
 enum tg_material_kind {
@@ -80,7 +80,9 @@ long long tg_launch_count(const tg_context* ctx);
  * + GlobalMatrixT::AddEquationSet/Initialize (MSRMatrixT.cpp:35-57). */
 int tg_mesh_upload(tg_context* ctx, int nnd, const double* coords_soa, int nel, const int* conn,
                    const int* eqnos);
-/* small_strain / total_lagrangian (ElementListT.cpp:738,752) */
+/* small_strain / total_lagrangian / updated_lagrangian (ElementListT.cpp:738,
+ * 752; UpdatedLagrangianT.cpp:94-171: gradients and integration weight of the
+ * current configuration, the same weak form as total_lagrangian) */
 int tg_element_set(tg_context* ctx, int formulation);
 /* strain_displacement option of small_strain (SmallStrainT.cpp:46-91,
  * 327-421): TG_STRAIN_STANDARD, or TG_STRAIN_BBAR for the mean-dilatation
@@ -327,6 +329,15 @@ int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
  * barrier after each staged tile; 1 each warp releases the stage on an
  * mbarrier and moves on (results are bitwise the same) */
 int tg_spmv_release(tg_context* ctx, int per_warp);
+/* Storage the single-vector PCG product streams: on = 1 (default) the
+ * symmetric format -- the upper node blocks only, each lower block read as
+ * the transpose of its upper twin (the symmetric MSR storage of
+ * MSRMatrixT.cpp:104-175 applied as in MSRMatrixT::Multx, MSRMatrixT.cpp:385-420),
+ * about 0.63 of the full storage's DRAM bytes; on = 0 the full block storage.
+ * Meshes composed from templates always use the full storage.  tile_blocks:
+ * upper blocks per streamed tile (0 keeps the current value, default 512).
+ * The results equal the full-storage product up to the order of the FP sums. */
+int tg_spmv_symmetric(tg_context* ctx, int on, int tile_blocks);
 /* elements per CTA of the tangent kernel: 2, 4 or 8 (default 8); element
  * matrices are bitwise the same for every choice */
 int tg_tangent_config(tg_context* ctx, int elems_per_block);

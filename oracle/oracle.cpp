@@ -466,7 +466,9 @@ void add_btdb(const double g[3][8], const double D[36], double scale, double* Ke
 
 /* Element Ke and internal force.  Small strain: SmallStrainT::FormKd/FormStiffness
  * (SmallStrainT.cpp:255-324).  Total Lagrangian: TotalLagrangianT::FormKd/
- * FormStiffness (TotalLagrangianT.cpp:40-144).  Returns 0, or -1 on a
+ * FormStiffness (TotalLagrangianT.cpp:40-144).  Updated Lagrangian:
+ * UpdatedLagrangianT::FormKd/FormStiffness (UpdatedLagrangianT.cpp:94-171),
+ * the same weak form evaluated on the current configuration.  Returns 0, or -1 on a
  * non-positive Jacobian (ExceptionT::BadJacobianDet). */
 int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut& out,
             bool update_state) {
@@ -578,14 +580,27 @@ int element(Model& M, int e, const double* u, int iteration, bool wantK, ElemOut
         out.mat[ip][1] = std::sqrt(3.0 * i2);
         out.mat[ip][2] = p;
       }
-      double Fi[9];
-      inv3(F, J, Fi);
-      /* spatial gradients dN/dx_k = sum_J dN/dX_J Finv(J,k) */
       double gx[3][8];
-      for (int k = 0; k < 3; ++k)
-        for (int n = 0; n < 8; ++n)
-          gx[k][n] = g[0][n] * Fi[0 * 3 + k] + g[1][n] * Fi[1 * 3 + k] + g[2][n] * Fi[2 * 3 + k];
-      double scale = wdet * J;
+      double scale;
+      if (M.form == ORC_UPDATED_LAGRANGIAN) {
+        /* UpdatedLagrangianT::SetGlobalShape / FormStiffness / FormKd
+         * (UpdatedLagrangianT.cpp:84-171): the shape functions of the
+         * current configuration x = X + u give dN/dx directly, and the
+         * integration runs over the current volume (w det dx/dxi) */
+        double xe[24];
+        for (int k = 0; k < 24; ++k) xe[k] = Xe[k] + ue[k];
+        const double detc = ip_gradients(xe, ip, gx);
+        if (!(detc > 0.0)) return -1;
+        scale = S.w[ip] * detc;
+      } else {
+        double Fi[9];
+        inv3(F, J, Fi);
+        /* spatial gradients dN/dx_k = sum_J dN/dX_J Finv(J,k) */
+        for (int k = 0; k < 3; ++k)
+          for (int n = 0; n < 8; ++n)
+            gx[k][n] = g[0][n] * Fi[0 * 3 + k] + g[1][n] * Fi[1 * 3 + k] + g[2][n] * Fi[2 * 3 + k];
+        scale = wdet * J;
+      }
       if (wantK) {
         add_btdb(gx, D, scale, out.Ke);
         double sm[9] = {s[0], s[5], s[4], s[5], s[1], s[3], s[4], s[3], s[2]};

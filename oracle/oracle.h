@@ -27,7 +27,7 @@ extern "C" {
 #endif
 
 /* formulations */
-enum { ORC_SMALL_STRAIN = 0, ORC_TOTAL_LAGRANGIAN = 1 };
+enum { ORC_SMALL_STRAIN = 0, ORC_TOTAL_LAGRANGIAN = 1, ORC_UPDATED_LAGRANGIAN = 2 };
 
 /* material kinds (parameter layout in oracle.cpp: orc_set_material) */
 enum {

@@ -13,7 +13,7 @@ from . import build as _build
 _lib = None
 
 MAT_KINDS = {"ss_hookean": 0, "ss_j2": 1, "fs_simo": 2, "fs_stvenant": 3}
-FORMS = {"small_strain": 0, "total_lagrangian": 1}
+FORMS = {"small_strain": 0, "total_lagrangian": 1, "updated_lagrangian": 2}
 J2_PLASTIC, J2_ELASTIC, J2_RESET, J2_UNALLOCATED = 0, 1, 3, 7
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -276,7 +276,10 @@ class OracleModel:
 
 
 def model_from_fixture(fx, threads=1):
-    m = OracleModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], threads=threads,
+    # the deck's own element group (updated_lagrangian decks run the UL element)
+    form = fx.get("reference_element", fx["formulation"])
+    m = OracleModel(fx["X"], fx["conn"], form if form in FORMS else fx["formulation"], fx["material"],
+                    threads=threads,
                     bbar=fx.get("strain_displacement") == "B-bar")
     m.set_schedule(fx["schedule"])
     for n, d, v, s in fx["kbc"]:

@@ -171,6 +171,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->d_blob_off32 = c->d_blob_off64 = nullptr;
   c->d_row_tile = nullptr;
   c->d_tile_row = nullptr;
+  c->sym = SymStore{};  // its buffers went back to the pool with the mesh
   c->d_minv32 = nullptr;
   c->d_minv64 = nullptr;
   c->d_block = nullptr;
@@ -414,6 +415,21 @@ int tg_spmv_release(tg_context* c, int per_warp) {
   return TG_OK;
 }
 
+int tg_spmv_symmetric(tg_context* c, int on, int tile_blocks) {
+  if (!c || (on != 0 && on != 1) || (tile_blocks != 0 && (tile_blocks < 32 || tile_blocks > 4096)))
+    return TG_ERR_ARG;
+  if (c->nnd > 0 && cudaSetDevice(c->device) != cudaSuccess) return TG_ERR_CUDA;
+  c->sym_mode = on;
+  if (tile_blocks) c->sym_tile_blocks = tile_blocks;
+  // the captured PCG chunk bakes in the product
+  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
+  c->pcg_graph = nullptr;
+  c->pcg_graph_key = -1;
+  // values of the current tangent in the (re-)built format
+  if (sym_active(c) && c->tangent_precision >= 0) return sym_convert(c, c->tangent_precision);
+  return TG_OK;
+}
+
 int tg_tangent_config(tg_context* c, int elems_per_block) {
   if (!c || (elems_per_block != 2 && elems_per_block != 4 && elems_per_block != 8)) return TG_ERR_ARG;
   c->tangent_epb = elems_per_block;
@@ -435,7 +451,9 @@ int tg_element_strain_displacement(tg_context* c, int option) {
 }
 
 int tg_element_set(tg_context* c, int formulation) {
-  if (!c || (formulation != TG_SMALL_STRAIN && formulation != TG_TOTAL_LAGRANGIAN)) return TG_ERR_ARG;
+  if (!c || (formulation != TG_SMALL_STRAIN && formulation != TG_TOTAL_LAGRANGIAN &&
+             formulation != TG_UPDATED_LAGRANGIAN))
+    return TG_ERR_ARG;
   c->formulation = formulation;
   c->mats.formulation = formulation;
   return TG_OK;

@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   const bool valid = e < nel;
   if (valid) {
     const int n = conn[e * 8 + ip];
-    if (!geo) {
+    if (!geo || mt.formulation == TG_UPDATED_LAGRANGIAN) {
       sX[le][ip][0] = X[n];
       sX[le][ip][1] = X[nnd + n];
       sX[le][ip][2] = X[2 * nnd + n];
@@ -450,14 +450,34 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
       const double J = det3(F);
       bool okm = J > 0.0;
       if (okm) okm = (m.kind == TG_MAT_FS_SIMO) ? simo<double>(m, F, s, nullptr) : stvenant<double>(m, F, s, nullptr);
+      const double sm[9] = {s[0], s[5], s[4], s[5], s[1], s[3], s[4], s[3], s[2]};
       if (!okm) {
         bad = true;
+      } else if (mt.formulation == TG_UPDATED_LAGRANGIAN) {
+        // UpdatedLagrangianT::FormKd (UpdatedLagrangianT.cpp:145-171): the
+        // shape functions of the current configuration x = X + u give dN/dx
+        // directly; f_a,i = w det(dx/dxi) sigma_ij dN_a/dx_j
+        double xc[8][3];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) xc[a][d] = sX[le][a][d] + sU[le][a][d];
+        double gc[3][8];
+        const double wc = point_gradients<double>(xc, ip, gc);  // weight 1
+        if (!(wc > 0.0)) {
+          bad = true;
+        } else {
+#pragma unroll
+          for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+              f[a][i] = wc * (sm[i * 3 + 0] * gc[0][a] + sm[i * 3 + 1] * gc[1][a] + sm[i * 3 + 2] * gc[2][a]);
+        }
       } else {
         double Fi[9];
         inv3(F, J, Fi);
         const double scale = wdet * J;
         // P/J = sigma F^-T; f_a,i = scale * sigma_ij dN_a/dx_j
-        const double sm[9] = {s[0], s[5], s[4], s[5], s[1], s[3], s[4], s[3], s[2]};
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
           double gx[3];
@@ -670,7 +690,24 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
         const T J = det3(F);
         okm = okm && J > T(0);
         if (okm) okm = (m.kind == TG_MAT_FS_SIMO) ? simo<T>(m, F, s, D) : stvenant<T>(m, F, s, D);
-        if (okm) {
+        if (okm && mt.formulation == TG_UPDATED_LAGRANGIAN) {
+          // UpdatedLagrangianT::FormStiffness (UpdatedLagrangianT.cpp:94-142):
+          // gradients and integration weight of the current configuration
+          // (coordinates relative to node 0: the gradients see differences)
+          T xc[8][3];
+#pragma unroll
+          for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xc[a][d] = sX[le][a][d] + sU[le][a][d];
+          T gc[3][8];
+          const T detc = point_gradients<T>(xc, ip, gc);
+          okm = detc > T(0);
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int a = 0; a < 8; ++a) sG[le][ip][k][a] = gc[k][a];
+          scale = detc;
+        } else if (okm) {
           T Fi[9];
           inv3(F, J, Fi);
 #pragma unroll
@@ -728,7 +765,7 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
   if (e >= nel) return;
   int a, b;
   slot_pair(slot, a, b);
-  const bool tl = mt.formulation == TG_TOTAL_LAGRANGIAN;
+  const bool tl = mt.formulation != TG_SMALL_STRAIN;  // geometric stiffness (TL and UL)
   T K[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) K[k] = T(0);

@@ -509,6 +509,8 @@ struct Grids {
   size_t spmv_smem;
   int stages;
   int warp_release = 0;
+  bool sym = false;  // the product streams the symmetric format (symspmv.cu)
+  SymLaunch sl;
 };
 
 // persistent grid for the streamed SpMV: as many CTAs as fit (shared memory
@@ -554,6 +556,10 @@ int spmv_config_n(Context* c, Grids& g) {
 }
 template <typename T>
 int spmv_config(Context* c, Grids& g) {
+  if (sym_active(c)) {
+    g.sym = true;
+    return sym_config(c, std::is_same<T, float>::value ? TG_MIXED : TG_FP64, g.sl);
+  }
   // the configured ring depth, or 8 stages when 16 do not fit (FP64 tiles)
   int optin = 0;
   if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
@@ -566,6 +572,10 @@ template <typename T>
 void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc) {
   using V = typename Vec4<T>::type;
   const bool f32 = std::is_same<T, float>::value;
+  if (g.sym) {
+    sym_launch(c, f32 ? TG_MIXED : TG_FP64, g.sl, p, q, partials, sc);
+    return;
+  }
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);

@@ -103,6 +103,8 @@ int form_tangent(Context* c, int precision) {
   }
   int s = launch_tangent(c, precision);
   if (!s) s = launch_assemble(c, precision);
+  // the symmetric stream format of the single-vector product
+  if (!s && sym_active(c)) s = sym_convert(c, precision);
   if (!s) s = check_status(c);
   if (!s) c->tangent_precision = precision;
   return s;
@@ -754,7 +756,10 @@ int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
   for (int r = 0; r < reps && !s; ++r) {
     cudaEventRecord(a, c->stream);
     if (which == 2) s = launch_tangent(c, c->tangent_precision);
-    else if (which == 3) s = launch_assemble(c, c->tangent_precision);
+    else if (which == 3) {
+      s = launch_assemble(c, c->tangent_precision);
+      if (!s && sym_active(c)) s = sym_convert(c, c->tangent_precision);
+    }
     else s = launch_residual(c);
     cudaEventRecord(b, c->stream);
     cudaEventSynchronize(b);

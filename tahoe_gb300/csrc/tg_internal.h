@@ -60,6 +60,34 @@ struct ResidScalars {
 
 struct MeshTemplate;  // a resident template mesh (compose.cu)
 
+// Symmetric stream format of the single-vector PCG product (symspmv.cu):
+// upper node blocks only, lower blocks read as transposes of their upper
+// twins.  Structure per tile in d_blob; values V8/V1 indexed by upper id.
+struct SymStore {
+  bool built = false;
+  int ntiles = 0;
+  int tile_blocks = 0;     // upper blocks per tile the structure was built for
+  long long nu = 0, nl = 0;  // upper blocks, lower entries
+  int cap_struct = 0;      // largest tile structure, bytes (rounded to 128)
+  int cap_blocks = 0;      // largest tile, upper blocks
+  int precision = -1;      // precision of the converted values
+  std::vector<long long> h_off;
+  unsigned char* d_blob = nullptr;
+  long long* d_off = nullptr;  // ntiles+1 structure offsets
+  int* d_koff = nullptr;       // ntiles+1 first upper id of each tile
+  int* d_urow = nullptr;       // nnd+1 first upper id of each row
+  int* d_diag = nullptr;       // nnd position of each row's diagonal block in the full CSR
+  float* d_v8_32 = nullptr;    // nu*8
+  float* d_v1_32 = nullptr;    // nu (+16 padding)
+  double* d_v8_64 = nullptr;
+  double* d_v1_64 = nullptr;
+};
+struct SymLaunch {
+  int grid = 0;
+  size_t smem = 0;
+  int stages = 2;
+};
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
@@ -105,6 +133,9 @@ struct Context {
   int spmv_stages = 2;
   int spmv_warp_release = 0;   // 1: per-warp stage release instead of a CTA barrier per tile
   int tangent_epb = 8;         // elements per CTA of the tangent kernel (2, 4, 8)
+  int sym_mode = 1;            // 1: the single-vector product streams the symmetric format (single meshes)
+  int sym_tile_blocks = 512;   // upper blocks per tile of the symmetric format
+  SymStore sym;
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
   std::vector<int> h_rowptr, h_col;
@@ -237,6 +268,15 @@ __host__ __device__ inline long long blob_tile_bytes(int nrows, int nb, int elem
 void build_node_elem(int nnd, int nel, const int* conn, std::vector<int>& ptr, std::vector<int>& list);
 void expand_pattern(int nnd, const int* eq, const std::vector<int>& rowptr, const std::vector<int>& col,
                     bool upper_only, int* row_ptr, int* col_idx, long long* nnz);
+
+// ---- symmetric stream format (symspmv.cu) ----
+bool sym_active(const Context* c);
+int sym_build(Context* c, int tile_blocks);
+int sym_convert(Context* c, int precision);  // values from the last assembly
+int sym_config(Context* c, int precision, SymLaunch& L);
+void sym_launch(Context* c, int precision, const SymLaunch& L, const void* p, void* q, double* partials,
+                PcgScalars* sc);
+void sym_free(Context* c);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----
 int launch_residual(Context* c);          // fint per element + gather + norm

@@ -314,12 +314,13 @@ class Deck:
 
     @property
     def formulation(self):
-        return "small_strain" if self.element == "small_strain" else "total_lagrangian"
+        # the deck's own element group (ElementListT names)
+        if self.element in ("small_strain", "total_lagrangian", "updated_lagrangian"):
+            return self.element
+        return "total_lagrangian"
 
     def model(self, device=0):
         """The deck as a GPU SolidModel (not yet set up)."""
-        if self.torsion:
-            raise ValueError("torsion boundary controller: not on the GPU step loop")
         m = SolidModel(self.X, self.conn, self.formulation, self.material, device=device,
                        strain_displacement=self.strain_displacement)
         for k, pts in self.schedules.items():
@@ -336,6 +337,9 @@ class Deck:
         for t in self.tractions:
             for (e, facet) in self.sidesets[t["side_set"]]:
                 m.add_traction(e, facet, t["t"])
+        for tc in self.torsion:
+            nodes = sorted({n for ns in tc["sets"] for n in self.nodesets[ns]})
+            m.add_torsion(tc["axis"], tc["rate"], tc["point"], nodes)
         return m
 
 

@@ -16,7 +16,7 @@ ERRORS = {
     -1: "TG_ERR_ARG", -2: "TG_ERR_CUDA", -3: "TG_ERR_OOM", -4: "TG_ERR_BAD_JACOBIAN", -5: "TG_ERR_NAN",
     -6: "TG_ERR_NOT_CONVERGED", -7: "TG_ERR_DIVERGED", -8: "TG_ERR_CAPACITY",
 }
-SMALL_STRAIN, TOTAL_LAGRANGIAN = 0, 1
+SMALL_STRAIN, TOTAL_LAGRANGIAN, UPDATED_LAGRANGIAN = 0, 1, 2
 STRAIN_STANDARD, STRAIN_BBAR = 0, 1
 MAT_SS_HOOKEAN, MAT_SS_J2, MAT_FS_SIMO, MAT_FS_STVENANT = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -82,6 +82,7 @@ _SIGS = {
     "tg_timer_stop": (ctypes.c_int, [_vp, _dp]),
     "tg_time_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     "tg_spmv_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "tg_spmv_symmetric": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "tg_tangent_config": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_element_strain_displacement": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_nodal_stress": (ctypes.c_int, [_vp, _dp]),
@@ -456,6 +457,11 @@ class Context:
 
     def spmv_release(self, per_warp):
         self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")
+
+    def spmv_symmetric(self, on, tile_blocks=0):
+        """Symmetric stream format of the single-vector product (on=True,
+        default on single meshes) or the full block storage (on=False)."""
+        self._chk(self.L.tg_spmv_symmetric(self.h, int(bool(on)), int(tile_blocks)), "tg_spmv_symmetric")
 
     def tangent_config(self, elems_per_block):
         self._chk(self.L.tg_tangent_config(self.h, int(elems_per_block)), "tg_tangent_config")

@@ -17,12 +17,11 @@ from .meshgen import equations
 
 # XML names registered by the reference factories (ElementListT.cpp:738,752;
 # SSSolidMatList3DT.cpp:199-207; FSSolidMatList3DT.cpp:409-415) and what the
-# GPU group runs for them.  updated_lagrangian converges to the same
-# displacement field as total_lagrangian for these hyperelastic materials.
+# GPU group runs for them.
 ELEMENT_GROUPS = {
     "small_strain": lib.SMALL_STRAIN,
     "total_lagrangian": lib.TOTAL_LAGRANGIAN,
-    "updated_lagrangian": lib.TOTAL_LAGRANGIAN,
+    "updated_lagrangian": lib.UPDATED_LAGRANGIAN,
 }
 STRAIN_DISPLACEMENT = {"standard": lib.STRAIN_STANDARD, "B-bar": lib.STRAIN_BBAR}
 MATERIALS = {
@@ -79,6 +78,7 @@ class SolidModel:
         self.blocks = None if blocks is None else np.ascontiguousarray(blocks, dtype=np.int32)
         self.schedule = None
         self.kbc = []       # (node, dof, value, scheduled)
+        self.torsions = []  # (axis, rate, point[3], nodes)
         self.forces = []    # (node, dof, value)
         self.tractions = []  # (elem, facet, t3)
         self.device = device
@@ -101,6 +101,45 @@ class SolidModel:
         n = int(scheduled) if not isinstance(scheduled, bool) else (1 if scheduled else 0)
         self.kbc.append((int(node), int(dof), float(value), n))
 
+    def add_torsion(self, axis, rate, point, nodes):
+        """Torsion boundary controller (TorsionKBCT, TorsionKBCT.cpp:39-99,
+        148-180): the nodes turn rigidly about coordinate axis `axis` (0..2)
+        through `point` by theta = rate * t; the two dofs across the axis are
+        prescribed (their values follow the turn of each node's initial
+        position), the dof along it stays free."""
+        if axis not in (0, 1, 2):
+            raise ValueError("torsion axis must be 0, 1 or 2")
+        self.torsions.append((int(axis), float(rate), np.asarray(point, dtype=np.float64).reshape(3),
+                              np.asarray(nodes, dtype=np.int64).reshape(-1)))
+
+    def _torsion_dofs(self):
+        """dof indices (node*3 + dof) the torsion controllers prescribe"""
+        across = {0: (1, 2), 1: (2, 0), 2: (0, 1)}
+        return [int(n) * 3 + d for (axis, _, _, nodes) in self.torsions for n in nodes for d in across[axis]]
+
+    def _torsion_values(self, t):
+        """prescribed values of _torsion_dofs() at time t: the displacement
+        that carries each node's initial position through the rigid turn
+        (radius vector from the axis rotated by theta; nodes on the axis stay)"""
+        across = {0: (1, 2), 1: (2, 0), 2: (0, 1)}
+        out = []
+        for axis, rate, point, nodes in self.torsions:
+            a = np.zeros(3)
+            a[axis] = 1.0
+            X = self.X[nodes]
+            d = X - point
+            r = d - np.outer(d @ a, a)
+            rad = np.linalg.norm(r, axis=1)
+            th = rate * t
+            e1 = np.where(rad[:, None] > 1e-12, r / np.maximum(rad, 1e-300)[:, None], 0.0)
+            e2 = np.cross(a, e1)
+            x = (X - r) + (rad * np.cos(th))[:, None] * e1 + (rad * np.sin(th))[:, None] * e2
+            u = np.where(rad[:, None] > 1e-12, x - X, 0.0)
+            for k in range(len(nodes)):
+                for dd in across[axis]:
+                    out.append(u[k, dd])
+        return np.array(out)
+
     def add_force(self, node, dof, value):
         self.forces.append((int(node), int(dof), float(value)))
 
@@ -108,7 +147,7 @@ class SolidModel:
         self.tractions.append((int(elem), int(facet), [float(x) for x in t]))
 
     def equations(self):
-        idx = [n * 3 + d for (n, d, _, _) in self.kbc]
+        idx = [n * 3 + d for (n, d, _, _) in self.kbc] + self._torsion_dofs()
         return equations(self.X.shape[0], idx)
 
     # set-up ----------------------------------------------------------------
@@ -137,6 +176,7 @@ class SolidModel:
         self._kbc_idx = np.array([n * 3 + d for (n, d, _, _) in self.kbc], dtype=np.int32)
         self._kbc_val = np.array([v for (_, _, v, _) in self.kbc])
         self._kbc_sch = np.array([s for (_, _, _, s) in self.kbc], dtype=np.int64)
+        self._tor_idx = np.array(self._torsion_dofs(), dtype=np.int32)
         return c
 
     def apply_step(self, t, predictor=None):
@@ -148,11 +188,16 @@ class SolidModel:
         scheds = getattr(self, "schedules", {1: self.schedule})
         factors = np.array([0.0] + [schedule_value(scheds.get(n), t) for n in range(1, max(scheds, default=1) + 1)])
         vals = np.where(self._kbc_sch > 0, factors[np.minimum(self._kbc_sch, len(factors) - 1)] * self._kbc_val, 0.0)
+        idx = self._kbc_idx
+        if len(self._tor_idx):
+            # torsion controllers: values of the rigid turn at time t
+            idx = np.concatenate([idx, self._tor_idx]).astype(np.int32)
+            vals = np.concatenate([vals, self._torsion_values(t)])
         if predictor is not None:
             prec, pc, tol = predictor
-            return self.ctx.predict_prescribed(self._kbc_idx, vals, precision=prec, precond=pc, lin_rel_tol=tol)
-        if len(self._kbc_idx):
-            self.ctx.set_prescribed(self._kbc_idx, vals)
+            return self.ctx.predict_prescribed(idx, vals, precision=prec, precond=pc, lin_rel_tol=tol)
+        if len(idx):
+            self.ctx.set_prescribed(idx, vals)
         return 0
 
     def run(self, nsteps, dt, rel_tol=1e-12, abs_tol=1e-10, max_iterations=10, div_tol=10.0, precision=lib.FP64,
@@ -180,6 +225,10 @@ class SolidModel:
         step_num, num_steps, cuts, status, quick = first_step - 1, nsteps, 0, "same", 0
         tstep, t = float(dt), (first_step - 1) * float(dt)
         self.step_cuts = 0
+        # Newton iterations per original step, failed attempts included (what
+        # the step sequence spends; converged sub-steps alone are in reports)
+        self.newton_per_step = []
+        spent = 0
         sub = []
         while step_num < num_steps:
             if status == "decrease":
@@ -199,6 +248,7 @@ class SolidModel:
             self.apply_step(t, (precision, precond, lin_rel_tol) if predictor else None)
             rc, rep = c.newton(rel_tol, abs_tol, div_tol, max_iterations, precision, precond, lin_rel_tol, lin_max_it,
                                check=False)
+            spent += rep.iterations
             if rc != lib.TG_OK:
                 # bad Jacobian, non-finite values, no convergence, divergence:
                 # NLSolver's kFailed, answered by a step cut; anything else
@@ -231,16 +281,23 @@ class SolidModel:
             if k >= 1 and abs(t - k * dt) <= 1e-9 * dt:
                 hist.append(c.get_u())
                 reports.append(sub[0] if len(sub) == 1 else sub)
+                self.newton_per_step.append(spent)
+                spent = 0
                 sub = []
         return np.array(hist), reports
 
 
 def model_from_fixture(fx, device=0):
-    m = SolidModel(fx["X"], fx["conn"], fx["formulation"], fx["material"], device=device,
+    # the deck's own element group (updated_lagrangian decks run the UL element)
+    form = fx.get("reference_element", fx["formulation"])
+    m = SolidModel(fx["X"], fx["conn"], form if form in ELEMENT_GROUPS else fx["formulation"], fx["material"],
+                   device=device,
                    strain_displacement=fx.get("strain_displacement", "standard"))
     m.set_schedule(fx["schedule"])
     for n, d, v, s in fx["kbc"]:
         m.add_kbc(n, d, v, s)
+    for axis, rate, px, py, pz, nodes in fx.get("torsion", []):
+        m.add_torsion(axis, rate, [px, py, pz], nodes)
     for n, d, v in fx.get("forces", []):
         m.add_force(n, d, v)
     for row in fx.get("tractions", []):

@@ -104,10 +104,11 @@ def test_large_strain_hookean_reads_as_st_venant_or_is_rejected():
         pass
 
 
-def test_torsion_controller_is_read_and_refused_by_the_gpu_step_loop(tmp_path):
+def test_torsion_controller_is_read_and_mapped_onto_the_model(tmp_path):
     """A deck with the reference's torsion controller: the axis, rate, point
-    and node sets are read (the oracle runs it); the GPU step loop refuses
-    it explicitly rather than dropping the rotation."""
+    and node sets are read, and the GPU model prescribes the two dofs across
+    the axis of every node of the sets with the rigid turn of its initial
+    position (distance to the axis kept, angle rate * t; TorsionKBCT)."""
     import shutil
     with open(os.path.join(DECKS, "cube8_j2.xml")) as f:
         xml = f.read()
@@ -119,8 +120,21 @@ def test_torsion_controller_is_read_and_refused_by_the_gpu_step_loop(tmp_path):
     path.write_text(xml)
     d = dk.Deck(str(path))
     assert d.torsion == [{"axis": 2, "rate": 0.5, "point": [0.5, 0.5, 0.0], "sets": [2]}]
-    try:
-        d.model()
-        raise AssertionError("torsion deck accepted by the GPU step loop")
-    except ValueError:
-        pass
+    m = d.model()
+    nodes = sorted(d.nodesets[2])
+    assert len(m.torsions) == 1 and list(m.torsions[0][3]) == nodes
+    idx = m._torsion_dofs()
+    assert idx == [n * 3 + dd for n in nodes for dd in (0, 1)]
+    eq = m.equations()
+    assert all(eq.reshape(-1)[i] <= 0 for i in idx)  # prescribed
+    t = 0.7
+    u = m._torsion_values(t).reshape(-1, 2)
+    X = d.X[nodes]
+    r0 = X[:, :2] - 0.5
+    r1 = r0 + u
+    assert np.allclose(np.linalg.norm(r1, axis=1), np.linalg.norm(r0, axis=1), atol=1e-14)
+    turned = np.linalg.norm(r0, axis=1) > 1e-12
+    ang = np.arctan2(r1[:, 1], r1[:, 0]) - np.arctan2(r0[:, 1], r0[:, 0])
+    ang = (ang + np.pi) % (2 * np.pi) - np.pi
+    assert np.allclose(ang[turned], 0.5 * t, atol=1e-13)
+    assert np.all(u[~turned] == 0.0)

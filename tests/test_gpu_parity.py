@@ -89,7 +89,8 @@ def test_equations_and_pattern_bit_exact(jitter):
 
 
 @pytest.mark.parametrize("formulation,material,scale", [
-    ("small_strain", HOOKE, 1e-3), ("total_lagrangian", SIMO, 0.05), ("total_lagrangian", STV, 0.05)])
+    ("small_strain", HOOKE, 1e-3), ("total_lagrangian", SIMO, 0.05), ("total_lagrangian", STV, 0.05),
+    ("updated_lagrangian", SIMO, 0.05), ("updated_lagrangian", STV, 0.05)])
 def test_element_matrices_match_oracle(formulation, material, scale):
     mesh, fixed = cube_case(3, jitter=0.2, seed=11)
     o = oracle_for(mesh, formulation, material, fixed)
@@ -137,7 +138,7 @@ def test_bbar_element_matrices_and_assembly_match_oracle():
 
 
 @pytest.mark.parametrize("formulation,material,scale", [
-    ("small_strain", HOOKE, 1e-3), ("total_lagrangian", SIMO, 0.05)])
+    ("small_strain", HOOKE, 1e-3), ("total_lagrangian", SIMO, 0.05), ("updated_lagrangian", SIMO, 0.05)])
 @pytest.mark.parametrize("precision", [lib.FP64, lib.MIXED])
 def test_assembled_tangent_and_residual(formulation, material, scale, precision):
     mesh, fixed = cube_case(4, jitter=0.2, seed=2)
@@ -162,6 +163,45 @@ def test_assembled_tangent_and_residual(formulation, material, scale, precision)
     assert rel_err(v, want) < tol
 
 
+def test_updated_lagrangian_newton_iterates_match_oracle():
+    """The updated-Lagrangian element inside Newton: every iteration's
+    residual norm of a finite compression step (large-strain St.Venant, a
+    jittered 4^3 block) against the oracle's UL restatement, and the same
+    iterates as the total-Lagrangian element (one weak form, two
+    evaluations)."""
+    mesh = BoxMesh(4, 4, 4, jitter=0.2, seed=5)
+    bottom, top = mesh.face_nodes(2, 0), mesh.face_nodes(2, 1)
+    norms = {}
+    for form in ("updated_lagrangian", "total_lagrangian"):
+        o = oracle_for(mesh, form, STV, [])
+        g = SolidModel(mesh.X, mesh.conn, form, STV)
+        for m in (o, g):
+            for n in bottom:
+                for d in range(3):
+                    m.add_kbc(n, d, 0.0, False)
+            for n in top:
+                m.add_kbc(n, 2, 0.0, False)
+        g.setup()
+        eq, _ = o.equations()
+        u = np.zeros((mesh.nnd, 3))
+        u[top, 2] = -0.01
+        o.set_u(u)
+        g.ctx.set_u(u)
+        g.ctx.set_iteration(-1)
+        _, n_g = g.ctx.residual(want_vector=True)
+        seq = []
+        for it in range(4):
+            n_o = o.residual(1.0, it - 1)
+            assert abs(n_g - n_o) <= 1e-12 * max(n_o, 1e-300), (form, it)
+            seq.append(n_g)
+            n_g, _ = g.ctx.newton_iteration(precision=lib.FP64, lin_rel_tol=1e-13, lin_max_it=20000)
+            o.newton_iteration(1.0, it - 1, 1e-13)
+            assert rel_err(g.ctx.get_u(), o.get_u()) < 1e-10, (form, it)
+        norms[form] = seq
+        g.ctx.close()
+    assert rel_err(norms["updated_lagrangian"], norms["total_lagrangian"]) < 1e-10
+
+
 def test_assembly_and_residual_bitwise_repeatable():
     mesh, fixed = cube_case(6, jitter=0.2, seed=4)
     g = gpu_model(mesh, "total_lagrangian", SIMO, fixed)
@@ -174,6 +214,36 @@ def test_assembly_and_residual_bitwise_repeatable():
         outs.append((R.copy(), v.copy()))
     assert np.array_equal(outs[0][0], outs[1][0])
     assert np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("tile_blocks", [512, 32])
+def test_symmetric_product_equals_full_storage(tile_blocks):
+    """The single-vector product streaming the symmetric format (upper blocks,
+    lower blocks as transposes, output masked at prescribed dofs) gives the
+    PCG solution of the full block storage: FP64 to 1e-11, the mixed form to
+    1e-5, the same iteration count within two; a small tile size spreads the
+    rows over many tiles (transposed blocks from other tiles)."""
+    mesh, fixed = cube_case(6, jitter=0.2, seed=4)
+    g = gpu_model(mesh, "total_lagrangian", SIMO, fixed)
+    u = random_u(mesh.nnd, 0.02, 3)
+    for node, d in fixed:
+        u[node, d] = 0.0
+    g.ctx.set_u(u)
+    R, _ = g.ctx.residual()
+    for prec, tol, lt in ((lib.FP64, 1e-11, 1e-12), (lib.MIXED, 1e-5, 1e-6)):
+        g.ctx.tangent(prec)
+        res = {}
+        for on in (0, 1):
+            g.ctx.spmv_symmetric(on, tile_blocks)
+            for pc in (lib.PRECOND_JACOBI, lib.PRECOND_BLOCK_JACOBI):
+                du, its, rr, rc = g.ctx.pcg(R, rel_tol=lt, max_it=20000, precond=pc)
+                assert rc == 0 and rr < lt
+                res[on, pc] = (du, its)
+            assert g.ctx.time_kernel(0, 2) > 0.0
+        for pc in (lib.PRECOND_JACOBI, lib.PRECOND_BLOCK_JACOBI):
+            assert rel_err(res[1, pc][0], res[0, pc][0]) < tol, (prec, pc)
+            assert abs(res[1, pc][1] - res[0, pc][1]) <= 2, (prec, pc)
+    g.ctx.spmv_symmetric(1, 512)
 
 
 def test_pcg_solves_oracle_system():
