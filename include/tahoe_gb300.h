@@ -277,11 +277,23 @@ int tg_segment_residual_norms(tg_context* ctx, double* norms);
  * at equilibrium to the reaction sum sum_{boundary a} f_a (x) X_a; P is
  * nseg*9 row-major (P_iJ), vol0 the reference volumes (NULL: no division) */
 int tg_segment_average_stress(tg_context* ctx, const double* vol0, double* P);
-/* Newton over the whole batch with NLSolver's exit test applied to every RVE
- * (relative to that RVE's first residual); iterates until all converge.
- * seg_rel (nseg, may be NULL) receives each RVE's final relative residual. */
+/* Newton over the whole batch with NLSolver's exit test (NLSolver.cpp:675-755)
+ * applied to every RVE, relative to that RVE's first residual.  With per-RVE
+ * Krylov solves (tg_segment_solver, default) every RVE runs its own PCG over
+ * the shared matrix stream; an RVE that has converged, diverged, reached the
+ * iteration limit or whose PCG broke down is frozen and reported on its own,
+ * and the others continue.  seg_rel (nseg, may be NULL) receives each RVE's
+ * final relative residual, seg_status (nseg, may be NULL) TG_OK or the RVE's
+ * failure code; the return is TG_OK when every RVE converged, else the first
+ * RVE failure code (CUDA and argument errors end the batch). */
 int tg_newton_solve_segmented(tg_context* ctx, const tg_newton_params* params, tg_newton_report* report,
-                              double* seg_rel);
+                              double* seg_rel, int* seg_status);
+/* Krylov solves of a segmented batch: per_rve = 1 (default) one PCG per RVE
+ * (own scaling, alpha, beta, tolerance relative to its own residual,
+ * convergence and breakdown; the solution of an RVE does not depend on the
+ * batch it shares, bitwise), per_rve = 0 one PCG over the whole batch (shared
+ * scalars, one tolerance).  No reference counterpart (FE^2 batching). */
+int tg_segment_solver(tg_context* ctx, int per_rve);
 /* Consistent macro tangent dP/dF of every RVE at the current (converged)
  * state, by static condensation onto the prescribed boundary dofs: for each
  * of the nine unit perturbations dF = e_k (x) e_L the interior response

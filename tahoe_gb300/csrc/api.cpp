@@ -33,6 +33,7 @@ namespace {
 void free_device(Context* c) {
   // the caller's timer events outlive mesh changes (a timed region may
   // cover composing a batch mesh)
+  seg_free(c);
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
   c->ckpt_valid = false;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
@@ -42,6 +43,7 @@ void free_device(Context* c) {
 }
 
 void free_all(Context* c) {
+  seg_free(c);
   if (c->ev_a) cudaEventDestroy(c->ev_a);
   if (c->ev_b) cudaEventDestroy(c->ev_b);
   c->ev_a = c->ev_b = nullptr;
@@ -427,6 +429,12 @@ int tg_spmv_symmetric(tg_context* c, int on, int tile_blocks) {
   c->pcg_graph_key = -1;
   // values of the current tangent in the (re-)built format
   if (sym_active(c) && c->tangent_precision >= 0) return sym_convert(c, c->tangent_precision);
+  return TG_OK;
+}
+
+int tg_segment_solver(tg_context* c, int per_rve) {
+  if (!c || (per_rve != 0 && per_rve != 1)) return TG_ERR_ARG;
+  c->seg_pcg_mode = per_rve;
   return TG_OK;
 }
 

@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
 template <typename T>
 __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
                                                const typename Vec4<T>::type* __restrict__ p,
-                                               typename Vec4<T>::type* __restrict__ q, Acc<T>& v0) {
+                                               typename Vec4<T>::type* __restrict__ q, Acc<T>& v0,
+                                               double* __restrict__ node_dot) {
   using V = typename Vec4<T>::type;
   const int sub = lane & 7;
   Acc<T>* v = &v0;
@@ -173,6 +174,13 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
       v[0].add_prod(pi.x, a0);
       v[0].add_prod(pi.y, a1);
       v[0].add_prod(pi.z, a2);
+      if (node_dot) {  // the row's own p.q (per-RVE reductions of a segmented batch)
+        Acc<T> d;
+        d.add_prod(pi.x, a0);
+        d.add_prod(pi.y, a1);
+        d.add_prod(pi.z, a2);
+        node_dot[I] = d.value();
+      }
     }
   }
 }
@@ -189,7 +197,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
                                                        const unsigned char* __restrict__ blob, int cap,
                                                        const typename Vec4<T>::type* __restrict__ p,
                                                        typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                       PcgScalars* sc, int* status) {
+                                                       PcgScalars* sc, int* status, double* node_dot) {
   using V = typename Vec4<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
@@ -234,7 +242,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
       stuck = s;
       break;
     }
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0]);
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0], node_dot);
     __syncthreads();  // stage s is free for the copy issued next iteration
   }
   if (stuck >= 0 && threadIdx.x == 0) {
@@ -248,6 +256,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
     sc->done = 2;
     sc->fail = 5;
   }
+  // a segmented batch reduces the rows' own products per RVE instead
+  if (node_dot) return;
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -272,7 +282,7 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
                                                           const unsigned char* __restrict__ blob, int cap,
                                                           const typename Vec4<T>::type* __restrict__ p,
                                                           typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                          PcgScalars* sc, int* status) {
+                                                          PcgScalars* sc, int* status, double* node_dot) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NST];
   __shared__ __align__(8) uint64_t empty[NST];
@@ -338,7 +348,7 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
       break;
     }
     if (threadIdx.x == 0) ++seen[s];
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0]);
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0], node_dot);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
@@ -352,6 +362,8 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
     sc->done = 2;
     sc->fail = 5;
   }
+  // a segmented batch reduces the rows' own products per RVE instead
+  if (node_dot) return;
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -504,14 +516,7 @@ __global__ void __launch_bounds__(256, 2) pcg_update_kernel(int nnd, const T* __
   }
 }
 
-struct Grids {
-  int spmv, vec;
-  size_t spmv_smem;
-  int stages;
-  int warp_release = 0;
-  bool sym = false;  // the product streams the symmetric format (symspmv.cu)
-  SymLaunch sl;
-};
+using Grids = SpmvPlan;
 
 // persistent grid for the streamed SpMV: as many CTAs as fit (shared memory
 // bound), at most one per tile
@@ -569,17 +574,18 @@ int spmv_config(Context* c, Grids& g) {
   return g.stages == 3 ? spmv_config_n<T, 3>(c, g) : spmv_config_n<T, 2>(c, g);
 }
 template <typename T>
-void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc) {
+void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc,
+                 double* node_dot = nullptr) {
   using V = typename Vec4<T>::type;
   const bool f32 = std::is_same<T, float>::value;
   if (g.sym) {
-    sym_launch(c, f32 ? TG_MIXED : TG_FP64, g.sl, p, q, partials, sc);
+    sym_launch(c, f32 ? TG_MIXED : TG_FP64, g.sl, p, q, partials, sc, node_dot);
     return;
   }
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);
-#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status
+#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot
   if (g.warp_release) {
     if (g.stages == 3)
       pcg_spmv_wr_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
@@ -974,8 +980,27 @@ int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsig
   return solve_scratch_t<double>(c, d_rhs_eq, d_du_eq, scratch, rel_tol, max_it, precond, iters, rel_res);
 }
 
+int pcg_vectors(Context* c, int precision) {
+  return precision == TG_MIXED ? ensure_vectors<float>(c, precision) : ensure_vectors<double>(c, precision);
+}
+
+int spmv_plan(Context* c, int precision, SpmvPlan& P) {
+  P = grids(c);
+  return precision == TG_MIXED ? spmv_config<float>(c, P) : spmv_config<double>(c, P);
+}
+
+void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void* q, double* partials, PcgScalars* sc,
+              double* node_dot) {
+  if (precision == TG_MIXED)
+    launch_spmv<float>(c, P, p, q, partials, sc, node_dot);
+  else
+    launch_spmv<double>(c, P, p, q, partials, sc, node_dot);
+}
+
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
               double* rel_res) {
+  // a batch of RVEs: one Krylov solve per RVE over the shared matrix stream
+  if (c->nseg > 0 && c->seg_pcg_mode) return pcg_solve_segmented(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
   if (c->tangent_precision == TG_MIXED) return solve_t<float>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
   if (c->tangent_precision == TG_FP64) return solve_t<double>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
   c->err = "tg_pcg_solve: no tangent formed";

@@ -573,6 +573,7 @@ int tg_set_segments(tg_context* c, int nseg, const int* node_off, const int* ele
     if (*p) dfree(c, *p);
     *p = nullptr;
   }
+  seg_free(c);  // the per-RVE solve's chunks follow the partition
   c->nseg = nseg;
   c->h_seg_node.assign(node_off, node_off + nseg + 1);
   c->h_seg_elem.assign(elem_off, elem_off + nseg + 1);
@@ -641,7 +642,8 @@ int tg_segment_macro_tangent(tg_context* c, const tg_newton_params* P, const dou
   return s;
 }
 
-int tg_newton_solve_segmented(tg_context* c, const tg_newton_params* P, tg_newton_report* rep, double* seg_rel) {
+int tg_newton_solve_segmented(tg_context* c, const tg_newton_params* P, tg_newton_report* rep, double* seg_rel,
+                              int* seg_status) {
   if (!c || !P || c->nseg <= 0) return TG_ERR_ARG;
   if (P->precision != TG_FP64 && P->precision != TG_MIXED) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
@@ -649,51 +651,98 @@ int tg_newton_solve_segmented(tg_context* c, const tg_newton_params* P, tg_newto
   std::memset(&r, 0, sizeof(r));
   PhaseTimer tm(rep != nullptr);
   c->iteration = -1;
-  std::vector<double> n0(c->nseg), nk(c->nseg);
+  const int ns = c->nseg;
+  std::vector<double> n0(ns), nk(ns);
   double err0 = 0.0;
   tm.start(c->stream);
   int s = residual_norm(c, &err0);
   if (!s) s = tg_segment_residual_norms(c, n0.data());
   r.ms_residual += tm.stop(c->stream);
   r.error0 = r.error = err0;
-  // NLSolver::ExitIteration per RVE: converged when rel < rel_tol or the
-  // absolute norm < abs_tol; the batch iterates until every RVE has
-  auto all_converged = [&](const std::vector<double>& nv, double* worst) {
-    bool okk = true;
-    double w = 0.0;
-    for (int i = 0; i < c->nseg; ++i) {
-      const double rel = n0[i] > 0.0 ? nv[i] / n0[i] : 0.0;
-      if (!(rel < P->rel_tol || nv[i] < P->abs_tol)) okk = false;
-      w = std::max(w, n0[i] > 0.0 ? rel : 0.0);
-    }
-    *worst = w;
-    return okk;
+  nk = n0;
+  // NLSolver::ExitIteration per RVE (NLSolver.cpp:675-755): converged when
+  // rel < rel_tol or the absolute norm < abs_tol, diverged when rel >
+  // div_tol, failed at the iteration limit.
+  const int kRunning = 1;
+  std::vector<int> state(ns, kRunning);  // kRunning, TG_OK, or the RVE's failure code
+  auto converged = [&](int i) {
+    const double rel = n0[i] > 0.0 ? nk[i] / n0[i] : 0.0;
+    return rel < P->rel_tol || nk[i] < P->abs_tol;
   };
-  double worst = 0.0;
-  bool converged = !s && all_converged(n0, &worst);
-  while (!s && !converged) {
+  for (int i = 0; i < ns; ++i)
+    if (n0[i] < P->abs_tol) state[i] = TG_OK;  // "hit on first try"
+  const bool per_rve = c->seg_pcg_mode != 0;
+  auto running = [&]() {
+    int k = 0;
+    for (int v : state) k += v == kRunning ? 1 : 0;
+    return k;
+  };
+  while (!s && running() > 0) {
+    // with per-RVE Krylov solves an RVE that has converged or failed is
+    // frozen (no further update) and fails alone; the batch-wide solve
+    // updates every RVE until all have converged
+    if (per_rve) {
+      c->seg_active.assign(ns, 0);
+      for (int i = 0; i < ns; ++i) c->seg_active[i] = state[i] == kRunning ? 1 : 0;
+      c->seg_tolerate = true;
+    }
     double err = 0.0;
     int its = 0;
     s = newton_iteration(c, P, &err, &its, &r, rep ? &tm : nullptr);
+    c->seg_tolerate = false;
     r.pcg_iterations += its;
     if (s) break;
     ++r.iterations;
     r.error = err;
     s = tg_segment_residual_norms(c, nk.data());
     if (s) break;
-    converged = all_converged(nk, &worst);
-    if (!converged && worst > P->div_tol) {
-      c->err = "diverging RVE";
-      s = TG_ERR_DIVERGED;
-    } else if (!converged && c->iteration >= P->max_iterations) {
-      c->err = "max iterations hit";
-      s = TG_ERR_NOT_CONVERGED;
+    if (per_rve) {
+      for (int i = 0; i < ns; ++i) {
+        if (state[i] != kRunning) continue;
+        const double rel = n0[i] > 0.0 ? nk[i] / n0[i] : 0.0;
+        if ((int)c->seg_status.size() == ns && c->seg_status[i] == TG_ERR_NAN) state[i] = TG_ERR_NAN;
+        else if (converged(i)) state[i] = TG_OK;
+        else if (rel > P->div_tol) state[i] = TG_ERR_DIVERGED;
+        else if (c->iteration >= P->max_iterations) state[i] = TG_ERR_NOT_CONVERGED;
+      }
+    } else {
+      double worst = 0.0;
+      bool all = true;
+      for (int i = 0; i < ns; ++i) {
+        all = all && converged(i);
+        if (n0[i] > 0.0) worst = std::max(worst, nk[i] / n0[i]);
+      }
+      if (all) {
+        std::fill(state.begin(), state.end(), (int)TG_OK);
+      } else if (worst > P->div_tol) {
+        c->err = "diverging RVE";
+        s = TG_ERR_DIVERGED;
+      } else if (c->iteration >= P->max_iterations) {
+        c->err = "max iterations hit";
+        s = TG_ERR_NOT_CONVERGED;
+      }
+    }
+  }
+  c->seg_active.clear();
+  int failed = 0, first_fail = TG_OK;
+  for (int i = 0; i < ns; ++i) {
+    if (state[i] == kRunning) state[i] = s;
+    if (state[i] != TG_OK) {
+      ++failed;
+      if (first_fail == TG_OK) first_fail = state[i];
     }
   }
   if (seg_rel)
-    for (int i = 0; i < c->nseg; ++i) seg_rel[i] = n0[i] > 0.0 ? (r.iterations ? nk[i] : n0[i]) / n0[i] : 0.0;
+    for (int i = 0; i < ns; ++i) seg_rel[i] = n0[i] > 0.0 ? nk[i] / n0[i] : 0.0;
+  if (seg_status)
+    for (int i = 0; i < ns; ++i) seg_status[i] = state[i];
   if (rep) *rep = r;
-  return s;
+  if (s) return s;
+  if (failed) {
+    c->err = std::to_string(failed) + " of " + std::to_string(ns) + " RVEs failed (status per RVE)";
+    return first_fail;
+  }
+  return TG_OK;
 }
 
 int tg_checkpoint(tg_context* c) {

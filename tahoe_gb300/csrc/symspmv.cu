@@ -105,7 +105,8 @@ __device__ __forceinline__ void sym_tile_rows(const unsigned char* sbase, const 
                                               const T* sv1, const typename V8T<T>::type* __restrict__ gv8,
                                               const T* __restrict__ gv1, const uint8_t* __restrict__ mask, int lane,
                                               int warp, int nwarps, const typename Vec4<T>::type* __restrict__ p,
-                                              typename Vec4<T>::type* __restrict__ q, Acc<T>& dot) {
+                                              typename Vec4<T>::type* __restrict__ q, Acc<T>& dot,
+                                              double* __restrict__ node_dot) {
   using V = typename Vec4<T>::type;
   using V8 = typename V8T<T>::type;
   const SymTileView tv = sym_view(sbase);
@@ -168,6 +169,13 @@ __device__ __forceinline__ void sym_tile_rows(const unsigned char* sbase, const 
       dot.add_prod(pi.x, a0);
       dot.add_prod(pi.y, a1);
       dot.add_prod(pi.z, a2);
+      if (node_dot) {  // the row's own p.q (per-RVE reductions of a segmented batch)
+        Acc<T> d;
+        d.add_prod(pi.x, a0);
+        d.add_prod(pi.y, a1);
+        d.add_prod(pi.z, a2);
+        node_dot[I] = d.value();
+      }
     }
   }
 }
@@ -184,7 +192,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) pcg_spmv_sym_kern
     const unsigned char* __restrict__ sblob, int cap_s, int cap_v8,
     int cap_v1, const typename V8T<T>::type* __restrict__ gv8, const T* __restrict__ gv1,
     const uint8_t* __restrict__ mask, const typename Vec4<T>::type* __restrict__ p, typename Vec4<T>::type* __restrict__ q,
-    double* partials, PcgScalars* sc, int* status) {
+    double* partials, PcgScalars* sc, int* status, double* node_dot) {
   using V8 = typename V8T<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
@@ -241,7 +249,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) pcg_spmv_sym_kern
     const int k0 = reinterpret_cast<const int*>(st)[2];
     const V8* sv8 = reinterpret_cast<const V8*>(st + cap_s);
     const T* sv1 = reinterpret_cast<const T*>(st + cap_s + cap_v8) + (k0 & (kV1Align - 1));
-    sym_tile_rows<T>(st, sv8, sv1, gv8, gv1, mask, lane, warp, nwarps, p, q, v[0]);
+    sym_tile_rows<T>(st, sv8, sv1, gv8, gv1, mask, lane, warp, nwarps, p, q, v[0], node_dot);
     __syncthreads();  // stage s is free for the copy issued next iteration
   }
   if (stuck >= 0 && threadIdx.x == 0) {
@@ -253,6 +261,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) pcg_spmv_sym_kern
     sc->done = 2;
     sc->fail = 5;
   }
+  // a segmented batch reduces the rows' own products per RVE instead
+  if (node_dot) return;
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -501,7 +511,8 @@ int sym_config(Context* c, int precision, SymLaunch& L) {
 }
 
 template <typename T>
-static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q, double* partials, PcgScalars* sc) {
+static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q, double* partials, PcgScalars* sc,
+                         double* node_dot) {
   using V = typename Vec4<T>::type;
   const SymStore& s = c->sym;
   const bool f32 = std::is_same<T, float>::value;
@@ -511,15 +522,15 @@ static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q,
   pcg_spmv_sym_kernel<T, 2><<<L.grid, 256, L.smem, c->stream>>>(s.ntiles, s.d_off, s.d_koff, s.d_blob, s.cap_struct,
                                                                 cap_bytes_v8<T>(s), cap_bytes_v1<T>(s), gv8, gv1,
                                                                 c->d_mask, (const V*)p, (V*)q, partials, sc,
-                                                                c->d_status);
+                                                                c->d_status, node_dot);
 }
 
 void sym_launch(Context* c, int precision, const SymLaunch& L, const void* p, void* q, double* partials,
-                PcgScalars* sc) {
+                PcgScalars* sc, double* node_dot) {
   if (precision == TG_MIXED)
-    sym_launch_t<float>(c, L, p, q, partials, sc);
+    sym_launch_t<float>(c, L, p, q, partials, sc, node_dot);
   else
-    sym_launch_t<double>(c, L, p, q, partials, sc);
+    sym_launch_t<double>(c, L, p, q, partials, sc, node_dot);
 }
 
 void sym_free(Context* c) {

@@ -51,6 +51,19 @@ struct PcgScalars {
   int fail;  // breakdown cause: 1 init non-finite, 2 p.q <= 0, 3 p.q non-finite, 4 update non-finite
 };
 
+// Scalars of one RVE's Krylov solve in a segmented batch (segpcg.cu).
+struct SegScalars {
+  double rz, rz_old, rr, rr0, alpha, beta, scale, unscale, tol2;
+  int done;   // 0 iterating, 1 converged (or not solved), 2 breakdown, 3 iteration limit
+  int iters;
+  int fail;   // breakdown cause as PcgScalars::fail
+  int max_it;
+};
+struct SegControl {
+  int active;  // RVEs still iterating
+  int pad;
+};
+
 // Scalars of the residual kernel.
 struct ResidScalars {
   double norm2;
@@ -82,10 +95,43 @@ struct SymStore {
   double* d_v8_64 = nullptr;
   double* d_v1_64 = nullptr;
 };
+struct SegScalars;
+struct SegControl;
+// Per-RVE Krylov solves of a segmented batch (segpcg.cu): node chunks of
+// every RVE, per-RVE scalars and arrival counters, the captured iteration.
+struct SegSolve {
+  bool built = false;
+  int nchunks = 0;
+  int4* d_chunk = nullptr;        // {RVE, first node, end node, chunk index within the RVE}
+  int* d_seg_chunk0 = nullptr;    // nseg+1 first chunk of each RVE
+  SegScalars* d_sc = nullptr;     // nseg
+  unsigned int* d_count = nullptr;  // nseg last-chunk counters (back to zero after each pass)
+  double* d_part = nullptr;       // nchunks*2 chunk partials
+  double* d_node_dot = nullptr;   // nnd: each row's z.w
+  void* d_s = nullptr;            // A p by recurrence (vectors of the solve's precision)
+  int s_precision = -1;
+  uint8_t* d_active = nullptr;    // nseg: 1 = the solve iterates the RVE
+  SegControl* d_ctl = nullptr;
+  PcgScalars* d_gate = nullptr;   // done = 1 once no RVE iterates (the product returns at once)
+  cudaGraphExec_t graph = nullptr;
+  int graph_key = -1;
+  void* graph_x = nullptr;
+  std::vector<SegScalars> h_sc;
+};
 struct SymLaunch {
   int grid = 0;
   size_t smem = 0;
   int stages = 2;
+};
+// Launch plan of the single-vector PCG product (krylov.cu): the streamed
+// full-storage kernel (grid, ring) or the symmetric format.
+struct SpmvPlan {
+  int spmv = 0, vec = 0;
+  size_t spmv_smem = 0;
+  int stages = 2;
+  int warp_release = 0;
+  bool sym = false;
+  SymLaunch sl;
 };
 
 template <typename T>
@@ -134,6 +180,11 @@ struct Context {
   int spmv_warp_release = 0;   // 1: per-warp stage release instead of a CTA barrier per tile
   int tangent_epb = 8;         // elements per CTA of the tangent kernel (2, 4, 8)
   int sym_mode = 1;            // 1: the single-vector product streams the symmetric format (single meshes)
+  int seg_pcg_mode = 1;        // 1: a segmented batch runs one Krylov solve per RVE (segpcg.cu)
+  SegSolve seg;
+  std::vector<uint8_t> seg_active;  // RVEs the next segmented solve iterates (empty: all)
+  std::vector<int> seg_status;      // per-RVE status of the last segmented solve
+  bool seg_tolerate = false;        // a breakdown of some RVEs is reported per RVE, not as an error
   int sym_tile_blocks = 512;   // upper blocks per tile of the symmetric format
   SymStore sym;
   int* d_contrib_ptr = nullptr; // nnzb+1
@@ -275,7 +326,18 @@ int sym_build(Context* c, int tile_blocks);
 int sym_convert(Context* c, int precision);  // values from the last assembly
 int sym_config(Context* c, int precision, SymLaunch& L);
 void sym_launch(Context* c, int precision, const SymLaunch& L, const void* p, void* q, double* partials,
-                PcgScalars* sc);
+                PcgScalars* sc, double* node_dot);
+// per-RVE solves of a segmented batch (segpcg.cu)
+int pcg_solve_segmented(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
+                        double* rel_res);
+void seg_free(Context* c);  // graph and bookkeeping (buffers go back with the mesh)
+int pcg_vectors(Context* c, int precision);  // x r z p q of the solve's precision (krylov.cu)
+// the single-vector product for other solvers (segpcg.cu): plan once per
+// mesh/precision, launch on (p, q); node_dot (nnd, may be NULL) receives
+// each row's p.q
+int spmv_plan(Context* c, int precision, SpmvPlan& P);
+void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void* q, double* partials, PcgScalars* sc,
+              double* node_dot);
 void sym_free(Context* c);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----

@@ -96,7 +96,8 @@ _SIGS = {
     "tg_segment_residual_norms": (ctypes.c_int, [_vp, _dp]),
     "tg_segment_average_stress": (ctypes.c_int, [_vp, _dp, _dp]),
     "tg_newton_solve_segmented": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), ctypes.POINTER(NewtonReport),
-                                                 _dp]),
+                                                 _dp, _ip]),
+    "tg_segment_solver": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_segment_macro_tangent": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), _dp, _dp, _ip]),
     "tg_template_add": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, _ip]),
     "tg_mesh_compose": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
@@ -433,10 +434,18 @@ class Context:
         P = NewtonParams(rel_tol, abs_tol, div_tol, max_iterations, precision, precond, lin_rel_tol, lin_max_it)
         R = NewtonReport()
         rel = np.zeros(self.nseg)
-        rc = self.L.tg_newton_solve_segmented(self.h, ctypes.byref(P), ctypes.byref(R), _d(rel))
+        st = np.zeros(self.nseg, dtype=np.int32)
+        rc = self.L.tg_newton_solve_segmented(self.h, ctypes.byref(P), ctypes.byref(R), _d(rel), _i(st))
+        # per-RVE status (TG_OK or the RVE's failure code) of the last solve
+        self.seg_status = st
         if check:
             self._chk(rc, "tg_newton_solve_segmented")
         return rc, R, rel
+
+    def segment_solver(self, per_rve):
+        """One PCG per RVE of a segmented batch (True, default) or one PCG
+        over the whole batch (False)."""
+        self._chk(self.L.tg_segment_solver(self.h, int(bool(per_rve))), "tg_segment_solver")
 
     def macro_tangent(self, vol0=None, precision=MIXED, precond=PRECOND_JACOBI, lin_rel_tol=1e-8, lin_max_it=20000):
         """(nseg, 9, 9) consistent macro tangents dP_jJ/dF_kL at the current

@@ -15,8 +15,11 @@ eigenvalue -0.35 for det F = 0.88), where conjugate gradients break down.
 Outputs: the volume-averaged first Piola stress of every RVE.
 
 The whole batch is one disconnected mesh on the device: one tangent, one
-Krylov solve and one residual per Newton iteration for all RVEs, with the
-exit test applied per RVE (tg_newton_solve_segmented).
+matrix stream and one residual per Newton iteration for all RVEs, with one
+Krylov solve per RVE over that stream and the exit test applied per RVE
+(tg_newton_solve_segmented): an RVE that has converged or failed is frozen and
+reported alone (status per RVE), and an RVE's result does not depend on the
+batch it is solved in.
 """
 import numpy as np
 
@@ -143,6 +146,7 @@ class RVEBatch:
                                           precision=precision, precond=precond, lin_rel_tol=lin_rel_tol,
                                           check=False)
         rep.pcg_iterations += pred_its
+        self.status = c.seg_status.copy()
         P = c.segment_stress(self.vol0)
         return rc, rep, rel, P
 
@@ -188,5 +192,6 @@ class ResidentRVEs:
                                           precision=precision, precond=precond, lin_rel_tol=lin_rel_tol,
                                           check=False)
         rep.pcg_iterations += pred_its
+        self.status = c.seg_status.copy()
         P = c.segment_stress(np.array([template(int(n)).vol for n in ns]))
         return rc, rep, rel, P

@@ -54,12 +54,15 @@ def gpu_batch_solver(precision=lib.MIXED, rel_tol=1e-8, lin_rel_tol=1e-4):
             lane_state["ctx"] = ctx
             lane_state["rves"] = res
         rc, rep, rel, P = res.solve(ns, Fs, precision=precision, rel_tol=rel_tol, lin_rel_tol=lin_rel_tol)
-        ok = (np.asarray(rel) < rel_tol) if rc == 0 else np.zeros(len(ns), dtype=bool)
-        if not ok.all():
+        # status per RVE: an RVE that failed fails alone, the others are valid
+        st = np.asarray(getattr(res, "status", np.full(len(ns), rc)), dtype=np.int64)
+        if rc not in (0, -4, -5, -6, -7):
+            st = np.full(len(ns), rc)  # a CUDA, memory or argument error ends the batch
+        if (st != 0).any():
             lane_state.setdefault("failures", []).append(
                 (rc, lane_state["ctx"].L.tg_last_error(lane_state["ctx"].h).decode(), list(map(int, ns)),
                  float(np.max(rel)) if len(rel) else None))
-        return np.where(ok, 0, rc if rc != 0 else -6), P
+        return st, P
 
     return solve
 

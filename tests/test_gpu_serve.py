@@ -1,6 +1,8 @@
 """Served RVE stream on the GPU: a Poisson trace through two lanes with
 continuous batching, mixed precision; every request's averaged first Piola
-stress equals (1e-6) the same RVE solved alone, one at a time, in FP64, a
+stress is bitwise the same request solved alone through the same mixed path
+(one Krylov solve per RVE), equals (1e-6) the same RVE solved one at a time
+in FP64, a
 sample of the served requests equals (1e-6) the oracle's solve of the same
 RVE, and the lanes actually batched and overlapped."""
 import numpy as np
@@ -30,6 +32,16 @@ def test_served_stream_equals_one_at_a_time_fp64():
     assert all(b[1] == 1 for b in ref["batches"])
     for r in range(len(ns)):
         assert rel_err(res["P"][r], ref["P"][r]) < 1e-6, (r, int(ns[r]))
+    # the same requests one at a time through the same mixed path: every
+    # served result (solved inside a batch of other requests) is bitwise the
+    # result of the request alone
+    alone = serve.Server(serve.gpu_batch_solver(lib.MIXED), lanes=1, max_batch=1)
+    try:
+        one = alone.run(arr, ns, Fs, time_scale=0.0)
+    finally:
+        alone.close()
+    assert np.all(one["status"] == 0)
+    assert np.array_equal(one["P"], res["P"])
     # served results against the oracle (independent of both GPU paths): the
     # first requests of each side length in the trace
     picked = [int(np.nonzero(ns == n)[0][0]) for n in np.unique(ns)][:4]
