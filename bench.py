@@ -80,10 +80,12 @@ def spmv_roofline(ctx, precision):
     from tahoe_gb300 import lib, workloads
     ms = ctx.time_kernel(0, 20)
     s_val = 4 if precision == lib.MIXED else 8
-    b = workloads.spmv_bytes(ctx.block_nnz, ctx.nnd, s_val)
+    sym = getattr(ctx, "sym_mode", 0) and not getattr(ctx, "composed", False)
+    b = (workloads.spmv_bytes_sym if sym else workloads.spmv_bytes)(ctx.block_nnz, ctx.nnd, s_val)
     peak, kind = peaks()
     ach = b / (ms * 1e-3) / 1e9
-    return {"kernel": "pcg_spmv_kernel", "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+    return {"kernel": "pcg_spmv_sym_kernel" if sym else "pcg_spmv_kernel", "storage": "symmetric" if sym else "full",
+            "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
             "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": int(b), "ms_per_launch": round(ms, 4)}
 
 
@@ -320,8 +322,8 @@ def run_ours(args):
         from tahoe_gb300 import autotune
         t = autotune.Tuner(reps=20)
         tuning = t.tune(ctx, prec, lib.TOTAL_LAGRANGIAN)
-        tuning = {k: tuning.get(k) for k in ("tile_blocks", "stages", "release", "tangent_epb", "spmv_ms", "tangent_ms",
-                                             "cached", "spmv_sweep")}
+        tuning = {k: tuning.get(k) for k in ("tile_blocks", "stages", "release", "sym", "sym_tile", "tangent_epb",
+                                             "spmv_ms", "tangent_ms", "cached", "spmv_sweep")}
 
     # warm-up (also captures the PCG graph)
     for _ in range(max(args.warmup, 1)):
@@ -375,7 +377,9 @@ def run_ours(args):
     t_res = ctx.time_kernel(4, 5)
     s_val = 4 if prec == lib.MIXED else 8
     nnzb = ctx.block_nnz
-    bytes_spmv = workloads.spmv_bytes(nnzb, nnd, s_val)
+    sym = bool(getattr(ctx, "sym_mode", 0))
+    prof = "pcg_spmv_sym_c2_64cubed.md" if sym else "pcg_spmv_c2_64cubed.md"
+    bytes_spmv = (workloads.spmv_bytes_sym if sym else workloads.spmv_bytes)(nnzb, nnd, s_val)
     peak, peak_kind = peaks()
     achieved = bytes_spmv / (t_spmv * 1e-3) / 1e9
     elements_per_s = mesh.nel / ((t_tan + t_asm) * 1e-3)
@@ -407,12 +411,13 @@ def run_ours(args):
         "elements_assembled_per_s": round(elements_per_s, 1),
         "kernel_ms": {"pcg_spmv": round(t_spmv, 5), "pcg_update": round(t_upd, 5), "tangent": round(t_tan, 4),
                       "assembly": round(t_asm, 4), "residual": round(t_res, 4)},
-        "roofline": {"kernel": "pcg_spmv_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+        "roofline": {"kernel": "pcg_spmv_sym_kernel" if sym else "pcg_spmv_kernel",
+                     "storage": "symmetric" if sym else "full", "bound": "hbm", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "algorithmic_bytes": int(bytes_spmv),
-                     "traffic": profiled_traffic("pcg_spmv_c2_64cubed.md") if prec == lib.MIXED else None,
-                     "traffic_source": "committed ncu capture of this kernel on this workload "
-                                       "(profiles/pcg_spmv_c2_64cubed.md), not measured in this run"},
+                     "traffic": profiled_traffic(prof) if prec == lib.MIXED else None,
+                     "traffic_source": "committed ncu capture of this kernel on this workload (profiles/%s), not "
+                                       "measured in this run" % prof},
         "other_rooflines": other_rooflines,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/Newton iteration", "h2d_bytes_per_step": nnd * 24,
                 "d2h_bytes_per_step": nnd * 24, "host_memory": host_mem},
@@ -575,19 +580,20 @@ def run_c4(args):
 
 
 def c5_trace(args, rates, requests, plain_requests):
-    """Configuration 5: a Poisson stream of RVE requests served with
-    continuous batching over several lanes (mixed precision), beside the plain
-    one-at-a-time FP64 GPU solve of the same requests."""
-    from tahoe_gb300 import lib, serve
+    """Configuration 5: a Poisson stream of RVE requests served by the
+    library's request loop (tg_serve_*: lanes as C++ threads, continuous
+    batching with admission by size, memory and a latency target; mixed
+    precision), beside the plain one-at-a-time FP64 GPU solve of the same
+    requests through the same loop (one lane, batches of one)."""
+    from tahoe_gb300 import lib, rve, serve
     import torch
     free, _ = torch.cuda.mem_get_info(0)
     budget = 0.5 * free
-    srv = serve.Server(serve.gpu_batch_solver(lib.MIXED), lanes=args.lanes, max_batch=args.max_batch,
-                       hbm_budget=budget)
-    plain = serve.Server(serve.gpu_batch_solver(lib.FP64), lanes=1, max_batch=1, hbm_budget=budget,
-                         precision=lib.FP64)
-    # warm-up: contexts, memory pools, one graph capture per lane
-    wa, wn, wF = serve.sample_requests(4 * args.lanes, 1e5, seed=99, nmin=4, nmax=8)
+    srv = serve.NativeServer(lanes=args.lanes, max_batch=args.max_batch, hbm_budget=budget, precision=lib.MIXED,
+                             target_batch_ms=args.c5_target_ms)
+    plain = serve.NativeServer(lanes=1, max_batch=1, hbm_budget=budget, precision=lib.FP64)
+    # warm-up: contexts, memory pools, templates, graph captures, the batch-time model
+    wa, wn, wF = serve.sample_requests(16 * args.lanes, 1e5, seed=99, nmin=4, nmax=24)
     srv.run(wa, wn, wF)
     plain.run(wa[:2], wn[:2], wF[:2])
     sweep = []
@@ -604,35 +610,41 @@ def c5_trace(args, rates, requests, plain_requests):
             "solves_per_s": round(res["solves_per_s"], 1), "p50_ms": round(res["p50_ms"], 2),
             "p99_ms": round(res["p99_ms"], 2), "mean_batch": round(res["mean_batch"], 1),
             "batches": len(res["batches"]), "max_concurrent_lanes": res["max_concurrent_lanes"],
+            "retried_alone": res["retried"],
             "plain_fp64": {"requests": k, "completed": ref["completed"], "solves_per_s": round(ref["solves_per_s"], 1),
                            "p50_ms": round(ref["p50_ms"], 2), "p99_ms": round(ref["p99_ms"], 2)},
             "P_rel_err_vs_plain_fp64_worst": float(d[both].max()) if both.any() else None,
         })
-        if res["retried"]:
-            sweep[-1]["retried_alone"] = res["retried"]
-            sweep[-1]["batch_failures"] = [[f[0], f[1][:120], f[2][:12], f[3]] for f in res["failures"][:3]]
         if res["completed"] < len(ns):
             codes, counts = np.unique(res["status"][res["status"] != 0], return_counts=True)
             sweep[-1]["failed"] = {int(k): int(v) for k, v in zip(codes, counts)}
-            sweep[-1]["errors"] = [e[2][:200] for e in res["errors"][:3]]
-    roof = None
-    lane_ctx = srv.lane_states[0].get("ctx")
-    if lane_ctx is not None and lane_ctx.nnd > 0:
-        lane_ctx.tangent(lib.MIXED)
-        roof = spmv_roofline(lane_ctx, lib.MIXED)
-        roof["on"] = "lane 0's last batch (%d nodes)" % lane_ctx.nnd
+            sweep[-1]["error"] = srv.error()[:200]
+    model = srv.stats()["model_ms_per_1000_elements"]
     srv.close()
     plain.close()
+    # SpMV roofline on a batch mesh of the stream's size mix (first 64 requests)
+    c = lib.Context(0)
+    res_t = rve.ResidentRVEs(c)
+    res_t.compose(ns[:64])
+    c.set_iteration(-1)
+    c.residual(want_vector=False)
+    c.tangent(lib.MIXED)
+    roof = spmv_roofline(c, lib.MIXED)
+    roof["on"] = "a batch mesh of the first 64 requests (%d nodes)" % c.nnd
+    c.close()
     top = max(sweep, key=lambda r: r["solves_per_s"])
     return {
         "metric": "served RVE solves/s", "value": top["solves_per_s"], "unit": "RVE/s", "higher_is_better": True,
         "n_gpus": 1,
         "config": {"workload": "C5: Poisson stream of RVE requests, n log-uniform in {4..24}, two-phase Simo "
-                               "neo-Hookean RVE as in C4, F = I + 0.05 S; %d lanes (one CUDA stream each), "
-                               "continuous batching up to %d RVEs per batch, admission by half of free HBM, "
-                               "mixed precision, Newton to 1e-8 per RVE" % (args.lanes, args.max_batch),
+                               "neo-Hookean RVE as in C4, F = I + 0.05 S; request loop in the library "
+                               "(tg_serve_*): %d lanes (C++ threads, one CUDA stream each), continuous batching up "
+                               "to %d RVEs per batch, admission by half of free HBM and a %g ms batch-time target, "
+                               "mixed precision, one PCG per RVE, Newton to 1e-8 per RVE"
+                               % (args.lanes, args.max_batch, args.c5_target_ms),
                    "hbm_budget_bytes": int(budget)},
         "sweep": sweep,
+        "batch_time_model_ms_per_1000_elements": round(model, 3),
         "roofline": roof,
     }
 
@@ -773,6 +785,8 @@ def main():
                          "blocks)")
     ap.add_argument("--c4-precond", default="block", choices=["jacobi", "block"], help="C4 batch preconditioner")
     ap.add_argument("--c5-rate", type=float, default=5000.0, help="C5 arrival rate of the default run's trace")
+    ap.add_argument("--c5-target-ms", type=float, default=100.0,
+                    help="C5 latency target: predicted batch time a lane admits up to (0: none)")
     ap.add_argument("--c5-requests", type=int, default=1000, help="C5 requests of the default run's trace")
     ap.add_argument("--c5-plain-requests", type=int, default=100, help="C5 one-at-a-time FP64 requests (default run)")
     args = ap.parse_args()

@@ -330,6 +330,38 @@ int tg_set_affine_prescribed(tg_context* ctx, const double* F);
  * the new prescribed values */
 int tg_predict_affine(tg_context* ctx, const double* F, const tg_newton_params* params, int* pcg_iterations);
 
+/* ---- served RVE stream ---------------------------------------------------
+ * The request loop of configuration 5 inside the library (no reference
+ * counterpart; the serving side of the FE^2 batch, SURVEY's tg_serve_submit /
+ * poll).  Requests are RVEs of side n (the benchmark RVE: n x n x n hex8 unit
+ * cube, centred spherical inclusion r = 0.3 with ten times the matrix's Simo
+ * neo-Hookean moduli, affine boundary displacement (F - I) X).  lanes host
+ * threads each own a context (one CUDA stream, resident templates); a free
+ * lane takes the arrived requests in order while the batch stays within
+ * max_batch, the device-memory budget of every batch in flight
+ * (budget_bytes) and the latency target target_batch_ms (predicted batch
+ * time from a model fitted to the lanes' own batches; 0 disables it), and
+ * solves them with tg_predict_affine + tg_newton_solve_segmented (an RVE that
+ * fails fails alone; a batch-level failure is retried request by request).
+ * The server is thread-safe: submit and poll from any thread. */
+typedef struct tg_server tg_server;
+int tg_serve_create(tg_server** server, int device, int lanes, int max_batch, double budget_bytes, int precision,
+                    int precond, double rel_tol, double lin_rel_tol, double target_batch_ms);
+/* queues one request (F: 3x3 row-major); *request_id numbers requests from 0 */
+int tg_serve_submit(tg_server* server, int n, const double* F, long long* request_id);
+/* TG_OK with the averaged first Piola stress P (9, row-major), the request's
+ * status and its latency (submission to completion, ms) once it is done;
+ * 1 while it is pending */
+int tg_serve_poll(tg_server* server, long long request_id, double* P, int* status, double* latency_ms);
+/* blocks until every submitted request is done */
+int tg_serve_wait(tg_server* server);
+/* out[0..5]: batches, mean batch size, most lanes busy at once, requests
+ * retried alone, predicted ms of a 1,000-element batch, completed requests */
+int tg_serve_stats(tg_server* server, double* out, int n);
+const char* tg_serve_error(const tg_server* server);
+/* finishes queued requests, joins the lanes and releases their contexts */
+int tg_serve_destroy(tg_server* server);
+
 /* ---- measurement and tuning helpers (no reference counterpart) ---------- */
 
 /* Shape of the streamed PCG matrix product: row tiles of at most tile_blocks
@@ -341,14 +373,17 @@ int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
  * barrier after each staged tile; 1 each warp releases the stage on an
  * mbarrier and moves on (results are bitwise the same) */
 int tg_spmv_release(tg_context* ctx, int per_warp);
-/* Storage the single-vector PCG product streams: on = 1 (default) the
- * symmetric format -- the upper node blocks only, each lower block read as
- * the transpose of its upper twin (the symmetric MSR storage of
- * MSRMatrixT.cpp:104-175 applied as in MSRMatrixT::Multx, MSRMatrixT.cpp:385-420),
- * about 0.63 of the full storage's DRAM bytes; on = 0 the full block storage.
- * Meshes composed from templates always use the full storage.  tile_blocks:
- * upper blocks per streamed tile (0 keeps the current value, default 512).
- * The results equal the full-storage product up to the order of the FP sums. */
+/* Storage the single-vector PCG product streams: on = 0 (default) the full
+ * block storage; on = 1, 2, 3 the symmetric format -- the upper node blocks
+ * only, each lower block read as the transpose of its upper twin (the
+ * symmetric MSR storage of MSRMatrixT.cpp:104-175 applied as in
+ * MSRMatrixT::Multx, MSRMatrixT.cpp:385-420), about 0.63 of the full
+ * storage's DRAM bytes -- with three launch shapes for the autotuner: 1 two
+ * staged tiles at 80 registers, 2 two staged tiles at 64, 3 three staged
+ * tiles at 80.  Meshes composed from templates always use the full storage.
+ * tile_blocks: upper blocks per streamed tile (0 keeps the current value,
+ * default 512).  The results equal the full-storage product up to the order
+ * of the FP sums. */
 int tg_spmv_symmetric(tg_context* ctx, int on, int tile_blocks);
 /* elements per CTA of the tangent kernel: 2, 4 or 8 (default 8); element
  * matrices are bitwise the same for every choice */

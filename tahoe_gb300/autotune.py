@@ -5,7 +5,10 @@ themselves (CUDA events, tg_time_kernel) on the current state:
 
   * the streamed PCG product: rows per tile (the unit of the tile-contiguous
     matrix storage, in block nonzeros) x depth of the shared-memory ring x
-    stage release (CTA barrier per tile, or per-warp release on an mbarrier);
+    stage release (CTA barrier per tile, or per-warp release on an mbarrier),
+    then the symmetric stream format (upper blocks only; three launch shapes
+    x upper blocks per tile), which replaces the full storage where it is
+    faster on the mesh at hand;
   * the element tangent: elements per CTA (one thread per upper node-pair
     block of each element).
 
@@ -25,6 +28,8 @@ SPMV_TILES = (256, 384, 512, 640, 768, 1024, 1536)
 SPMV_STAGES = (2, 3)
 SPMV_RELEASE = (0, 1)
 TANGENT_EPB = (2, 4, 8)
+SYM_MODES = (1, 2, 3)
+SYM_TILES = (256, 384, 512)
 KERNEL_SPMV, KERNEL_TANGENT = 0, 2
 
 _DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tuning.json")
@@ -48,10 +53,11 @@ def pick(timings):
 
 class Tuner:
     def __init__(self, cache_path=_DEFAULT_CACHE, reps=20, tiles=SPMV_TILES, stages=SPMV_STAGES, epbs=TANGENT_EPB,
-                 releases=SPMV_RELEASE):
+                 releases=SPMV_RELEASE, sym_modes=SYM_MODES, sym_tiles=SYM_TILES):
         self.cache_path = cache_path
         self.reps = reps
         self.tiles, self.stages, self.epbs, self.releases = tiles, stages, epbs, releases
+        self.sym_modes, self.sym_tiles = sym_modes, sym_tiles
         self.table = {}
         if cache_path and os.path.exists(cache_path):
             try:
@@ -73,6 +79,7 @@ class Tuner:
     def apply(ctx, cfg):
         ctx.spmv_config(cfg["tile_blocks"], cfg["stages"])
         ctx.spmv_release(cfg.get("release", 0))
+        ctx.spmv_symmetric(cfg.get("sym", 0), cfg.get("sym_tile", 0))
         ctx.tangent_config(cfg["tangent_epb"])
 
     def tune(self, ctx, precision, formulation, gpu="gpu0", force=False, timer=None):
@@ -110,18 +117,33 @@ class Tuner:
         ctx.spmv_config(tb, st)
         ctx.spmv_release(rl)
         ctx.tangent(precision)
+        # the symmetric stream format, against the best full-storage shape
+        sym = {}
+        for m in self.sym_modes:
+            for t in self.sym_tiles:
+                try:
+                    ctx.spmv_symmetric(m, t)
+                    sym[(m, t)] = timer(ctx, KERNEL_SPMV, self.reps)
+                except lib.TahoeError as e:
+                    if e.code != -8:
+                        raise
+                    sym[(m, t)] = None
+        best_sym, sym_ms = pick(sym) if sym else (None, float("inf"))
+        sm, stile = (best_sym if best_sym is not None and sym_ms < spmv_ms else (0, 0))
+        ctx.spmv_symmetric(sm, stile)
         tang = {}
         for e in self.epbs:
             ctx.tangent_config(e)
             tang[e] = timer(ctx, KERNEL_TANGENT, max(3, self.reps // 4))
         epb, tang_ms = pick(tang)
-        cfg = {"tile_blocks": tb, "stages": st, "release": rl, "tangent_epb": epb, "spmv_ms": spmv_ms,
-               "tangent_ms": tang_ms}
+        cfg = {"tile_blocks": tb, "stages": st, "release": rl, "sym": sm, "sym_tile": stile, "tangent_epb": epb,
+               "spmv_ms": min(spmv_ms, sym_ms) if sm else spmv_ms, "tangent_ms": tang_ms}
         self.apply(ctx, cfg)
         ctx.tangent(precision)
         self.table[key] = cfg
         self.save()
         out = dict(cfg, cached=False)
         out["spmv_sweep"] = {"%dx%dr%d" % k: v for k, v in spmv.items()}
+        out["spmv_sweep"].update({"sym%dx%d" % k: v for k, v in sym.items()})
         out["tangent_sweep"] = {str(k): v for k, v in tang.items()}
         return out

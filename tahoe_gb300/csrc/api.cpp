@@ -418,8 +418,7 @@ int tg_spmv_release(tg_context* c, int per_warp) {
 }
 
 int tg_spmv_symmetric(tg_context* c, int on, int tile_blocks) {
-  if (!c || (on != 0 && on != 1) || (tile_blocks != 0 && (tile_blocks < 32 || tile_blocks > 4096)))
-    return TG_ERR_ARG;
+  if (!c || on < 0 || on > 3 || (tile_blocks != 0 && (tile_blocks < 32 || tile_blocks > 4096))) return TG_ERR_ARG;
   if (c->nnd > 0 && cudaSetDevice(c->device) != cudaSuccess) return TG_ERR_CUDA;
   c->sym_mode = on;
   if (tile_blocks) c->sym_tile_blocks = tile_blocks;

@@ -98,6 +98,33 @@ __device__ __forceinline__ T point_gradients(const T (*Xe)[3], int ip, T g[3][8]
   return d;
 }
 
+// The same for the current configuration x = X + u (updated Lagrangian):
+// gradients dN/dx and det(dx/dxi), no coordinate array formed.
+template <typename T>
+__device__ __forceinline__ T point_gradients_current(const T (*Xe)[3], const T (*Ue)[3], int ip, T g[3][8]) {
+  T dN[3][8];
+  ref_grad<T>(ip, dN);
+  T J[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      T acc = T(0);
+#pragma unroll
+      for (int a = 0; a < 8; ++a) acc += (Xe[a][i] + Ue[a][i]) * dN[k][a];
+      J[i * 3 + k] = acc;
+    }
+  const T d = det3(J);
+  T Ji[9];
+  inv3(J, d, Ji);
+#pragma unroll
+  for (int l = 0; l < 3; ++l)
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+      g[l][a] = Ji[0 * 3 + l] * dN[0][a] + Ji[1 * 3 + l] * dN[1][a] + Ji[2 * 3 + l] * dN[2][a];
+  return d;
+}
+
 template <typename T>
 __device__ __forceinline__ void hooke(const double* C, const T e[6], T s[6]) {
 #pragma unroll
@@ -457,13 +484,8 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
         // UpdatedLagrangianT::FormKd (UpdatedLagrangianT.cpp:145-171): the
         // shape functions of the current configuration x = X + u give dN/dx
         // directly; f_a,i = w det(dx/dxi) sigma_ij dN_a/dx_j
-        double xc[8][3];
-#pragma unroll
-        for (int a = 0; a < 8; ++a)
-#pragma unroll
-          for (int d = 0; d < 3; ++d) xc[a][d] = sX[le][a][d] + sU[le][a][d];
-        double gc[3][8];
-        const double wc = point_gradients<double>(xc, ip, gc);  // weight 1
+        // (the reference gradients are no longer needed: g takes dN/dx)
+        const double wc = point_gradients_current<double>(sX[le], sU[le], ip, g);  // weight 1
         if (!(wc > 0.0)) {
           bad = true;
         } else {
@@ -471,7 +493,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
           for (int a = 0; a < 8; ++a)
 #pragma unroll
             for (int i = 0; i < 3; ++i)
-              f[a][i] = wc * (sm[i * 3 + 0] * gc[0][a] + sm[i * 3 + 1] * gc[1][a] + sm[i * 3 + 2] * gc[2][a]);
+              f[a][i] = wc * (sm[i * 3 + 0] * g[0][a] + sm[i * 3 + 1] * g[1][a] + sm[i * 3 + 2] * g[2][a]);
         }
       } else {
         double Fi[9];
@@ -616,7 +638,10 @@ __device__ __forceinline__ void slot_pair(int slot, int& a, int& b) {
   }
 }
 
-template <typename T, int kTanElems>
+// UL: the updated-Lagrangian gradients and weight (compiled only into the
+// instantiation that needs them, so the other formulations keep their
+// register budget)
+template <typename T, int kTanElems, bool UL>
 __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const double* __restrict__ X, int nnd,
                                                               const int* __restrict__ conn,
                                                               const int8_t* __restrict__ blk, int nel,
@@ -690,22 +715,16 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
         const T J = det3(F);
         okm = okm && J > T(0);
         if (okm) okm = (m.kind == TG_MAT_FS_SIMO) ? simo<T>(m, F, s, D) : stvenant<T>(m, F, s, D);
-        if (okm && mt.formulation == TG_UPDATED_LAGRANGIAN) {
+        if (UL && okm) {
           // UpdatedLagrangianT::FormStiffness (UpdatedLagrangianT.cpp:94-142):
           // gradients and integration weight of the current configuration
           // (coordinates relative to node 0: the gradients see differences)
-          T xc[8][3];
-#pragma unroll
-          for (int a = 0; a < 8; ++a)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) xc[a][d] = sX[le][a][d] + sU[le][a][d];
-          T gc[3][8];
-          const T detc = point_gradients<T>(xc, ip, gc);
+          const T detc = point_gradients_current<T>(sX[le], sU[le], ip, g);
           okm = detc > T(0);
 #pragma unroll
           for (int k = 0; k < 3; ++k)
 #pragma unroll
-            for (int a = 0; a < 8; ++a) sG[le][ip][k][a] = gc[k][a];
+            for (int a = 0; a < 8; ++a) sG[le][ip][k][a] = g[k][a];
           scale = detc;
         } else if (okm) {
           T Fi[9];
@@ -979,15 +998,23 @@ int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out) {
   return ok(c, cudaGetLastError(), "nodal_stress_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
-template <int EPB>
-void launch_tangent_epb(Context* c, int precision) {
+template <int EPB, bool UL>
+void launch_tangent_form(Context* c, int precision) {
   const int grid = (c->nel + EPB - 1) / EPB;
   if (precision == TG_MIXED)
-    tangent_kernel<float, EPB><<<grid, EPB * kSlots, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel,
-                                                                     c->d_u, c->mats, j2view(c), c->d_Ke32, c->d_status);
+    tangent_kernel<float, EPB, UL><<<grid, EPB * kSlots, 0, c->stream>>>(
+        c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats, j2view(c), c->d_Ke32, c->d_status);
   else
-    tangent_kernel<double, EPB><<<grid, EPB * kSlots, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel,
-                                                                      c->d_u, c->mats, j2view(c), c->d_Ke64, c->d_status);
+    tangent_kernel<double, EPB, UL><<<grid, EPB * kSlots, 0, c->stream>>>(
+        c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats, j2view(c), c->d_Ke64, c->d_status);
+}
+
+template <int EPB>
+void launch_tangent_epb(Context* c, int precision) {
+  if (c->mats.formulation == TG_UPDATED_LAGRANGIAN)
+    launch_tangent_form<EPB, true>(c, precision);
+  else
+    launch_tangent_form<EPB, false>(c, precision);
 }
 
 int launch_tangent(Context* c, int precision) {

@@ -186,8 +186,8 @@ __device__ __forceinline__ void sym_tile_rows(const unsigned char* sbase, const 
 // wait is bounded; a timeout sets an error flag, drains the copies in flight
 // (bounded) and marks the solve broken down.  The last CTA forms p.q and
 // alpha exactly as the full-storage product does.
-template <typename T, int NST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) pcg_spmv_sym_kernel(
+template <typename T, int NST, int MINB>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? MINB : 2) pcg_spmv_sym_kernel(
     int ntiles, const long long* __restrict__ soff, const int* __restrict__ koff,
     const unsigned char* __restrict__ sblob, int cap_s, int cap_v8,
     int cap_v1, const typename V8T<T>::type* __restrict__ gv8, const T* __restrict__ gv1,
@@ -470,7 +470,7 @@ int sym_convert(Context* c, int precision) {
   return TG_OK;
 }
 
-template <typename T, int NST>
+template <typename T, int NST, int MINB>
 static int sym_config_n(Context* c, SymLaunch& L) {
   const SymStore& s = c->sym;
   L.smem = (size_t)NST * ((size_t)s.cap_struct + cap_bytes_v8<T>(s) + cap_bytes_v1<T>(s));
@@ -478,18 +478,18 @@ static int sym_config_n(Context* c, SymLaunch& L) {
   if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
     return TG_ERR_CUDA;
   cudaFuncAttributes fa;
-  if (!ok(c, cudaFuncGetAttributes(&fa, pcg_spmv_sym_kernel<T, NST>), "function attributes")) return TG_ERR_CUDA;
+  if (!ok(c, cudaFuncGetAttributes(&fa, pcg_spmv_sym_kernel<T, NST, MINB>), "function attributes")) return TG_ERR_CUDA;
   if (L.smem + fa.sharedSizeBytes + 1024 > (size_t)optin) {
     c->err = "symmetric SpMV tile ring does not fit in shared memory (reduce the tile size)";
     return TG_ERR_CAPACITY;
   }
   // one value for every context (the attribute belongs to the function)
-  if (!ok(c, cudaFuncSetAttribute(pcg_spmv_sym_kernel<T, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (!ok(c, cudaFuncSetAttribute(pcg_spmv_sym_kernel<T, NST, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   optin - (int)fa.sharedSizeBytes),
           "smem attribute"))
     return TG_ERR_CUDA;
   int per_sm = 0;
-  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_spmv_sym_kernel<T, NST>, 256, L.smem),
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_spmv_sym_kernel<T, NST, MINB>, 256, L.smem),
           "occupancy"))
     return TG_ERR_CUDA;
   if (per_sm < 1) {
@@ -498,6 +498,7 @@ static int sym_config_n(Context* c, SymLaunch& L) {
   }
   L.grid = std::max(1, std::min(s.ntiles, c->num_sms * per_sm));
   L.stages = NST;
+  L.minb = MINB;
   return TG_OK;
 }
 
@@ -506,8 +507,14 @@ int sym_config(Context* c, int precision, SymLaunch& L) {
     c->err = "symmetric SpMV: values not converted for this precision";
     return TG_ERR_ARG;
   }
+  // launch shapes: 1 two staged tiles at up to 80 registers (3 CTAs/SM), 2
+  // two staged tiles at 64 (4 CTAs/SM), 3 three staged tiles at 80
   const bool f32 = precision == TG_MIXED;
-  return f32 ? sym_config_n<float, 2>(c, L) : sym_config_n<double, 2>(c, L);
+  switch (c->sym_mode) {
+    case 2: return f32 ? sym_config_n<float, 2, 4>(c, L) : sym_config_n<double, 2, 4>(c, L);
+    case 3: return f32 ? sym_config_n<float, 3, 3>(c, L) : sym_config_n<double, 3, 3>(c, L);
+    default: return f32 ? sym_config_n<float, 2, 3>(c, L) : sym_config_n<double, 2, 3>(c, L);
+  }
 }
 
 template <typename T>
@@ -519,10 +526,15 @@ static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q,
   const typename V8T<T>::type* gv8 =
       reinterpret_cast<const typename V8T<T>::type*>(f32 ? (const void*)s.d_v8_32 : (const void*)s.d_v8_64);
   const T* gv1 = reinterpret_cast<const T*>(f32 ? (const void*)s.d_v1_32 : (const void*)s.d_v1_64);
-  pcg_spmv_sym_kernel<T, 2><<<L.grid, 256, L.smem, c->stream>>>(s.ntiles, s.d_off, s.d_koff, s.d_blob, s.cap_struct,
-                                                                cap_bytes_v8<T>(s), cap_bytes_v1<T>(s), gv8, gv1,
-                                                                c->d_mask, (const V*)p, (V*)q, partials, sc,
-                                                                c->d_status, node_dot);
+#define TG_SYM_ARGS s.ntiles, s.d_off, s.d_koff, s.d_blob, s.cap_struct, cap_bytes_v8<T>(s), cap_bytes_v1<T>(s), gv8, \
+    gv1, c->d_mask, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot
+  if (L.stages == 3)
+    pcg_spmv_sym_kernel<T, 3, 3><<<L.grid, 256, L.smem, c->stream>>>(TG_SYM_ARGS);
+  else if (L.minb == 4)
+    pcg_spmv_sym_kernel<T, 2, 4><<<L.grid, 256, L.smem, c->stream>>>(TG_SYM_ARGS);
+  else
+    pcg_spmv_sym_kernel<T, 2, 3><<<L.grid, 256, L.smem, c->stream>>>(TG_SYM_ARGS);
+#undef TG_SYM_ARGS
 }
 
 void sym_launch(Context* c, int precision, const SymLaunch& L, const void* p, void* q, double* partials,

@@ -122,6 +122,7 @@ struct SymLaunch {
   int grid = 0;
   size_t smem = 0;
   int stages = 2;
+  int minb = 3;  // CTAs per SM the register budget targets
 };
 // Launch plan of the single-vector PCG product (krylov.cu): the streamed
 // full-storage kernel (grid, ring) or the symmetric format.
@@ -179,7 +180,7 @@ struct Context {
   int spmv_stages = 2;
   int spmv_warp_release = 0;   // 1: per-warp stage release instead of a CTA barrier per tile
   int tangent_epb = 8;         // elements per CTA of the tangent kernel (2, 4, 8)
-  int sym_mode = 1;            // 1: the single-vector product streams the symmetric format (single meshes)
+  int sym_mode = 0;            // 1-3: the single-vector product streams the symmetric format (single meshes)
   int seg_pcg_mode = 1;        // 1: a segmented batch runs one Krylov solve per RVE (segpcg.cu)
   SegSolve seg;
   std::vector<uint8_t> seg_active;  // RVEs the next segmented solve iterates (empty: all)

@@ -98,6 +98,15 @@ _SIGS = {
     "tg_newton_solve_segmented": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), ctypes.POINTER(NewtonReport),
                                                  _dp, _ip]),
     "tg_segment_solver": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tg_serve_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double]),
+    "tg_serve_submit": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong)]),
+    "tg_serve_poll": (ctypes.c_int, [_vp, ctypes.c_longlong, _dp, ctypes.POINTER(ctypes.c_int), _dp]),
+    "tg_serve_wait": (ctypes.c_int, [_vp]),
+    "tg_serve_stats": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+    "tg_serve_error": (ctypes.c_char_p, [_vp]),
+    "tg_serve_destroy": (ctypes.c_int, [_vp]),
     "tg_segment_macro_tangent": (ctypes.c_int, [_vp, ctypes.POINTER(NewtonParams), _dp, _dp, _ip]),
     "tg_template_add": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, _ip]),
     "tg_mesh_compose": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
@@ -468,9 +477,10 @@ class Context:
         self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")
 
     def spmv_symmetric(self, on, tile_blocks=0):
-        """Symmetric stream format of the single-vector product (on=True,
-        default on single meshes) or the full block storage (on=False)."""
-        self._chk(self.L.tg_spmv_symmetric(self.h, int(bool(on)), int(tile_blocks)), "tg_spmv_symmetric")
+        """Symmetric stream format of the single-vector product (on = 1, 2, 3:
+        three launch shapes) or the full block storage (on = 0, default)."""
+        self._chk(self.L.tg_spmv_symmetric(self.h, int(on), int(tile_blocks)), "tg_spmv_symmetric")
+        self.sym_mode = int(on)
 
     def tangent_config(self, elems_per_block):
         self._chk(self.L.tg_tangent_config(self.h, int(elems_per_block)), "tg_tangent_config")

@@ -14,6 +14,7 @@ unrelated batch to finish unless every lane or the memory budget is taken.
 The batch solver is pluggable so the admission logic can be exercised on the
 host without a GPU.
 """
+import ctypes
 import threading
 import time
 
@@ -188,6 +189,101 @@ class Server:
             ctx = st.pop("ctx", None)
             if ctx is not None:
                 ctx.close()
+
+
+class NativeServer:
+    """The request loop in the library (tg_serve_*): lanes are C++ threads,
+    each with its own context and resident RVE templates; admission by size,
+    device-memory budget and a latency target (predicted batch time).  This
+    class only replays a trace: it submits each request at its arrival time
+    and collects the results."""
+
+    def __init__(self, lanes=4, max_batch=1024, hbm_budget=64e9, precision=lib.MIXED,
+                 precond=lib.PRECOND_BLOCK_JACOBI, rel_tol=1e-8, lin_rel_tol=1e-4, target_batch_ms=0.0, device=0):
+        self.L = lib.load()
+        h = ctypes.c_void_p()
+        rc = self.L.tg_serve_create(ctypes.byref(h), int(device), int(lanes), int(max_batch), float(hbm_budget),
+                                    int(precision), int(precond), float(rel_tol), float(lin_rel_tol),
+                                    float(target_batch_ms))
+        if rc != lib.TG_OK:
+            raise lib.TahoeError(rc, "tg_serve_create", "bad arguments")
+        self.h = h
+
+    def submit(self, n, F):
+        F = np.ascontiguousarray(F, dtype=np.float64).reshape(9)
+        rid = ctypes.c_longlong(0)
+        rc = self.L.tg_serve_submit(self.h, int(n), F.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                    ctypes.byref(rid))
+        if rc != lib.TG_OK:
+            raise lib.TahoeError(rc, "tg_serve_submit", "bad arguments")
+        return rid.value
+
+    def result(self, rid):
+        """(status, P (3,3), latency ms) or None while pending"""
+        P = np.zeros(9)
+        st = ctypes.c_int(0)
+        lat = ctypes.c_double(0)
+        rc = self.L.tg_serve_poll(self.h, ctypes.c_longlong(rid), P.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  ctypes.byref(st), ctypes.byref(lat))
+        if rc == 1:
+            return None
+        if rc != lib.TG_OK:
+            raise lib.TahoeError(rc, "tg_serve_poll", "unknown request")
+        return st.value, P.reshape(3, 3), lat.value
+
+    def stats(self):
+        out = np.zeros(6)
+        self.L.tg_serve_stats(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 6)
+        return dict(batches=int(out[0]), mean_batch=float(out[1]), max_concurrent_lanes=int(out[2]),
+                    retried=int(out[3]), model_ms_per_1000_elements=float(out[4]), completed=int(out[5]))
+
+    def run(self, arrivals, ns, Fs, time_scale=1.0):
+        """Replays the trace in real time; same result dict as Server.run."""
+        count = len(arrivals)
+        ids = np.zeros(count, dtype=np.int64)
+        s0 = self.stats()
+        t0 = time.perf_counter()
+        for i in range(count):
+            wait = arrivals[i] * time_scale - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            ids[i] = self.submit(ns[i], Fs[i])
+        self.L.tg_serve_wait(self.h)
+        status = np.zeros(count, dtype=np.int64)
+        P = np.zeros((count, 3, 3))
+        lat = np.zeros(count)
+        for i in range(count):
+            st, Pi, li = self.result(ids[i])
+            status[i], P[i], lat[i] = st, Pi, li * 1e-3
+        s1 = self.stats()
+        okm = status == 0
+        # elapsed: first arrival to last completion (latency of the last finisher)
+        finish = arrivals * time_scale + lat
+        elapsed = float(np.max(finish) - arrivals[0] * time_scale) if count else 0.0
+        nb = s1["batches"] - s0["batches"]
+        return {
+            "P": P, "status": status, "latency": lat, "completed": int(okm.sum()), "elapsed_s": elapsed,
+            "solves_per_s": float(okm.sum() / elapsed) if elapsed > 0 else 0.0,
+            "p50_ms": float(np.percentile(lat[okm], 50) * 1e3) if okm.any() else None,
+            "p99_ms": float(np.percentile(lat[okm], 99) * 1e3) if okm.any() else None,
+            "mean_batch": float(count / nb) if nb else 0.0, "batches": [None] * nb,
+            "max_concurrent_lanes": s1["max_concurrent_lanes"], "retried": s1["retried"] - s0["retried"],
+            "errors": [], "failures": [], "model_ms_per_1000_elements": s1["model_ms_per_1000_elements"],
+        }
+
+    def error(self):
+        return self.L.tg_serve_error(self.h).decode()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tg_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _max_overlap(batches):

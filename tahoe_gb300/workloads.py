@@ -70,6 +70,17 @@ def spmv_bytes(nnzb, nnd, s_val):
     return nnzb * (9 * s_val + 4) + (nnd + 1) * 4 + nnd * s_vec + nnd * s_vec
 
 
+def spmv_bytes_sym(nnzb, nnd, s_val):
+    """Algorithmic DRAM bytes of one product streaming the symmetric format:
+    the nu = (nnzb + nnd) / 2 upper blocks (nine values + a column index),
+    the nl = (nnzb - nnd) / 2 lower entries (column + upper block id; their
+    transposed values are re-reads served from L2), upper and lower row
+    pointers, the gathered vector once, the product written, the dof mask."""
+    s_vec = 4 * s_val
+    nu, nl = (nnzb + nnd) // 2, (nnzb - nnd) // 2
+    return nu * (9 * s_val + 4) + nl * 8 + 2 * (nnd + 1) * 4 + 2 * nnd * s_vec + nnd
+
+
 def assembly_bytes(nel, nnzb, nnd, s_val):
     """Algorithmic bytes of one assembly launch: element blocks (36 blocks of
     3 rows padded to 4 values per element) read once, the 64 contribution

@@ -9,7 +9,7 @@ from tahoe_gb300 import autotune, lib
 class FakeCtx:
     def __init__(self, nnd=5000, nel=4000):
         self.nnd, self.nel = nnd, nel
-        self.cfg = {"tile_blocks": 640, "stages": 2, "tangent_epb": 8, "release": 0}
+        self.cfg = {"tile_blocks": 640, "stages": 2, "tangent_epb": 8, "release": 0, "sym": 0, "sym_tile": 0}
         self.tangents = 0
 
     def spmv_config(self, t, s):
@@ -21,6 +21,11 @@ class FakeCtx:
 
     def spmv_release(self, r):
         self.cfg["release"] = r
+
+    def spmv_symmetric(self, on, tile_blocks=0):
+        self.cfg["sym"] = on
+        if tile_blocks:
+            self.cfg["sym_tile"] = tile_blocks
 
     def tangent_config(self, e):
         self.cfg["tangent_epb"] = e
@@ -36,6 +41,9 @@ def fake_timer(ctx, which, reps):
     if which == autotune.KERNEL_SPMV and c["tile_blocks"] == 1024 and c["stages"] == 2 and c["release"] == 1:
         # a ring that fits the configuration call but not the launch
         raise lib.TahoeError(-8, "tg_time_kernel", "does not fit")
+    if which == autotune.KERNEL_SPMV and c["sym"]:
+        # symmetric format: faster than every full-storage shape only as mode 2 at 384 blocks per tile
+        return 0.5 if (c["sym"], c["sym_tile"]) == (2, 384) else 5.0
     if which == autotune.KERNEL_SPMV:
         return abs(c["tile_blocks"] - 768) / 100.0 + (0.5 if c["stages"] == 3 else 0.0) + 1.0 - 0.1 * c["release"]
     return {2: 3.0, 4: 1.5, 8: 2.0}[c["tangent_epb"]]
@@ -48,7 +56,8 @@ def test_picks_fastest_and_caches(tmp_path):
     out = t.tune(ctx, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=fake_timer)
     assert not out["cached"]
     assert (out["tile_blocks"], out["stages"], out["release"], out["tangent_epb"]) == (768, 2, 1, 4)
-    assert ctx.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1}
+    assert (out["sym"], out["sym_tile"]) == (2, 384) and out["spmv_ms"] == 0.5
+    assert ctx.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1, "sym": 2, "sym_tile": 384}
     # 1024x3 and 1536x2/3 do not fit and are skipped, not chosen
     assert out["spmv_sweep"]["1536x2r0"] is None and out["spmv_sweep"]["1024x3r1"] is None
     assert out["spmv_sweep"]["1024x2r1"] is None and out["spmv_sweep"]["1024x2r0"] is not None
@@ -59,7 +68,8 @@ def test_picks_fastest_and_caches(tmp_path):
     ctx2 = FakeCtx(nnd=5100, nel=4050)  # same size class
     t2 = autotune.Tuner(cache_path=path)
     out2 = t2.tune(ctx2, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=lambda *a: 1 / 0)
-    assert out2["cached"] and ctx2.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1}
+    assert out2["cached"] and ctx2.cfg == {"tile_blocks": 768, "stages": 2, "tangent_epb": 4, "release": 1,
+                                           "sym": 2, "sym_tile": 384}
     # another size class or precision is tuned separately
     assert autotune.signature(FakeCtx(nnd=50000), lib.MIXED, 1) != autotune.signature(ctx, lib.MIXED, 1)
     assert autotune.signature(ctx, lib.FP64, 1) != autotune.signature(ctx, lib.MIXED, 1)
@@ -68,3 +78,15 @@ def test_picks_fastest_and_caches(tmp_path):
 def test_pick_ignores_unavailable():
     assert autotune.pick({"a": None, "b": 2.0, "c": 1.0}) == ("c", 1.0)
     assert autotune.pick({"a": None}) == (None, float("inf"))
+
+
+def test_full_storage_kept_when_symmetric_is_slower(tmp_path):
+    def timer(ctx, which, reps):
+        if which == autotune.KERNEL_SPMV and ctx.cfg["sym"]:
+            return 9.0
+        return fake_timer(ctx, which, reps)
+
+    t = autotune.Tuner(cache_path=str(tmp_path / "t.json"), reps=4)
+    ctx = FakeCtx()
+    out = t.tune(ctx, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=timer)
+    assert out["sym"] == 0 and ctx.cfg["sym"] == 0

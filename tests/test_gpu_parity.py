@@ -192,14 +192,16 @@ def test_updated_lagrangian_newton_iterates_match_oracle():
         seq = []
         for it in range(4):
             n_o = o.residual(1.0, it - 1)
-            assert abs(n_g - n_o) <= 1e-12 * max(n_o, 1e-300), (form, it)
+            # relative to the step's first residual (late norms sit at round-off)
+            assert abs(n_g - n_o) <= 1e-12 * max(seq[0] if seq else n_o, 1e-300), (form, it)
             seq.append(n_g)
             n_g, _ = g.ctx.newton_iteration(precision=lib.FP64, lin_rel_tol=1e-13, lin_max_it=20000)
             o.newton_iteration(1.0, it - 1, 1e-13)
             assert rel_err(g.ctx.get_u(), o.get_u()) < 1e-10, (form, it)
         norms[form] = seq
         g.ctx.close()
-    assert rel_err(norms["updated_lagrangian"], norms["total_lagrangian"]) < 1e-10
+    nu, nt = np.array(norms["updated_lagrangian"]), np.array(norms["total_lagrangian"])
+    assert np.abs(nu - nt).max() <= 1e-10 * nt[0]
 
 
 def test_assembly_and_residual_bitwise_repeatable():
@@ -219,13 +221,14 @@ def test_assembly_and_residual_bitwise_repeatable():
 @pytest.mark.parametrize("tile_blocks", [512, 32])
 def test_symmetric_product_equals_full_storage(tile_blocks):
     """The single-vector product streaming the symmetric format (upper blocks,
-    lower blocks as transposes, output masked at prescribed dofs) gives the
-    PCG solution of the full block storage: FP64 to 1e-11, the mixed form to
-    1e-5, the same iteration count within two; a small tile size spreads the
-    rows over many tiles (transposed blocks from other tiles)."""
+    lower blocks as transposes, output masked at prescribed dofs; all three
+    launch shapes) gives the PCG solution of the full block storage: FP64 to
+    1e-11, the mixed form to 1e-5, the same iteration count within two; a
+    small tile size spreads the rows over many tiles (transposed blocks from
+    other tiles)."""
     mesh, fixed = cube_case(6, jitter=0.2, seed=4)
     g = gpu_model(mesh, "total_lagrangian", SIMO, fixed)
-    u = random_u(mesh.nnd, 0.02, 3)
+    u = random_u(mesh.nnd, 0.002, 3)  # small enough for a positive definite tangent
     for node, d in fixed:
         u[node, d] = 0.0
     g.ctx.set_u(u)
@@ -233,17 +236,18 @@ def test_symmetric_product_equals_full_storage(tile_blocks):
     for prec, tol, lt in ((lib.FP64, 1e-11, 1e-12), (lib.MIXED, 1e-5, 1e-6)):
         g.ctx.tangent(prec)
         res = {}
-        for on in (0, 1):
+        for on in (0, 1, 2, 3):
             g.ctx.spmv_symmetric(on, tile_blocks)
             for pc in (lib.PRECOND_JACOBI, lib.PRECOND_BLOCK_JACOBI):
                 du, its, rr, rc = g.ctx.pcg(R, rel_tol=lt, max_it=20000, precond=pc)
                 assert rc == 0 and rr < lt
                 res[on, pc] = (du, its)
             assert g.ctx.time_kernel(0, 2) > 0.0
-        for pc in (lib.PRECOND_JACOBI, lib.PRECOND_BLOCK_JACOBI):
-            assert rel_err(res[1, pc][0], res[0, pc][0]) < tol, (prec, pc)
-            assert abs(res[1, pc][1] - res[0, pc][1]) <= 2, (prec, pc)
-    g.ctx.spmv_symmetric(1, 512)
+        for on in (1, 2, 3):
+            for pc in (lib.PRECOND_JACOBI, lib.PRECOND_BLOCK_JACOBI):
+                assert rel_err(res[on, pc][0], res[0, pc][0]) < tol, (prec, on, pc)
+                assert abs(res[on, pc][1] - res[0, pc][1]) <= 2, (prec, on, pc)
+    g.ctx.spmv_symmetric(0, 512)
 
 
 def test_pcg_solves_oracle_system():

@@ -65,3 +65,24 @@ def test_lane_context_reused_across_batches():
     st, P_fresh = solve(*small, {"device": 0})
     assert np.all(st == 0)
     assert rel_err(P_reused, P_fresh) < 1e-12
+
+
+def test_native_request_loop_equals_one_at_a_time():
+    """The request loop in the library (tg_serve_*: lanes as C++ threads,
+    admission by size, memory and latency target): every request completes,
+    batches form, and each result is bitwise the same request solved alone
+    (the C++ RVE templates are the Python ones, node for node)."""
+    arr, ns, Fs = serve.sample_requests(24, 20000.0, seed=3, nmin=4, nmax=8)
+    srv = serve.NativeServer(lanes=2, max_batch=8, hbm_budget=8e9, precision=lib.MIXED, target_batch_ms=50.0)
+    try:
+        res = srv.run(arr, ns, Fs)
+    finally:
+        srv.close()
+    assert np.all(res["status"] == 0), res["status"]
+    assert res["mean_batch"] > 1.0
+    alone = serve.Server(serve.gpu_batch_solver(lib.MIXED), lanes=1, max_batch=1)
+    try:
+        one = alone.run(arr, ns, Fs, time_scale=0.0)
+    finally:
+        alone.close()
+    assert np.array_equal(one["P"], res["P"])
