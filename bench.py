@@ -434,6 +434,7 @@ def run_ours(args):
         line["c4"] = c4_batch(args.rves, args.c4_precond, with_cpu=False, macro=True)
         line["c5"] = c5_trace(args, rates=[args.c5_rate], requests=args.c5_requests,
                               plain_requests=args.c5_plain_requests)
+        line["c3"] = c3_run(args.c3_extra_steps, tune=False)
         line["extras_wall_s"] = round(time.perf_counter() - t_extra, 1)
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -655,6 +656,10 @@ def run_c5(args):
 
 
 def run_c3(args):
+    print(json.dumps(c3_run(args.c3_steps, args.max_step_cuts, args.quick_solve_iter, tune=not args.no_tune)))
+
+
+def c3_run(nsteps, max_step_cuts=6, quick_solve_iter=0, tune=True):
     """Configuration 3: small-strain J2 plate 96 x 96 x 48 under cyclic
     uniaxial displacement (+-0.5 % strain over 40 steps).  Both forms run the
     same load history through the reference's step sequence (Newton to 1e-8
@@ -662,7 +667,7 @@ def run_c3(args):
     (yielding) set of the mixed form is compared bitwise with the plain FP64
     form's, and the displacements at every original step end are compared."""
     from tahoe_gb300 import autotune, lib, workloads
-    nsteps = args.c3_steps
+    args = argparse.Namespace(no_tune=not tune, max_step_cuts=max_step_cuts, quick_solve_iter=quick_solve_iter)
     out, flags_ref, u_last = {}, {}, {}
     for name, prec in (("mixed", lib.MIXED), ("fp64", lib.FP64)):
         mesh, model, run = workloads.c3(nsteps=40)
@@ -735,7 +740,7 @@ def run_c3(args):
         "u_rel_err_mixed_vs_fp64_worst_step": float(max(
             np.abs(a - b).max() / max(np.abs(b).max(), 1e-300) for a, b in zip(u_last["mixed"], u_last["fp64"]))),
     }
-    print(json.dumps(line))
+    return line
 
 
 def run_kernel_only(args):
@@ -771,6 +776,7 @@ def main():
     ap.add_argument("--n", type=int, default=64, help="mesh size per side for --kernel")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--c3-steps", type=int, default=40, help="C3 load steps to run (of 40)")
+    ap.add_argument("--c3-extra-steps", type=int, default=2, help="C3 load steps in the default run's line")
     ap.add_argument("--max-step-cuts", type=int, default=6, help="C3 load-step cuts allowed (TimeManagerT)")
     ap.add_argument("--quick-solve-iter", type=int, default=0,
                     help="C3 NLSolver quick_solve_iter (<= 1: a cut step is never doubled back)")
@@ -785,7 +791,7 @@ def main():
                          "blocks)")
     ap.add_argument("--c4-precond", default="block", choices=["jacobi", "block"], help="C4 batch preconditioner")
     ap.add_argument("--c5-rate", type=float, default=5000.0, help="C5 arrival rate of the default run's trace")
-    ap.add_argument("--c5-target-ms", type=float, default=100.0,
+    ap.add_argument("--c5-target-ms", type=float, default=200.0,
                     help="C5 latency target: predicted batch time a lane admits up to (0: none)")
     ap.add_argument("--c5-requests", type=int, default=1000, help="C5 requests of the default run's trace")
     ap.add_argument("--c5-plain-requests", type=int, default=100, help="C5 one-at-a-time FP64 requests (default run)")

@@ -70,24 +70,33 @@ def test_rve_alone_equals_rve_in_batch(batch):
 
 
 def test_failing_rve_fails_alone():
-    """With one Newton iteration allowed, an RVE under a tiny deformation
-    converges (exact inner solves) while one under F = I + 0.05 S does not:
-    the batch reports the failure for that RVE alone, and the converged RVE's
-    result equals its own solve, bitwise."""
+    """With one Newton iteration allowed (exact inner solves) some RVEs of a
+    batch converge and some do not (an RVE under a tiny deformation starts
+    at round-off and cannot gain eight digits; F = I + 0.05 S converges in
+    one).  Every RVE's outcome in the batch is its outcome alone, the
+    failures are reported per RVE, and every converged RVE's result is its
+    own solve, bitwise."""
     rng = np.random.default_rng(5)
-    S0, S1 = rve.sample_F(rng) - np.eye(3), rve.sample_F(rng) - np.eye(3)
-    ns = np.array([4, 5])
-    Fs = np.stack([np.eye(3) + 2e-5 * S0, np.eye(3) + S1])
+    S = [rve.sample_F(rng) - np.eye(3) for _ in range(4)]
+    ns = np.array([4, 5, 4, 6])
+    Fs = np.stack([np.eye(3) + 2e-5 * S[0], np.eye(3) + S[1], np.eye(3) + 2e-5 * S[2], np.eye(3) + S[3]])
     kw = dict(precision=lib.FP64, rel_tol=1e-8, lin_rel_tol=1e-12, max_iterations=1)
+    alone = []
+    for r in range(len(ns)):
+        one = rve.RVEBatch(ns[r:r + 1], Fs[r:r + 1])
+        one.setup()
+        rc1, _, _, P1 = one.solve(**kw)
+        alone.append((int(one.status[0]), P1[0]))
     b = rve.RVEBatch(ns, Fs)
     b.setup()
     rc, rep, rel, P = b.solve(**kw)
-    assert rc == -6
-    assert list(b.status) == [0, -6]
-    one = rve.RVEBatch(ns[:1], Fs[:1])
-    one.setup()
-    rc1, _, _, P1 = one.solve(**kw)
-    assert rc1 == 0 and np.array_equal(P1[0], P[0])
+    st = [int(v) for v in b.status]
+    assert st == [a[0] for a in alone]
+    assert 0 in st and any(v != 0 for v in st)
+    assert rc == next(v for v in st if v != 0)
+    for r in range(len(ns)):
+        if st[r] == 0:
+            assert np.array_equal(P[r], alone[r][1]), r
 
 
 def test_batch_wide_solver_still_selectable(batch):
