@@ -48,48 +48,23 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
       T acc[9];
 #pragma unroll
       for (int k = 0; k < 9; ++k) acc[k] = T(0);
-      // The block's contributions in ascending (element, slot) order: the
-      // codes of up to eight in one round of loads, then the element blocks
-      // two at a time, so the diagonal block of a hex8 row (eight
-      // contributions) waits on five rounds of memory latency instead of
-      // sixteen while the register budget stays at four CTAs per SM.  The
-      // sum order is unchanged.
-      const int cbeg = cptr[j], cend = cptr[j + 1];
-      for (int cb = cbeg; cb < cend; cb += 8) {
-        int code[8];
+      const int c1 = cptr[j + 1];
+      for (int c = cptr[j]; c < c1; ++c) {
+        const int code = contrib[c];
+        const int e = code >> 6, a = (code >> 3) & 7, b = code & 7;
+        // the element block's three padded rows: one aligned vector load each
+        const V4* src = reinterpret_cast<const V4*>(
+            Ke + ((long long)e * kSlots + (a <= b ? upper_slot(a, b) : upper_slot(b, a))) * kKeBlock);
+        const V4 k0 = src[0], k1 = src[1], k2 = src[2];
+        const T m[9] = {k0.x, k0.y, k0.z, k1.x, k1.y, k1.z, k2.x, k2.y, k2.z};
+        if (a <= b) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) code[k] = cb + k < cend ? contrib[cb + k] : -1;
+          for (int k = 0; k < 9; ++k) acc[k] += m[k];
+        } else {
 #pragma unroll
-        for (int g = 0; g < 8; g += 2) {
-          if (code[g] < 0) break;
-          V4 blk[2][3];
+          for (int p = 0; p < 3; ++p)
 #pragma unroll
-          for (int k = 0; k < 2; ++k)
-            if (code[g + k] >= 0) {
-              const int e = code[g + k] >> 6, a = (code[g + k] >> 3) & 7, b = code[g + k] & 7;
-              // the element block's three padded rows: one aligned vector load each
-              const V4* src = reinterpret_cast<const V4*>(
-                  Ke + ((long long)e * kSlots + (a <= b ? upper_slot(a, b) : upper_slot(b, a))) * kKeBlock);
-              blk[k][0] = src[0];
-              blk[k][1] = src[1];
-              blk[k][2] = src[2];
-            }
-#pragma unroll
-          for (int k = 0; k < 2; ++k)
-            if (code[g + k] >= 0) {
-              const int a = (code[g + k] >> 3) & 7, b = code[g + k] & 7;
-              const T m[9] = {blk[k][0].x, blk[k][0].y, blk[k][0].z, blk[k][1].x, blk[k][1].y,
-                              blk[k][1].z, blk[k][2].x, blk[k][2].y, blk[k][2].z};
-              if (a <= b) {
-#pragma unroll
-                for (int q = 0; q < 9; ++q) acc[q] += m[q];
-              } else {
-#pragma unroll
-                for (int p = 0; p < 3; ++p)
-#pragma unroll
-                  for (int q = 0; q < 3; ++q) acc[p * 3 + q] += m[q * 3 + p];
-              }
-            }
+            for (int q = 0; q < 3; ++q) acc[p * 3 + q] += m[q * 3 + p];
         }
       }
       const int J = col[j];

@@ -1,22 +1,18 @@
 // (Block-)Jacobi preconditioned CG on the node-block CSR matrix, sm_103a.
 //
 // Each iteration is two kernels:
-//   pcg_spmv_kernel   the product of the preconditioned residual z (the one
-//                     vector gathered at the neighbours) with the direction
-//                     update folded into each row's epilogue:
-//                     p_I = z_I + beta p_I, q_I = (A z)_I + beta q_I (so
-//                     q = A p by recurrence), partial p.q; the last CTA
-//                     forms alpha
+//   pcg_spmv_kernel   q = A p, partial p.q; the last CTA forms alpha (the
+//                     product is exact each iteration: no recurrence for A p)
 //   pcg_update_kernel x += alpha p; r -= alpha q; z = M^-1 r; partial r.z,
-//                     r.r; the last CTA forms beta and the convergence flag
-// Both are plain launches on persistent grids: no grid barrier (the
-// direction update touches only a row's own entries, so it rides along with
-// the product of the row).  The reductions of FP64 partial sums run in a
-// fixed order (bitwise repeatable, no floating-point atomics) and compute
-// alpha / beta and the convergence flag on the device.  Iterations run in
-// chunks captured once in a CUDA graph; kernels return immediately once the
-// flag is set, and the host reads each chunk's flag while the next chunk
-// runs.
+//                     r.r; a grid barrier (cooperative launch); every CTA
+//                     then forms the same r.z and beta from the partials in
+//                     the same order and updates its nodes' p = z + beta p in
+//                     place, so the product gathers one vector per neighbour
+// The reductions of FP64 partial sums run in a fixed order (bitwise
+// repeatable, no floating-point atomics) and compute alpha / beta and the
+// convergence flag on the device.  Iterations run in chunks captured once in
+// a CUDA graph; kernels return immediately once the flag is set, and the host
+// reads each chunk's flag while the next chunk runs.
 //
 // Vectors are stored per node, padded to 4 lanes (float4 in the mixed form,
 // double4_32a in the plain FP64 form).  Dot products and norms accumulate in
@@ -84,7 +80,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
     x[n] = mk<V, T>(T(0), T(0), T(0));
     r[n] = mk<V, T>(rx, ry, rz);
     z[n] = mk<V, T>(zx, zy, zz);
-    p[n] = mk<V, T>(T(0), T(0), T(0));  // the first product forms p = z (beta = 0)
+    p[n] = mk<V, T>(zx, zy, zz);  // first direction p = z
     q[n] = mk<V, T>(T(0), T(0), T(0));
     v[0].add_prod(rx, zx);
     v[0].add_prod(ry, zy);
@@ -113,15 +109,13 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
 
 
 // The rows of one staged tile handled by this warp: 8 lanes per row, 4 rows
-// per warp at a time, each lane over every 8th block of the gathered vector
-// p; the row epilogue writes q (and, fused, the direction) and accumulates
-// the dot product into v.
+// per warp at a time, each lane over every 8th block; q = A p written for the
+// rows, p.q accumulated into v.
 template <typename T>
 __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
                                                const typename Vec4<T>::type* __restrict__ p,
                                                typename Vec4<T>::type* __restrict__ q, Acc<T>& v0,
-                                               double* __restrict__ node_dot, typename Vec4<T>::type* pdir,
-                                               T beta) {
+                                               double* __restrict__ node_dot) {
   using V = typename Vec4<T>::type;
   const int sub = lane & 7;
   Acc<T>* v = &v0;
@@ -133,14 +127,8 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
   for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
     const bool live = li < nrows;
     const int I = r0 + li;
-    V pi, qo, po;
-    if (live && sub == 0) {
-      pi = p[I];
-      if (pdir) {
-        qo = q[I];
-        po = pdir[I];
-      }
-    }
+    V pi;
+    if (live && sub == 0) pi = p[I];
     T a0 = T(0), a1 = T(0), a2 = T(0);
     const int e0 = live ? rp[li] : 0;
     const int e1 = live ? rp[li + 1] : 0;
@@ -181,7 +169,19 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
       a1 += __shfl_xor_sync(0xffffffffu, a1, o);
       a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
-    if (live && sub == 0) row_epilogue<T, V>(I, pi, qo, po, a0, a1, a2, q, pdir, beta, v[0], node_dot);
+    if (live && sub == 0) {
+      q[I] = mk<V, T>(a0, a1, a2);
+      v[0].add_prod(pi.x, a0);
+      v[0].add_prod(pi.y, a1);
+      v[0].add_prod(pi.z, a2);
+      if (node_dot) {  // the row's own p.q (per-RVE reductions of a segmented batch)
+        Acc<T> d;
+        d.add_prod(pi.x, a0);
+        d.add_prod(pi.y, a1);
+        d.add_prod(pi.z, a2);
+        node_dot[I] = d.value();
+      }
+    }
   }
 }
 
@@ -197,14 +197,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
                                                        const unsigned char* __restrict__ blob, int cap,
                                                        const typename Vec4<T>::type* __restrict__ p,
                                                        typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                       PcgScalars* sc, int* status, double* node_dot,
-                                                       typename Vec4<T>::type* pdir) {
+                                                       PcgScalars* sc, int* status, double* node_dot) {
   using V = typename Vec4<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
   if (((volatile PcgScalars*)sc)->done) return;
-  const T beta = pdir ? T(sc->beta) : T(0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -244,7 +242,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
       stuck = s;
       break;
     }
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0], node_dot, pdir, beta);
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0], node_dot);
     __syncthreads();  // stage s is free for the copy issued next iteration
   }
   if (stuck >= 0 && threadIdx.x == 0) {
@@ -284,14 +282,12 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
                                                           const unsigned char* __restrict__ blob, int cap,
                                                           const typename Vec4<T>::type* __restrict__ p,
                                                           typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                          PcgScalars* sc, int* status, double* node_dot,
-                                                          typename Vec4<T>::type* pdir) {
+                                                          PcgScalars* sc, int* status, double* node_dot) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NST];
   __shared__ __align__(8) uint64_t empty[NST];
   __shared__ volatile int abort_flag;
   if (((volatile PcgScalars*)sc)->done) return;
-  const T beta = pdir ? T(sc->beta) : T(0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -352,7 +348,7 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
       break;
     }
     if (threadIdx.x == 0) ++seen[s];
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0], node_dot, pdir, beta);
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v[0], node_dot);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
@@ -381,25 +377,25 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
   }
 }
 
-// One streaming pass per iteration: x += alpha p; r -= alpha q; z = M^-1 r
-// and the partial r.z and r.r; the last CTA forms the totals, beta for the
-// next product (which folds p = z + beta p into its epilogue) and the
-// convergence flag.  Each thread takes its nodes n0, n0 + stride, ... four
-// (FP32) or two (FP64) at a time with all their loads issued before any use
-// (the partial sums keep that node order).  No grid barrier: the direction
-// update that needed one lives in the product.
+// Launched cooperatively (every CTA resident): the grid barrier between the
+// two phases is bounded and, should it ever give up, the solve ends flagged
+// as broken down instead of waiting.  Each thread takes its nodes
+// n0, n0 + stride, ... four (FP32) or two (FP64) at a time with all their
+// loads issued before any use (the partial sums keep that node order).
 template <typename T>
-__global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __restrict__ minv,
-                                                         typename Vec4<T>::type* __restrict__ x,
-                                                         typename Vec4<T>::type* __restrict__ r,
-                                                         typename Vec4<T>::type* __restrict__ z,
-                                                         const typename Vec4<T>::type* __restrict__ p,
-                                                         const typename Vec4<T>::type* __restrict__ q,
-                                                         double* partials, PcgScalars* sc) {
+__global__ void __launch_bounds__(256, 2) pcg_update_kernel(int nnd, const T* __restrict__ minv,
+                                                            typename Vec4<T>::type* __restrict__ x,
+                                                            typename Vec4<T>::type* __restrict__ r,
+                                                            typename Vec4<T>::type* __restrict__ z,
+                                                            typename Vec4<T>::type* __restrict__ p,
+                                                            const typename Vec4<T>::type* __restrict__ q,
+                                                            double* partials, PcgScalars* sc, int* status) {
   using V = typename Vec4<T>::type;
-  constexpr int U = sizeof(T) == 4 ? 4 : 2;
+  constexpr int U = sizeof(T) == 4 ? 4 : 2;  // within 128 registers: two CTAs per SM
+  __shared__ double totals[2];
   if (((volatile PcgScalars*)sc)->done) return;
   const T alpha = T(sc->alpha);
+  const double rz_old = sc->rz;  // read before the barrier: CTA 0 replaces it after
   const int stride = gridDim.x * blockDim.x;
   const int n0 = blockIdx.x * blockDim.x + threadIdx.x;
   Acc<T> v[2];
@@ -443,13 +439,68 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __res
       }
     }
   }
-  double tot[2];
-  if (last_block_total<T, 2>(v, partials, &sc->count_b, tot) && threadIdx.x == 0) {
-    const double rz = tot[0], rr = tot[1];
+  {
+    double bt[2];
+    block_total<T, 2>(v, bt);
+    if (threadIdx.x == 0) {
+      partials[blockIdx.x] = bt[0];
+      partials[gridDim.x + blockIdx.x] = bt[1];
+    }
+  }
+  if (!grid_barrier(&sc->bar_count, kBarrierLimit)) {
+    if (threadIdx.x == 0) {
+      atomicOr(status, kStatusWaitTimeout);
+      sc->fail = 5;
+      atomicExch(&sc->done, 2);
+    }
+    return;
+  }
+  // every CTA forms the same totals from the partials, in the same order
+  // (one warp: lane-strided sums, then a fixed shuffle tree)
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll 4
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+      s0 += ((volatile double*)partials)[b];
+      s1 += ((volatile double*)partials)[gridDim.x + b];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if (lane == 0) {
+      totals[0] = s0;
+      totals[1] = s1;
+    }
+  }
+  __syncthreads();
+  const double rz = totals[0], rr = totals[1];
+  const double beta_d = rz / rz_old;
+  const T beta = T(beta_d);
+  // next search direction, in place: p = z + beta p
+  for (int base = n0; base < nnd; base += U * stride) {
+    V zn[U], pn[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = base + u * stride;
+      if (n < nnd) {
+        zn[u] = z[n];
+        pn[u] = p[n];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = base + u * stride;
+      if (n < nnd)
+        p[n] = mk<V, T>(zn[u].x + beta * pn[u].x, zn[u].y + beta * pn[u].y, zn[u].z + beta * pn[u].z);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     const int it = sc->iters + 1;
     sc->iters = it;
-    sc->beta = rz / sc->rz;
-    sc->rz_old = sc->rz;
+    sc->beta = beta_d;
     sc->rz = rz;
     sc->rr = rr;
     int done = 0;
@@ -461,7 +512,7 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int nnd, const T* __res
     } else if (it >= sc->max_it) {
       done = 3;
     }
-    if (done) atomicCAS(&sc->done, 0, done);  // a product's breakdown keeps its flag
+    if (done) atomicCAS(&sc->done, 0, done);  // a barrier failure elsewhere keeps its flag
   }
 }
 
@@ -524,17 +575,17 @@ int spmv_config(Context* c, Grids& g) {
 }
 template <typename T>
 void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc,
-                 double* node_dot = nullptr, void* pdir = nullptr) {
+                 double* node_dot = nullptr) {
   using V = typename Vec4<T>::type;
   const bool f32 = std::is_same<T, float>::value;
   if (g.sym) {
-    sym_launch(c, f32 ? TG_MIXED : TG_FP64, g.sl, p, q, partials, sc, node_dot, pdir);
+    sym_launch(c, f32 ? TG_MIXED : TG_FP64, g.sl, p, q, partials, sc, node_dot);
     return;
   }
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);
-#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot, (V*)pdir
+#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot
   if (g.warp_release) {
     if (g.stages == 3)
       pcg_spmv_wr_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
@@ -549,8 +600,8 @@ void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* par
 #undef TG_SPMV_ARGS
 }
 
-// The vector update on a persistent grid (every SM busy, the last-CTA
-// reduction's partials within capacity).
+// The vector update as a cooperative launch (its grid barrier needs every
+// CTA resident; the grid is clamped to what fits at once).
 template <typename T>
 cudaError_t launch_update(Context* c, int grid, const T* minv, void* x, void* r, void* z, void* p, const void* q,
                           double* partials, PcgScalars* sc) {
@@ -558,11 +609,19 @@ cudaError_t launch_update(Context* c, int grid, const T* minv, void* x, void* r,
   int per_sm = 0;
   const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_update_kernel<T>, 256, 0);
   if (oe != cudaSuccess) return oe;
-  grid = std::max(1, std::min(grid, c->num_sms * std::max(per_sm, 1)));
-  grid = std::min(grid, c->partials_cap / 2);
-  pcg_update_kernel<T><<<grid, 256, 0, c->stream>>>(c->nnd, minv, (V*)x, (V*)r, (V*)z, (const V*)p, (const V*)q,
-                                                   partials, sc);
-  return cudaGetLastError();
+  grid = std::max(1, std::min(grid, c->num_sms * per_sm));  // every CTA resident at once
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, pcg_update_kernel<T>, c->nnd, minv, (V*)x, (V*)r, (V*)z, (V*)p, (const V*)q,
+                            partials, sc, c->d_status);
 }
 
 Grids grids(const Context* c) {
@@ -570,7 +629,7 @@ Grids grids(const Context* c) {
   g.spmv = 0;
   g.spmv_smem = 0;
   g.stages = 8;
-  g.vec = std::min((c->nnd + 255) / 256, c->num_sms * 4);
+  g.vec = std::min((c->nnd + 255) / 256, c->num_sms * 2);
   return g;
 }
 
@@ -585,7 +644,7 @@ int capture_chunk(Context* c, const T* minv) {
   if (!ok(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return TG_ERR_CUDA;
   cudaError_t le = cudaSuccess;
   for (int k = 0; k < kChunk && le == cudaSuccess; ++k) {
-    launch_spmv<T>(c, g, c->d_z, c->d_q, c->d_partials, c->d_pcg, nullptr, c->d_p);
+    launch_spmv<T>(c, g, c->d_p, c->d_q, c->d_partials, c->d_pcg);
     le = cudaGetLastError();
     if (le == cudaSuccess)
       le = launch_update<T>(c, g.vec, minv, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_partials, c->d_pcg);
@@ -811,7 +870,7 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
     cudaMemcpyAsync(c->d_pcg, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream);
     cudaEventRecord(a, c->stream);
     if (which == 0)
-      launch_spmv<T>(c, g, c->d_z, c->d_q, c->d_partials, c->d_pcg, nullptr, c->d_p);
+      launch_spmv<T>(c, g, c->d_p, c->d_q, c->d_partials, c->d_pcg);
     else if (!ok(c, launch_update<T>(c, g.vec, minv, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_partials,
                                      c->d_pcg),
                  "pcg_update_kernel"))
@@ -879,7 +938,7 @@ int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigne
   const int max_chunks = max_it / kChunk + 2;
   for (int ch = 0; ch < max_chunks; ++ch) {
     for (int k = 0; k < kChunk; ++k) {
-      launch_spmv<T>(c, g, z, q, partials, sc, nullptr, p);
+      launch_spmv<T>(c, g, p, q, partials, sc);
       if (!ok(c, launch_update<T>(c, g.vec, minv, x, r, z, p, q, partials, sc), "pcg_update_kernel"))
         return TG_ERR_CUDA;
     }

@@ -130,40 +130,6 @@ __device__ __forceinline__ void apply_minv(const T* __restrict__ minv, int n, T 
   zz = B[6] * rx + B[7] * ry + B[8] * rz;
 }
 
-// Row epilogue of the PCG product, a = (A g)_I for the gathered vector g.
-// Plain (pdir == nullptr): q_I = a and the row's g_I . a.  Fused: the
-// direction update of the conjugate-gradient recurrence is folded into the
-// product, p_I = g_I + beta p_I and q_I = a + beta q_I (q = A p kept by
-// recurrence), both on the row's own entries, and the row's p_I . q_I.
-// gi, qo, po are the row's own entries, loaded when the row started.
-template <typename T, typename V>
-__device__ __forceinline__ void row_epilogue(int I, const V& gi, const V& qo, const V& po, T a0, T a1, T a2, V* q,
-                                             V* pdir, T beta, Acc<T>& v, double* node_dot) {
-  if (pdir) {
-    a0 += beta * qo.x;
-    a1 += beta * qo.y;
-    a2 += beta * qo.z;
-    const T px = gi.x + beta * po.x, py = gi.y + beta * po.y, pz = gi.z + beta * po.z;
-    q[I] = mk<V, T>(a0, a1, a2);
-    pdir[I] = mk<V, T>(px, py, pz);
-    v.add_prod(px, a0);
-    v.add_prod(py, a1);
-    v.add_prod(pz, a2);
-    return;
-  }
-  q[I] = mk<V, T>(a0, a1, a2);
-  v.add_prod(gi.x, a0);
-  v.add_prod(gi.y, a1);
-  v.add_prod(gi.z, a2);
-  if (node_dot) {  // the row's own g.(A g) (per-RVE reductions of a segmented batch)
-    Acc<T> d;
-    d.add_prod(gi.x, a0);
-    d.add_prod(gi.y, a1);
-    d.add_prod(gi.z, a2);
-    node_dot[I] = d.value();
-  }
-}
-
 // ---- bulk-copy (TMA) staging of the streamed matrix ----------------------
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));

@@ -106,7 +106,7 @@ __device__ __forceinline__ void sym_tile_rows(const unsigned char* sbase, const 
                                               const T* __restrict__ gv1, const uint8_t* __restrict__ mask, int lane,
                                               int warp, int nwarps, const typename Vec4<T>::type* __restrict__ p,
                                               typename Vec4<T>::type* __restrict__ q, Acc<T>& dot,
-                                              double* __restrict__ node_dot, typename Vec4<T>::type* pdir, T beta) {
+                                              double* __restrict__ node_dot) {
   using V = typename Vec4<T>::type;
   using V8 = typename V8T<T>::type;
   const SymTileView tv = sym_view(sbase);
@@ -114,14 +114,8 @@ __device__ __forceinline__ void sym_tile_rows(const unsigned char* sbase, const 
   for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < tv.nrows; li += nwarps * 4) {
     const bool live = li < tv.nrows;
     const int I = tv.r0 + li;
-    V pi, qo, po;
-    if (live && sub == 0) {
-      pi = p[I];
-      if (pdir) {
-        qo = q[I];
-        po = pdir[I];
-      }
-    }
+    V pi;
+    if (live && sub == 0) pi = p[I];
     T a0 = T(0), a1 = T(0), a2 = T(0);
     const int u0 = live ? tv.urp[li] : 0, u1 = live ? tv.urp[li + 1] : 0;
     const int l0 = live ? tv.lrp[li] : 0, l1 = live ? tv.lrp[li + 1] : 0;
@@ -171,7 +165,17 @@ __device__ __forceinline__ void sym_tile_rows(const unsigned char* sbase, const 
       if (!(m & 1)) a0 = T(0);
       if (!(m & 2)) a1 = T(0);
       if (!(m & 4)) a2 = T(0);
-      row_epilogue<T, V>(I, pi, qo, po, a0, a1, a2, q, pdir, beta, dot, node_dot);
+      q[I] = mk<V, T>(a0, a1, a2);
+      dot.add_prod(pi.x, a0);
+      dot.add_prod(pi.y, a1);
+      dot.add_prod(pi.z, a2);
+      if (node_dot) {  // the row's own p.q (per-RVE reductions of a segmented batch)
+        Acc<T> d;
+        d.add_prod(pi.x, a0);
+        d.add_prod(pi.y, a1);
+        d.add_prod(pi.z, a2);
+        node_dot[I] = d.value();
+      }
     }
   }
 }
@@ -188,13 +192,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? MINB : 2) pcg_spmv_sym_k
     const unsigned char* __restrict__ sblob, int cap_s, int cap_v8,
     int cap_v1, const typename V8T<T>::type* __restrict__ gv8, const T* __restrict__ gv1,
     const uint8_t* __restrict__ mask, const typename Vec4<T>::type* __restrict__ p, typename Vec4<T>::type* __restrict__ q,
-    double* partials, PcgScalars* sc, int* status, double* node_dot, typename Vec4<T>::type* pdir) {
+    double* partials, PcgScalars* sc, int* status, double* node_dot) {
   using V8 = typename V8T<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
   if (((volatile PcgScalars*)sc)->done) return;
-  const T beta = pdir ? T(sc->beta) : T(0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const size_t stage_bytes = (size_t)cap_s + cap_v8 + cap_v1;
   if (threadIdx.x == 0) {
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? MINB : 2) pcg_spmv_sym_k
     const int k0 = reinterpret_cast<const int*>(st)[2];
     const V8* sv8 = reinterpret_cast<const V8*>(st + cap_s);
     const T* sv1 = reinterpret_cast<const T*>(st + cap_s + cap_v8) + (k0 & (kV1Align - 1));
-    sym_tile_rows<T>(st, sv8, sv1, gv8, gv1, mask, lane, warp, nwarps, p, q, v[0], node_dot, pdir, beta);
+    sym_tile_rows<T>(st, sv8, sv1, gv8, gv1, mask, lane, warp, nwarps, p, q, v[0], node_dot);
     __syncthreads();  // stage s is free for the copy issued next iteration
   }
   if (stuck >= 0 && threadIdx.x == 0) {
@@ -516,7 +519,7 @@ int sym_config(Context* c, int precision, SymLaunch& L) {
 
 template <typename T>
 static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q, double* partials, PcgScalars* sc,
-                         double* node_dot, void* pdir) {
+                         double* node_dot) {
   using V = typename Vec4<T>::type;
   const SymStore& s = c->sym;
   const bool f32 = std::is_same<T, float>::value;
@@ -524,7 +527,7 @@ static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q,
       reinterpret_cast<const typename V8T<T>::type*>(f32 ? (const void*)s.d_v8_32 : (const void*)s.d_v8_64);
   const T* gv1 = reinterpret_cast<const T*>(f32 ? (const void*)s.d_v1_32 : (const void*)s.d_v1_64);
 #define TG_SYM_ARGS s.ntiles, s.d_off, s.d_koff, s.d_blob, s.cap_struct, cap_bytes_v8<T>(s), cap_bytes_v1<T>(s), gv8, \
-    gv1, c->d_mask, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot, (V*)pdir
+    gv1, c->d_mask, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot
   if (L.stages == 3)
     pcg_spmv_sym_kernel<T, 3, 3><<<L.grid, 256, L.smem, c->stream>>>(TG_SYM_ARGS);
   else if (L.minb == 4)
@@ -535,11 +538,11 @@ static void sym_launch_t(Context* c, const SymLaunch& L, const void* p, void* q,
 }
 
 void sym_launch(Context* c, int precision, const SymLaunch& L, const void* p, void* q, double* partials,
-                PcgScalars* sc, double* node_dot, void* pdir) {
+                PcgScalars* sc, double* node_dot) {
   if (precision == TG_MIXED)
-    sym_launch_t<float>(c, L, p, q, partials, sc, node_dot, pdir);
+    sym_launch_t<float>(c, L, p, q, partials, sc, node_dot);
   else
-    sym_launch_t<double>(c, L, p, q, partials, sc, node_dot, pdir);
+    sym_launch_t<double>(c, L, p, q, partials, sc, node_dot);
 }
 
 void sym_free(Context* c) {

@@ -47,7 +47,7 @@ struct PcgScalars {
   int iters;
   int max_it;
   unsigned int count_a, count_b;  // last-block-done counters
-  unsigned int bar_count;  // not used by the single-vector solve (its update has no grid barrier)
+  unsigned int bar_count;  // arrivals at the vector update's grid barrier (reset per solve)
   int fail;  // breakdown cause: 1 init non-finite, 2 p.q <= 0, 3 p.q non-finite, 4 update non-finite
 };
 
@@ -327,7 +327,7 @@ int sym_build(Context* c, int tile_blocks);
 int sym_convert(Context* c, int precision);  // values from the last assembly
 int sym_config(Context* c, int precision, SymLaunch& L);
 void sym_launch(Context* c, int precision, const SymLaunch& L, const void* p, void* q, double* partials,
-                PcgScalars* sc, double* node_dot, void* pdir);
+                PcgScalars* sc, double* node_dot);
 // per-RVE solves of a segmented batch (segpcg.cu)
 int pcg_solve_segmented(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
                         double* rel_res);
