@@ -373,6 +373,25 @@ int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
  * barrier after each staged tile; 1 each warp releases the stage on an
  * mbarrier and moves on (results are bitwise the same) */
 int tg_spmv_release(tg_context* ctx, int per_warp);
+/* Recurrences of the single-vector PCG (both precisions, full block
+ * storage).  form = 1 (default): the single-reduction form of Chronopoulos &
+ * Gear -- per iteration one product kernel (w = A u, CTA partials of u.w) and
+ * one vector kernel whose CTAs each form the iteration's scalars from the
+ * partials and run one fused pass over p, s, x, r, u; no grid barrier and no
+ * atomic in either kernel.  form = 0: the textbook recurrences (product with
+ * a last-block reduction; vector update with a grid barrier between its two
+ * passes).  Both solve the same (block-)Jacobi CG system to the same
+ * tolerance; the iterates differ by rounding.  The symmetric format,
+ * segmented batches and the no-allocation entry point use their own
+ * kernels. */
+int tg_pcg_form(tg_context* ctx, int form);
+/* L2 priorities of the streamed matrix.  bytes >= 0: the leading whole
+ * tiles within `bytes` of the matrix storage are copied with evict_last
+ * (kept in the L2 from one product to the next) and the rest with
+ * evict_first (streamed past the PCG vectors, which then stay L2-resident
+ * across the iterations); default 16 MiB.  bytes = -1: plain bulk copies.
+ * A cache hint only: results are bitwise the same for every value. */
+int tg_spmv_l2_keep(tg_context* ctx, long long bytes);
 /* Storage the single-vector PCG product streams: on = 0 (default) the full
  * block storage; on = 1, 2, 3 the symmetric format -- the upper node blocks
  * only, each lower block read as the transpose of its upper twin (the

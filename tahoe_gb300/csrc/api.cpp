@@ -34,6 +34,7 @@ void free_device(Context* c) {
   // the caller's timer events outlive mesh changes (a timed region may
   // cover composing a batch mesh)
   seg_free(c);
+  cg_free(c);
   c->d_u_ckpt = c->d_R_ckpt = nullptr;
   c->ckpt_valid = false;
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
@@ -44,6 +45,7 @@ void free_device(Context* c) {
 
 void free_all(Context* c) {
   seg_free(c);
+  cg_free(c);
   if (c->ev_a) cudaEventDestroy(c->ev_a);
   if (c->ev_b) cudaEventDestroy(c->ev_b);
   c->ev_a = c->ev_b = nullptr;
@@ -160,6 +162,8 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->pcg_graph_key = -1;
   c->tangent_precision = -1;
   c->d_x = c->d_r = c->d_z = c->d_p = c->d_q = nullptr;
+  c->d_cg_s = nullptr;
+  c->cg_s_precision = -1;
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
   c->d_geo = nullptr;
@@ -200,7 +204,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
               dalloc(c, &c->d_contrib_ptr, (size_t)nnzb + 1) && dalloc(c, &c->d_contrib, nip * 8) &&
               dalloc(c, &c->d_u, (size_t)nnd) && dalloc(c, &c->d_fext, (size_t)nnd) && dalloc(c, &c->d_R, (size_t)nnd) &&
               dalloc(c, &c->d_fint, nip) && dalloc(c, &c->d_status, 1) && dalloc(c, &c->d_resid, 1) &&
-              dalloc(c, &c->d_pcg, 1);
+              dalloc(c, &c->d_pcg, 2);  // [1]: next state of the single-reduction PCG
   c->partials_cap = 4096;
   good = good && dalloc(c, &c->d_partials, (size_t)c->partials_cap * 2);
   good = good && dalloc(c, &c->d_j2_flags, nip) && dalloc(c, &c->d_j2_alloc, (size_t)nel) &&
@@ -215,7 +219,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
          ok(c, cudaMemsetAsync(c->d_R, 0, sizeof(double4_32a) * nnd, s), "R") &&
          ok(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s), "st") &&
          ok(c, cudaMemsetAsync(c->d_resid, 0, sizeof(ResidScalars), s), "rs") &&
-         ok(c, cudaMemsetAsync(c->d_pcg, 0, sizeof(PcgScalars), s), "pcg") &&
+         ok(c, cudaMemsetAsync(c->d_pcg, 0, 2 * sizeof(PcgScalars), s), "pcg") &&
          ok(c, cudaMemsetAsync(c->d_j2_flags, TG_J2_UNALLOCATED, nip, s), "fl") &&
          ok(c, cudaMemsetAsync(c->d_j2_alloc, 0, nel, s), "al") &&
          ok(c, cudaMemsetAsync(c->d_j2_alpha, 0, sizeof(double) * nip, s), "a") &&
@@ -373,11 +377,18 @@ int build_tiles(Context* c, int tile_blocks) {
           "off") ||
       !ok(c, cudaStreamSynchronize(st), "sync"))
     return TG_ERR_CUDA;
-  // the captured PCG chunk bakes in the launch shape
+  drop_graphs(c);  // the captured iterations bake in the launch shape
+  return TG_OK;
+}
+
+void drop_graphs(Context* c) {
+  cg_free(c);
   if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
   c->pcg_graph = nullptr;
   c->pcg_graph_key = -1;
-  return TG_OK;
+  if (c->seg.graph) cudaGraphExecDestroy(c->seg.graph);
+  c->seg.graph = nullptr;
+  c->seg.graph_key = -1;
 }
 
 // Allocates the matrix storage of one precision and writes its structure
@@ -410,10 +421,20 @@ int tg_spmv_config(tg_context* c, int tile_blocks, int stages) {
 int tg_spmv_release(tg_context* c, int per_warp) {
   if (!c || (per_warp != 0 && per_warp != 1)) return TG_ERR_ARG;
   c->spmv_warp_release = per_warp;
-  // the captured PCG chunk bakes in the kernel
-  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
-  c->pcg_graph = nullptr;
-  c->pcg_graph_key = -1;
+  drop_graphs(c);  // the captured iterations bake in the kernel
+  return TG_OK;
+}
+
+int tg_pcg_form(tg_context* c, int form) {
+  if (!c || (form != 0 && form != 1)) return TG_ERR_ARG;
+  c->pcg_form = form;
+  return TG_OK;
+}
+
+int tg_spmv_l2_keep(tg_context* c, long long bytes) {
+  if (!c || bytes < -1) return TG_ERR_ARG;
+  c->l2_keep = bytes;
+  drop_graphs(c);  // the captured iterations bake in the tiles kept
   return TG_OK;
 }
 
@@ -422,10 +443,7 @@ int tg_spmv_symmetric(tg_context* c, int on, int tile_blocks) {
   if (c->nnd > 0 && cudaSetDevice(c->device) != cudaSuccess) return TG_ERR_CUDA;
   c->sym_mode = on;
   if (tile_blocks) c->sym_tile_blocks = tile_blocks;
-  // the captured PCG chunk bakes in the product
-  if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
-  c->pcg_graph = nullptr;
-  c->pcg_graph_key = -1;
+  drop_graphs(c);  // the captured iterations bake in the product
   // values of the current tangent in the (re-)built format
   if (sym_active(c) && c->tangent_precision >= 0) return sym_convert(c, c->tangent_precision);
   return TG_OK;

@@ -108,81 +108,20 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
 }
 
 
-// The rows of one staged tile handled by this warp: 8 lanes per row, 4 rows
-// per warp at a time, each lane over every 8th block; q = A p written for the
-// rows, p.q accumulated into v.
-template <typename T>
-__device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
-                                               const typename Vec4<T>::type* __restrict__ p,
-                                               typename Vec4<T>::type* __restrict__ q, Acc<T>& v0,
-                                               double* __restrict__ node_dot) {
-  using V = typename Vec4<T>::type;
-  const int sub = lane & 7;
-  Acc<T>* v = &v0;
-  const int* hdr = reinterpret_cast<const int*>(base);
-  const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
-  const int* rp = hdr + 4;
-  const int* cl = rp + ceil4(nrows + 1);
-  const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
-  for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
-    const bool live = li < nrows;
-    const int I = r0 + li;
-    V pi;
-    if (live && sub == 0) pi = p[I];
-    T a0 = T(0), a1 = T(0), a2 = T(0);
-    const int e0 = live ? rp[li] : 0;
-    const int e1 = live ? rp[li + 1] : 0;
-    // the first 4 blocks of this lane (32 per row, a hex8 row has at most
-    // 27): all column indices, then all neighbour gathers, then the
-    // arithmetic, so the L2 round trips of one lane overlap instead of
-    // chaining
-    {
-      int Jk[4];
-      V pk[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int j = e0 + sub + 8 * u;
-        Jk[u] = j < e1 ? cl[j] : -1;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (Jk[u] >= 0) pk[u] = p[Jk[u]];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (Jk[u] >= 0) {
-          const T* vv = pl + e0 + sub + 8 * u;
-          a0 += vv[0 * ps] * pk[u].x + vv[1 * ps] * pk[u].y + vv[2 * ps] * pk[u].z;
-          a1 += vv[3 * ps] * pk[u].x + vv[4 * ps] * pk[u].y + vv[5 * ps] * pk[u].z;
-          a2 += vv[6 * ps] * pk[u].x + vv[7 * ps] * pk[u].y + vv[8 * ps] * pk[u].z;
-        }
-    }
-    for (int j = e0 + sub + 32; j < e1; j += 8) {
-      const V pj = p[cl[j]];
-      const T* vv = pl + j;
-      a0 += vv[0 * ps] * pj.x + vv[1 * ps] * pj.y + vv[2 * ps] * pj.z;
-      a1 += vv[3 * ps] * pj.x + vv[4 * ps] * pj.y + vv[5 * ps] * pj.z;
-      a2 += vv[6 * ps] * pj.x + vv[7 * ps] * pj.y + vv[8 * ps] * pj.z;
-    }
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (live && sub == 0) {
-      q[I] = mk<V, T>(a0, a1, a2);
-      v[0].add_prod(pi.x, a0);
-      v[0].add_prod(pi.y, a1);
-      v[0].add_prod(pi.z, a2);
-      if (node_dot) {  // the row's own p.q (per-RVE reductions of a segmented batch)
-        Acc<T> d;
-        d.add_prod(pi.x, a0);
-        d.add_prod(pi.y, a1);
-        d.add_prod(pi.z, a2);
-        node_dot[I] = d.value();
-      }
-    }
+// Whether a product launch has nothing to do (the solve is over), decided
+// by one thread and the same for every thread of the CTA.  For the
+// single-reduction PCG (cta_only) block 0 first hands the state the last
+// vector kernel wrote (scalars[1]) over to the one the next vector kernel
+// reads (scalars[0]); the flag is read from scalars[1], which no kernel
+// rewrites while a product runs except on a stage timeout.
+__device__ __forceinline__ bool skip_launch(PcgScalars* sc, int cta_only) {
+  __shared__ int skip;
+  if (threadIdx.x == 0) {
+    if (cta_only && blockIdx.x == 0) sc[0] = sc[1];
+    skip = ((volatile PcgScalars*)(cta_only ? sc + 1 : sc))->done != 0;
   }
+  __syncthreads();
+  return skip != 0;
 }
 
 // q = A p on a persistent grid.  Each CTA streams its row tiles through a ring of NST
@@ -197,12 +136,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
                                                        const unsigned char* __restrict__ blob, int cap,
                                                        const typename Vec4<T>::type* __restrict__ p,
                                                        typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                       PcgScalars* sc, int* status, double* node_dot) {
+                                                       PcgScalars* sc, int* status, double* node_dot,
+                                                       int keep, int cta_only) {
   using V = typename Vec4<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
-  if (((volatile PcgScalars*)sc)->done) return;
+  if (skip_launch(sc, cta_only)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -213,11 +153,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
   __syncthreads();
   Acc<T> v[1];
   const int t0 = blockIdx.x, G = gridDim.x;
+  uint64_t pol_last = 0, pol_first = 0;
+  if (threadIdx.x == 0 && keep >= 0) {
+    pol_last = l2_policy_evict_last();
+    pol_first = l2_policy_evict_first();
+  }
   auto issue = [&](int t, int stage) {
     const long long o0 = blob_off[t], o1 = blob_off[t + 1];
     const unsigned bytes = (unsigned)(o1 - o0);
     mbar_expect_tx(&bars[stage], bytes);
-    bulk_copy(smem + (size_t)stage * cap, blob + o0, bytes, &bars[stage]);
+    stage_tile(smem + (size_t)stage * cap, blob + o0, bytes, &bars[stage], t, keep, pol_last, pol_first);
   };
   if (threadIdx.x == 0)
 #pragma unroll
@@ -255,9 +200,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
     }
     sc->done = 2;
     sc->fail = 5;
+    if (cta_only) {  // the single-reduction PCG's next state too (it is copied over scalars[0])
+      sc[1].done = 2;
+      sc[1].fail = 5;
+    }
   }
   // a segmented batch reduces the rows' own products per RVE instead
   if (node_dot) return;
+  if (cta_only) {  // the single-reduction PCG forms the totals in its vector kernel
+    typename Partial<T>::type bt[1];
+    block_total_acc<T, 1>(v, bt);
+    if (threadIdx.x == 0) reinterpret_cast<typename Partial<T>::type*>(partials)[blockIdx.x] = bt[0];
+    return;
+  }
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -282,12 +237,13 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
                                                           const unsigned char* __restrict__ blob, int cap,
                                                           const typename Vec4<T>::type* __restrict__ p,
                                                           typename Vec4<T>::type* __restrict__ q, double* partials,
-                                                          PcgScalars* sc, int* status, double* node_dot) {
+                                                          PcgScalars* sc, int* status, double* node_dot,
+                                                          int keep, int cta_only) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NST];
   __shared__ __align__(8) uint64_t empty[NST];
   __shared__ volatile int abort_flag;
-  if (((volatile PcgScalars*)sc)->done) return;
+  if (skip_launch(sc, cta_only)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -307,11 +263,16 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
 #pragma unroll
   for (int k = 0; k < NST; ++k) issued[k] = seen[k] = 0;
   unsigned eph = 0u;
+  uint64_t pol_last = 0, pol_first = 0;
+  if (threadIdx.x == 0 && keep >= 0) {
+    pol_last = l2_policy_evict_last();
+    pol_first = l2_policy_evict_first();
+  }
   auto issue = [&](int t, int stage) {
     const long long o0 = blob_off[t], o1 = blob_off[t + 1];
     const unsigned bytes = (unsigned)(o1 - o0);
     mbar_expect_tx(&full[stage], bytes);
-    bulk_copy(smem + (size_t)stage * cap, blob + o0, bytes, &full[stage]);
+    stage_tile(smem + (size_t)stage * cap, blob + o0, bytes, &full[stage], t, keep, pol_last, pol_first);
   };
   if (threadIdx.x == 0)
 #pragma unroll
@@ -361,9 +322,19 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
       if (issued[k] > seen[k]) mbar_wait(&full[k], (unsigned)(seen[k] & 1), kWaitLimit);
     sc->done = 2;
     sc->fail = 5;
+    if (cta_only) {
+      sc[1].done = 2;
+      sc[1].fail = 5;
+    }
   }
   // a segmented batch reduces the rows' own products per RVE instead
   if (node_dot) return;
+  if (cta_only) {  // the single-reduction PCG forms the totals in its vector kernel
+    typename Partial<T>::type bt[1];
+    block_total_acc<T, 1>(v, bt);
+    if (threadIdx.x == 0) reinterpret_cast<typename Partial<T>::type*>(partials)[blockIdx.x] = bt[0];
+    return;
+  }
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -557,6 +528,14 @@ int spmv_config_n(Context* c, Grids& g) {
   }
   g.spmv = std::max(1, std::min(c->ntiles, c->num_sms * per_sm));
   g.warp_release = c->spmv_warp_release;
+  // leading whole tiles within the bytes kept in L2
+  g.keep = -1;
+  if (c->l2_keep >= 0) {
+    const std::vector<long long>& off = std::is_same<T, float>::value ? c->h_blob_off32 : c->h_blob_off64;
+    int t = 0;
+    while (t < c->ntiles && off[t + 1] <= c->l2_keep) ++t;
+    g.keep = t;
+  }
   return TG_OK;
 }
 template <typename T>
@@ -575,7 +554,7 @@ int spmv_config(Context* c, Grids& g) {
 }
 template <typename T>
 void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc,
-                 double* node_dot = nullptr) {
+                 double* node_dot = nullptr, int cta_only = 0) {
   using V = typename Vec4<T>::type;
   const bool f32 = std::is_same<T, float>::value;
   if (g.sym) {
@@ -585,7 +564,7 @@ void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* par
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);
-#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot
+#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot, g.keep, cta_only
   if (g.warp_release) {
     if (g.stages == 3)
       pcg_spmv_wr_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
@@ -677,19 +656,13 @@ int ensure_vectors(Context* c, int precision) {
     c->pcg_graph = nullptr;
   }
   c->pcg_graph_key = -1;
+  cg_free(c);  // its captured chunk names the old vectors
   return TG_OK;
 }
 
 template <typename T>
-int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
-            double* rel_res) {
+int start_t(Context* c, const double4_32a* d_rhs, const T* minv, double rel_tol, int max_it) {
   using V = typename Vec4<T>::type;
-  const int precision = std::is_same<T, float>::value ? TG_MIXED : TG_FP64;
-  int s = ensure_vectors<T>(c, precision);
-  if (s) return s;
-  const T* minv_base = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
-  const T* minv = minv_base + (precond == TG_PRECOND_BLOCK_JACOBI ? (long long)c->nnd * 9 : 0);
-  const int key = precision * 2 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0);
   const Grids g = grids(c);
   pcg_scale_kernel<T><<<g.vec, 256, 0, c->stream>>>(c->nnd, d_rhs, c->d_mask, minv, c->d_partials, c->d_pcg);
   c->launches++;
@@ -697,7 +670,20 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
                                                   (V*)c->d_z, (V*)c->d_p, (V*)c->d_q, c->d_partials, c->d_pcg,
                                                   rel_tol, max_it);
   c->launches++;
-  if (!ok(c, cudaGetLastError(), "pcg_init_kernel")) return TG_ERR_CUDA;
+  return ok(c, cudaGetLastError(), "pcg_init_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+template <typename T>
+int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
+            double* rel_res) {
+  const int precision = std::is_same<T, float>::value ? TG_MIXED : TG_FP64;
+  int s = ensure_vectors<T>(c, precision);
+  if (s) return s;
+  const T* minv_base = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
+  const T* minv = minv_base + (precond == TG_PRECOND_BLOCK_JACOBI ? (long long)c->nnd * 9 : 0);
+  const int key = precision * 2 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0);
+  s = start_t<T>(c, d_rhs, minv, rel_tol, max_it);
+  if (s) return s;
   if (c->pcg_graph_key != key || !c->pcg_graph) {
     s = capture_chunk<T>(c, minv);
     if (s) return s;
@@ -723,7 +709,17 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
     }
   }
   if (!ok(c, cudaStreamSynchronize(c->stream), "pcg sync")) return TG_ERR_CUDA;
-  const PcgScalars& h = c->h_pcg[last];
+  return pcg_finish(c, c->h_pcg[last], iters, rel_res);
+}
+
+}  // namespace
+
+int pcg_start(Context* c, int precision, const double4_32a* d_rhs, const void* minv, double rel_tol, int max_it) {
+  if (precision == TG_MIXED) return start_t<float>(c, d_rhs, (const float*)minv, rel_tol, max_it);
+  return start_t<double>(c, d_rhs, (const double*)minv, rel_tol, max_it);
+}
+
+int pcg_finish(Context* c, const PcgScalars& h, int* iters, double* rel_res) {
   if (iters) *iters = h.iters;
   if (rel_res) *rel_res = h.rr0 > 0 ? std::sqrt(h.rr / h.rr0) : 0.0;
   c->have_du = true;
@@ -739,6 +735,8 @@ int solve_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, in
   c->err = "PCG iteration limit reached";
   return TG_ERR_NOT_CONVERGED;
 }
+
+namespace {
 
 // rhs = R - K v on the node-block matrix (prescribed rows are zero in K and
 // in R), accumulated in FP64 whatever the matrix precision
@@ -990,19 +988,22 @@ int spmv_plan(Context* c, int precision, SpmvPlan& P) {
 }
 
 void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void* q, double* partials, PcgScalars* sc,
-              double* node_dot) {
+              double* node_dot, int cta_only) {
   if (precision == TG_MIXED)
-    launch_spmv<float>(c, P, p, q, partials, sc, node_dot);
+    launch_spmv<float>(c, P, p, q, partials, sc, node_dot, cta_only);
   else
-    launch_spmv<double>(c, P, p, q, partials, sc, node_dot);
+    launch_spmv<double>(c, P, p, q, partials, sc, node_dot, cta_only);
 }
 
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
               double* rel_res) {
   // a batch of RVEs: one Krylov solve per RVE over the shared matrix stream
   if (c->nseg > 0 && c->seg_pcg_mode) return pcg_solve_segmented(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
-  if (c->tangent_precision == TG_MIXED) return solve_t<float>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
-  if (c->tangent_precision == TG_FP64) return solve_t<double>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
+  const int prec = c->tangent_precision;
+  if ((prec == TG_MIXED || prec == TG_FP64) && c->pcg_form == 1 && !sym_active(c))
+    return pcg_solve_cg(c, prec, d_rhs, rel_tol, max_it, precond, iters, rel_res);
+  if (prec == TG_MIXED) return solve_t<float>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
+  if (prec == TG_FP64) return solve_t<double>(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
   c->err = "tg_pcg_solve: no tangent formed";
   return TG_ERR_ARG;
 }

@@ -96,6 +96,51 @@ __device__ __forceinline__ void block_total(Acc<T> (&v)[NV], double (&out)[NV]) 
   __syncthreads();
 }
 
+// CTA partial of a reduction as kept between kernels, in one 8-byte slot: a
+// compensated FP32 pair (hi, lo) in the FP32 form -- summed across CTAs with
+// error-free FP32 transformations, since GB300 issues FP64 at a small
+// fraction of the FP32 rate and every CTA of a kernel may repeat the sum --
+// and an FP64 value in the FP64 form.
+template <typename T> struct Partial;
+template <> struct Partial<float> { using type = float2; };
+template <> struct Partial<double> { using type = double; };
+
+__device__ __forceinline__ float2 to_partial(const Acc<float>& a) { return make_float2(a.hi, a.lo); }
+__device__ __forceinline__ double to_partial(const Acc<double>& a) { return a.s; }
+__device__ __forceinline__ void acc_merge(Acc<float>& a, float2 p) { a.merge(p.x, p.y); }
+__device__ __forceinline__ void acc_merge(Acc<double>& a, double p) { a.add(p); }
+__device__ __forceinline__ double partial_value(float2 p) { return (double)p.x + (double)p.y; }
+__device__ __forceinline__ double partial_value(double p) { return p; }
+
+// Block total of NV accumulators kept in the accumulator's own arithmetic
+// (no FP64 in the FP32 form), fixed order, on thread 0.
+template <typename T, int NV>
+__device__ __forceinline__ void block_total_acc(Acc<T> (&v)[NV], typename Partial<T>::type (&out)[NV]) {
+  using P = typename Partial<T>::type;
+  __shared__ P shp[NV][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k].shfl_merge(o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) shp[k][w] = to_partial(v[k]);
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      Acc<T> a;
+      if (lane < nw) acc_merge(a, shp[k][lane]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a.shfl_merge(o);
+      out[k] = to_partial(a);
+    }
+  }
+  __syncthreads();
+}
+
 // Last-block reduction of per-block partials (partials[k*gridDim + b]) in
 // FP64 and a fixed order; true in the last block, totals on thread 0.
 template <typename T, int NV>
@@ -163,6 +208,38 @@ __device__ __forceinline__ void bulk_copy(void* dst_smem, const void* src, unsig
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// L2 eviction priorities of the streamed matrix.  The matrix is larger than
+// the L2 and is read once per product, so most of it is streamed with
+// evict_first (it never displaces the PCG vectors, which every kernel of an
+// iteration reads and writes); a leading part of it may be kept with
+// evict_last, so that part is served from the L2 on every later product.
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void bulk_copy_hint(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar,
+                                               uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          smem_addr(dst_smem)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+      : "memory");
+}
+// One staged tile: a plain bulk copy (keep < 0), or with the tile's L2
+// priority (tiles below `keep` evict_last, the rest evict_first).
+__device__ __forceinline__ void stage_tile(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar, int t,
+                                           int keep, uint64_t pol_last, uint64_t pol_first) {
+  if (keep < 0)
+    bulk_copy(dst_smem, src, bytes, bar);
+  else
+    bulk_copy_hint(dst_smem, src, bytes, bar, t < keep ? pol_last : pol_first);
+}
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
@@ -170,6 +247,83 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 constexpr int kWaitLimit = 1 << 18;  // polls before a staged tile is declared lost
+
+// The rows of one staged tile handled by this warp: 8 lanes per row, 4 rows
+// per warp at a time, each lane over every 8th block; q = A p written for the
+// rows, p.q accumulated into v.
+template <typename T>
+__device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
+                                               const typename Vec4<T>::type* __restrict__ p,
+                                               typename Vec4<T>::type* __restrict__ q, Acc<T>& v0,
+                                               double* __restrict__ node_dot) {
+  using V = typename Vec4<T>::type;
+  const int sub = lane & 7;
+  Acc<T>* v = &v0;
+  const int* hdr = reinterpret_cast<const int*>(base);
+  const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
+  const int* rp = hdr + 4;
+  const int* cl = rp + ceil4(nrows + 1);
+  const T* pl = reinterpret_cast<const T*>(cl + ceil4(nb));
+  for (int li = warp * 4 + (lane >> 3); li - (lane >> 3) < nrows; li += nwarps * 4) {
+    const bool live = li < nrows;
+    const int I = r0 + li;
+    V pi;
+    if (live && sub == 0) pi = p[I];
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    const int e0 = live ? rp[li] : 0;
+    const int e1 = live ? rp[li + 1] : 0;
+    // the first 4 blocks of this lane (32 per row, a hex8 row has at most
+    // 27): all column indices, then all neighbour gathers, then the
+    // arithmetic, so the L2 round trips of one lane overlap instead of
+    // chaining
+    {
+      int Jk[4];
+      V pk[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = e0 + sub + 8 * u;
+        Jk[u] = j < e1 ? cl[j] : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (Jk[u] >= 0) pk[u] = p[Jk[u]];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (Jk[u] >= 0) {
+          const T* vv = pl + e0 + sub + 8 * u;
+          a0 += vv[0 * ps] * pk[u].x + vv[1 * ps] * pk[u].y + vv[2 * ps] * pk[u].z;
+          a1 += vv[3 * ps] * pk[u].x + vv[4 * ps] * pk[u].y + vv[5 * ps] * pk[u].z;
+          a2 += vv[6 * ps] * pk[u].x + vv[7 * ps] * pk[u].y + vv[8 * ps] * pk[u].z;
+        }
+    }
+    for (int j = e0 + sub + 32; j < e1; j += 8) {
+      const V pj = p[cl[j]];
+      const T* vv = pl + j;
+      a0 += vv[0 * ps] * pj.x + vv[1 * ps] * pj.y + vv[2 * ps] * pj.z;
+      a1 += vv[3 * ps] * pj.x + vv[4 * ps] * pj.y + vv[5 * ps] * pj.z;
+      a2 += vv[6 * ps] * pj.x + vv[7 * ps] * pj.y + vv[8 * ps] * pj.z;
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (live && sub == 0) {
+      q[I] = mk<V, T>(a0, a1, a2);
+      v[0].add_prod(pi.x, a0);
+      v[0].add_prod(pi.y, a1);
+      v[0].add_prod(pi.z, a2);
+      if (node_dot) {  // the row's own p.q (per-RVE reductions of a segmented batch)
+        Acc<T> d;
+        d.add_prod(pi.x, a0);
+        d.add_prod(pi.y, a1);
+        d.add_prod(pi.z, a2);
+        node_dot[I] = d.value();
+      }
+    }
+  }
+}
 
 // ---- grid-wide barrier of a cooperative launch ---------------------------
 constexpr int kBarrierLimit = 1 << 24;  // polls before a grid barrier is declared broken

@@ -131,6 +131,7 @@ struct SpmvPlan {
   size_t spmv_smem = 0;
   int stages = 2;
   int warp_release = 0;
+  int keep = -1;  // matrix tiles streamed with L2 priorities: -1 none, else tiles [0, keep) evict_last
   bool sym = false;
   SymLaunch sl;
 };
@@ -179,6 +180,7 @@ struct Context {
   int spmv_tile_blocks = kTileBlocks;
   int spmv_stages = 2;
   int spmv_warp_release = 0;   // 1: per-warp stage release instead of a CTA barrier per tile
+  long long l2_keep = 16ll << 20;  // matrix bytes the product keeps in L2 (<0: no L2 priorities)
   int tangent_epb = 8;         // elements per CTA of the tangent kernel (2, 4, 8)
   int sym_mode = 0;            // 1-3: the single-vector product streams the symmetric format (single meshes)
   int seg_pcg_mode = 1;        // 1: a segmented batch runs one Krylov solve per RVE (segpcg.cu)
@@ -237,6 +239,11 @@ struct Context {
   void* d_z = nullptr;
   void* d_p = nullptr;   // search direction (updated in place by the vector update)
   void* d_q = nullptr;
+  void* d_cg_s = nullptr;  // s = A p by recurrence (single-reduction PCG), in the solve's precision
+  int cg_s_precision = -1;
+  int pcg_form = 1;        // 1: single-vector solves on full storage run the single-reduction PCG (pcg_cg.cu)
+  cudaGraphExec_t cg_graph = nullptr;  // captured chunk of the single-reduction PCG
+  int cg_graph_key = -1;
   int pcg_vec_precision = -1;
   PcgScalars* d_pcg = nullptr;
   double* d_partials = nullptr;  // reduction partials
@@ -309,6 +316,7 @@ void build_block_pattern(int nnd, int nel, const int* conn, std::vector<int>& ro
 void build_contrib_map(int nnd, int nel, const int* conn, const std::vector<int>& rowptr,
                        const std::vector<int>& col, std::vector<int>& cptr, std::vector<int>& contrib);
 int build_tiles(Context* c, int tile_blocks);
+void drop_graphs(Context* c);  // captured Krylov iterations (their launches bake in the product's shape)
 int ensure_blob(Context* c, int precision);
 
 // blob geometry shared by host and device code
@@ -333,12 +341,13 @@ int pcg_solve_segmented(Context* c, const double4_32a* d_rhs, double rel_tol, in
                         double* rel_res);
 void seg_free(Context* c);  // graph and bookkeeping (buffers go back with the mesh)
 int pcg_vectors(Context* c, int precision);  // x r z p q of the solve's precision (krylov.cu)
-// the single-vector product for other solvers (segpcg.cu): plan once per
-// mesh/precision, launch on (p, q); node_dot (nnd, may be NULL) receives
-// each row's p.q
+// the single-vector product for other solvers (segpcg.cu, pcg_cg.cu): plan
+// once per mesh/precision, launch on (p, q); node_dot (nnd, may be NULL)
+// receives each row's p.q; cta_only: each CTA writes its partial p.q to
+// partials[CTA] and no total is formed
 int spmv_plan(Context* c, int precision, SpmvPlan& P);
 void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void* q, double* partials, PcgScalars* sc,
-              double* node_dot);
+              double* node_dot, int cta_only = 0);
 void sym_free(Context* c);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----
@@ -366,6 +375,13 @@ int launch_apply_update(Context* c);
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
               double* rel_res);
 int time_pcg_kernel(Context* c, int which, int reps, double* ms);
+// scale + init launches of a single-vector PCG, and the result of its final scalars (krylov.cu)
+int pcg_start(Context* c, int precision, const double4_32a* d_rhs, const void* minv, double rel_tol, int max_it);
+int pcg_finish(Context* c, const PcgScalars& h, int* iters, double* rel_res);
+// single-reduction PCG (Chronopoulos-Gear) on full storage (pcg_cg.cu)
+int pcg_solve_cg(Context* c, int precision, const double4_32a* d_rhs, double rel_tol, int max_it, int precond,
+                 int* iters, double* rel_res);
+void cg_free(Context* c);  // the captured iterations
 // PCG with every work vector, partial sum and scalar in caller scratch
 constexpr size_t kScratchScalarBytes = 256;
 constexpr size_t kScratchPartialBytes = 32768;

@@ -91,6 +91,8 @@ _SIGS = {
     "tg_state_load": (ctypes.c_int, [_vp, _vp, ctypes.c_longlong]),
     "tg_nodal_material_output": (ctypes.c_int, [_vp, _dp]),
     "tg_spmv_release": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tg_spmv_l2_keep": (ctypes.c_int, [_vp, ctypes.c_longlong]),
+    "tg_pcg_form": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
     "tg_segment_residual_norms": (ctypes.c_int, [_vp, _dp]),
@@ -475,6 +477,18 @@ class Context:
 
     def spmv_release(self, per_warp):
         self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")
+
+    def pcg_form(self, form):
+        """Recurrences of the single-vector PCG: 1 single-reduction
+        (default), 0 textbook."""
+        self._chk(self.L.tg_pcg_form(self.h, int(form)), "tg_pcg_form")
+        self.form = int(form)
+
+    def spmv_l2_keep(self, nbytes):
+        """Matrix bytes the streamed product keeps in the L2 (evict_last;
+        the rest streams evict_first); -1 plain copies."""
+        self._chk(self.L.tg_spmv_l2_keep(self.h, int(nbytes)), "tg_spmv_l2_keep")
+        self.l2_keep = int(nbytes)
 
     def spmv_symmetric(self, on, tile_blocks=0):
         """Symmetric stream format of the single-vector product (on = 1, 2, 3:

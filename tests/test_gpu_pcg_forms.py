@@ -1,0 +1,111 @@
+"""The two recurrence forms of the single-vector PCG and the L2 priorities of
+the streamed matrix, through the C ABI.
+
+tg_pcg_form selects the textbook recurrences (form 0: product with a
+last-block reduction, vector update with a grid barrier) or the single-
+reduction recurrences of Chronopoulos & Gear (form 1, the default: the
+product writes CTA partials, every CTA of the vector kernel forms the
+iteration's scalars from them).  Both solve the same (block-)Jacobi CG
+system, so they reach the same solution to the solve's tolerance; each is
+bitwise repeatable.  tg_spmv_l2_keep only changes cache priorities of the
+bulk copies, so every setting gives bitwise the same iterates.
+"""
+import numpy as np
+import pytest
+
+from tahoe_gb300 import lib
+from tahoe_gb300.meshgen import BoxMesh
+from tahoe_gb300.model import SolidModel
+
+pytestmark = pytest.mark.gpu
+
+SIMO = {"kind": "fs_simo", "mu": 1.0, "kappa": 10.0}
+
+
+def _model(n=12):
+    mesh = BoxMesh(n, n, n, jitter=0.2, seed=3)
+    m = SolidModel(mesh.X, mesh.conn, "total_lagrangian", SIMO)
+    for node in mesh.face_nodes(2, 0):
+        for d in range(3):
+            m.add_kbc(node, d)
+    for node in mesh.face_nodes(2, 1):
+        m.add_kbc(node, 2, -0.02, True)
+    m.set_schedule([(0.0, 1.0)])
+    m.setup()
+    return m
+
+
+def _system(m, precision, precond):
+    m.apply_step(1.0, (precision, precond, 1e-8))
+    c = m.ctx
+    c.set_iteration(-1)
+    R, _ = c.residual()
+    c.tangent(precision)
+    return c, R
+
+
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+@pytest.mark.parametrize("precond", [lib.PRECOND_JACOBI, lib.PRECOND_BLOCK_JACOBI])
+def test_forms_reach_the_same_solution(precision, precond):
+    m = _model()
+    c, R = _system(m, precision, precond)
+    tol = 1e-7 if precision == lib.MIXED else 1e-10
+    sol = {}
+    for form in (0, 1):
+        c.pcg_form(form)
+        du, its, rr, rc = c.pcg(R, rel_tol=tol, max_it=20000, precond=precond)
+        assert rc == 0, form
+        assert rr <= tol, (form, rr)
+        sol[form] = (du, its)
+    scale = np.abs(sol[0][0]).max()
+    # both are within the tolerance of the exact solution of the same system
+    bound = 2e-4 if precision == lib.MIXED else 1e-6
+    assert np.abs(sol[1][0] - sol[0][0]).max() <= bound * scale
+    # the same Krylov method: iteration counts within a few percent
+    assert abs(sol[1][1] - sol[0][1]) <= max(3, 0.05 * sol[0][1])
+
+
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+def test_single_reduction_form_is_bitwise_repeatable(precision):
+    m = _model()
+    c, R = _system(m, precision, lib.PRECOND_JACOBI)
+    c.pcg_form(1)
+    a = c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_JACOBI)
+    b = c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_JACOBI)
+    assert a[3] == 0 and b[3] == 0
+    assert a[1] == b[1]
+    assert np.array_equal(a[0], b[0])
+
+
+def test_l2_priorities_leave_the_iterates_bitwise_unchanged():
+    m = _model(16)
+    c, R = _system(m, lib.MIXED, lib.PRECOND_JACOBI)
+    nbytes = c.block_nnz * 40
+    ref = None
+    for form in (1, 0):
+        c.pcg_form(form)
+        ref = None
+        for keep in (-1, 0, 1 << 20, nbytes // 3, 4 * nbytes):
+            c.spmv_l2_keep(keep)
+            du, its, rr, rc = c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_JACOBI)
+            assert rc == 0
+            if ref is None:
+                ref = (du, its)
+            assert its == ref[1], (form, keep)
+            assert np.array_equal(du, ref[0]), (form, keep)
+    c.spmv_l2_keep(16 << 20)
+
+
+def test_single_reduction_form_converges_within_the_first_chunk():
+    # a loose tolerance ends the solve inside the first 16-iteration replay:
+    # the scalars handed from one vector kernel to the next carry the flag
+    m = _model(6)
+    c, R = _system(m, lib.MIXED, lib.PRECOND_BLOCK_JACOBI)
+    c.pcg_form(1)
+    du, its, rr, rc = c.pcg(R, rel_tol=0.3, max_it=20000, precond=lib.PRECOND_BLOCK_JACOBI)
+    assert rc == 0
+    assert 1 <= its < 16
+    assert rr <= 0.3
+    c.pcg_form(0)
+    du0, its0, rr0, rc0 = c.pcg(R, rel_tol=0.3, max_it=20000, precond=lib.PRECOND_BLOCK_JACOBI)
+    assert rc0 == 0 and abs(its0 - its) <= 1

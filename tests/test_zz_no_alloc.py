@@ -3,9 +3,10 @@
 tg_pcg_solve_noalloc serves callers that cannot allocate device memory: hosts
 that reserve all device memory themselves up front, or whose request path must
 not enter the CUDA allocator.  It keeps its work vectors in a fixed static
-device array (meshes up to 32,768 nodes).  This test calls it through the C ABI
-on caller-owned device buffers, twice in a row, and compares each result with
-tg_pcg_solve on the same tangent and right-hand side.  The file name sorts
+device array (meshes up to 32,768 nodes) and runs the two-kernel form of the
+PCG.  This test calls it through the C ABI on caller-owned device buffers,
+twice in a row, and compares each result with tg_pcg_solve in the same form
+on the same tangent and right-hand side.  The file name sorts
 last so a run that stops at the first failure has run every other test.
 """
 import numpy as np
@@ -43,6 +44,8 @@ def test_noalloc_solve_matches_allocating_solve_twice(precision, precond):
     c.set_iteration(-1)
     R, _ = c.residual()
     c.tangent(precision)
+    # the scratch solve runs the two-kernel recurrences: compare like with like
+    c.pcg_form(0)
     du_ref, its_ref, rr_ref, rc = c.pcg(R, rel_tol=1e-8, max_it=5000, precond=precond)
     assert rc == 0
     d_rhs = torch.tensor(R, dtype=torch.float64, device="cuda:0")
