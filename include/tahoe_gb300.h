@@ -378,12 +378,16 @@ int tg_spmv_release(tg_context* ctx, int per_warp);
  * Gear -- per iteration one product kernel (w = A u, CTA partials of u.w) and
  * one vector kernel whose CTAs each form the iteration's scalars from the
  * partials and run one fused pass over p, s, x, r, u; no grid barrier and no
- * atomic in either kernel.  form = 0: the textbook recurrences (product with
- * a last-block reduction; vector update with a grid barrier between its two
- * passes).  Both solve the same (block-)Jacobi CG system to the same
- * tolerance; the iterates differ by rounding.  The symmetric format,
- * segmented batches and the no-allocation entry point use their own
- * kernels. */
+ * atomic in either kernel; each kernel launches with a programmatic
+ * dependency on the one before, so its independent prologue (the product's
+ * first matrix tiles, the vector kernel's node vectors) overlaps the
+ * previous kernel's last CTAs.  form = 2: the same without programmatic
+ * dependencies.  form = 0: the textbook recurrences (product with a
+ * last-block reduction; vector update with a grid barrier between its two
+ * passes).  All solve the same (block-)Jacobi CG system to the same
+ * tolerance; forms 1 and 2 take bitwise the same iterates, form 0 differs
+ * from them by rounding.  The symmetric format, segmented batches and the
+ * no-allocation entry point use their own kernels. */
 int tg_pcg_form(tg_context* ctx, int form);
 /* L2 priorities of the streamed matrix.  bytes >= 0: the leading whole
  * tiles within `bytes` of the matrix storage are copied with evict_last

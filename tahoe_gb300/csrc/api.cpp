@@ -331,30 +331,76 @@ int tg_mesh_upload(tg_context* c, int nnd, const double* coords, int nel, const 
 }  // extern "C"
 
 namespace tg {
-// Row tiles of the streamed SpMV: consecutive rows holding at most
-// tile_blocks block nonzeros (a longer row is a tile of its own), and the
-// byte offsets of every tile in the tile-contiguous matrix storage of each
-// precision.  Any existing matrix storage is dropped (its layout changes).
+// Row tiles of the streamed SpMV and the byte offsets of every tile in the
+// tile-contiguous matrix storage of each precision.  Any existing matrix
+// storage is dropped (its layout changes).
+//
+// The persistent product grid of G CTAs takes tiles t, t + G, ...: tiles
+// cut greedily (consecutive rows holding at most tile_blocks block
+// nonzeros) leave some CTAs one tile more than others, and the whole
+// product waits for them.  So the rows are cut into exactly k G tiles of
+// equal block count (k the smallest count keeping tiles within
+// tile_blocks, cut at the row boundary nearest each share), which gives
+// every CTA k tiles of the same size -- unless that tiling no longer fits
+// G CTAs (a larger largest tile) or the mesh has too few rows, where the
+// greedy tiles stay.
+namespace {
+struct TileSet {
+  std::vector<int> start;  // first row of each tile, then nnd
+  long long cap32 = 0, cap64 = 0;
+};
+TileSet tile_set(const Context* c, const std::vector<int>& start) {
+  TileSet ts;
+  ts.start = start;
+  for (size_t t = 0; t + 1 < start.size(); ++t) {
+    const int nrows = start[t + 1] - start[t];
+    const int nb = c->h_rowptr[start[t + 1]] - c->h_rowptr[start[t]];
+    ts.cap32 = std::max(ts.cap32, blob_tile_bytes(nrows, nb, 4));
+    ts.cap64 = std::max(ts.cap64, blob_tile_bytes(nrows, nb, 8));
+  }
+  return ts;
+}
+}  // namespace
+
 int build_tiles(Context* c, int tile_blocks) {
   if (ensure_host_mesh(c)) return TG_ERR_CUDA;
-  std::vector<int> tiles(1, 0);
+  std::vector<int> greedy(1, 0);
   for (int r = 0; r < c->nnd; ++r)
-    if (r > tiles.back() && c->h_rowptr[r + 1] - c->h_rowptr[tiles.back()] > tile_blocks) tiles.push_back(r);
-  tiles.push_back(c->nnd);
+    if (r > greedy.back() && c->h_rowptr[r + 1] - c->h_rowptr[greedy.back()] > tile_blocks) greedy.push_back(r);
+  greedy.push_back(c->nnd);
+  TileSet ts = tile_set(c, greedy);
+  const long long nnzb = c->h_rowptr[c->nnd];
+  const int G = spmv_grid_for(c, ts.cap32);
+  if (G > 0 && nnzb > 0) {
+    const long long k = (nnzb + (long long)G * tile_blocks - 1) / ((long long)G * tile_blocks);
+    const long long parts = k * G;
+    if (parts <= c->nnd) {
+      std::vector<int> bal(1, 0);
+      for (long long j = 1; j < parts; ++j) {
+        const long long target = (j * nnzb + parts / 2) / parts;
+        int r = (int)(std::lower_bound(c->h_rowptr.begin(), c->h_rowptr.begin() + c->nnd + 1, (int)target) -
+                      c->h_rowptr.begin());
+        if (r > 0 && target - c->h_rowptr[r - 1] < c->h_rowptr[r] - target) --r;
+        if (r > bal.back() && r < c->nnd) bal.push_back(r);
+      }
+      bal.push_back(c->nnd);
+      TileSet tb = tile_set(c, bal);
+      if ((long long)bal.size() - 1 == parts && spmv_grid_for(c, tb.cap32) == G) ts = tb;
+    }
+  }
+  const std::vector<int>& tiles = ts.start;
   const int nt = (int)tiles.size() - 1;
   std::vector<int> row_tile(c->nnd);
   c->h_blob_off32.assign(nt + 1, 0);
   c->h_blob_off64.assign(nt + 1, 0);
-  c->blob_cap32 = c->blob_cap64 = 0;
+  c->blob_cap32 = ts.cap32;
+  c->blob_cap64 = ts.cap64;
   for (int t = 0; t < nt; ++t) {
     const int nrows = tiles[t + 1] - tiles[t];
     const int nb = c->h_rowptr[tiles[t + 1]] - c->h_rowptr[tiles[t]];
     for (int r = tiles[t]; r < tiles[t + 1]; ++r) row_tile[r] = t;
-    const long long b32 = blob_tile_bytes(nrows, nb, 4), b64 = blob_tile_bytes(nrows, nb, 8);
-    c->h_blob_off32[t + 1] = c->h_blob_off32[t] + b32;
-    c->h_blob_off64[t + 1] = c->h_blob_off64[t] + b64;
-    c->blob_cap32 = std::max(c->blob_cap32, b32);
-    c->blob_cap64 = std::max(c->blob_cap64, b64);
+    c->h_blob_off32[t + 1] = c->h_blob_off32[t] + blob_tile_bytes(nrows, nb, 4);
+    c->h_blob_off64[t + 1] = c->h_blob_off64[t] + blob_tile_bytes(nrows, nb, 8);
   }
   for (void** p : {(void**)&c->d_tile_row, (void**)&c->d_row_tile, (void**)&c->d_blob_off32,
                    (void**)&c->d_blob_off64, (void**)&c->d_blob32, (void**)&c->d_blob64}) {
@@ -426,8 +472,13 @@ int tg_spmv_release(tg_context* c, int per_warp) {
 }
 
 int tg_pcg_form(tg_context* c, int form) {
-  if (!c || (form != 0 && form != 1)) return TG_ERR_ARG;
-  c->pcg_form = form;
+  if (!c || form < 0 || form > 2) return TG_ERR_ARG;
+  c->pcg_form = form == 0 ? 0 : 1;
+  const int pdl = form == 1 ? 1 : 0;
+  if (pdl != c->cg_pdl) {
+    c->cg_pdl = pdl;
+    drop_graphs(c);  // the captured chunk bakes in its launch dependencies
+  }
   return TG_OK;
 }
 

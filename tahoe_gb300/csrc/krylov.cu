@@ -108,22 +108,6 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(int nnd, const double4_32
 }
 
 
-// Whether a product launch has nothing to do (the solve is over), decided
-// by one thread and the same for every thread of the CTA.  For the
-// single-reduction PCG (cta_only) block 0 first hands the state the last
-// vector kernel wrote (scalars[1]) over to the one the next vector kernel
-// reads (scalars[0]); the flag is read from scalars[1], which no kernel
-// rewrites while a product runs except on a stage timeout.
-__device__ __forceinline__ bool skip_launch(PcgScalars* sc, int cta_only) {
-  __shared__ int skip;
-  if (threadIdx.x == 0) {
-    if (cta_only && blockIdx.x == 0) sc[0] = sc[1];
-    skip = ((volatile PcgScalars*)(cta_only ? sc + 1 : sc))->done != 0;
-  }
-  __syncthreads();
-  return skip != 0;
-}
-
 // q = A p on a persistent grid.  Each CTA streams its row tiles through a ring of NST
 // shared-memory stages: one bulk copy per tile (the tile-contiguous storage
 // makes a tile one range), completing on the stage's mbarrier, is issued
@@ -137,12 +121,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
                                                        const typename Vec4<T>::type* __restrict__ p,
                                                        typename Vec4<T>::type* __restrict__ q, double* partials,
                                                        PcgScalars* sc, int* status, double* node_dot,
-                                                       int keep, int cta_only) {
+                                                       int keep) {
   using V = typename Vec4<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int abort_flag;
-  if (skip_launch(sc, cta_only)) return;
+  if (skip_launch(sc, 0)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -200,19 +184,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_spmv_kernel(i
     }
     sc->done = 2;
     sc->fail = 5;
-    if (cta_only) {  // the single-reduction PCG's next state too (it is copied over scalars[0])
-      sc[1].done = 2;
-      sc[1].fail = 5;
-    }
   }
   // a segmented batch reduces the rows' own products per RVE instead
   if (node_dot) return;
-  if (cta_only) {  // the single-reduction PCG forms the totals in its vector kernel
-    typename Partial<T>::type bt[1];
-    block_total_acc<T, 1>(v, bt);
-    if (threadIdx.x == 0) reinterpret_cast<typename Partial<T>::type*>(partials)[blockIdx.x] = bt[0];
-    return;
-  }
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -238,12 +212,12 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
                                                           const typename Vec4<T>::type* __restrict__ p,
                                                           typename Vec4<T>::type* __restrict__ q, double* partials,
                                                           PcgScalars* sc, int* status, double* node_dot,
-                                                          int keep, int cta_only) {
+                                                          int keep) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NST];
   __shared__ __align__(8) uint64_t empty[NST];
   __shared__ volatile int abort_flag;
-  if (skip_launch(sc, cta_only)) return;
+  if (skip_launch(sc, 0)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -322,19 +296,9 @@ __global__ void __launch_bounds__(256) pcg_spmv_wr_kernel(int ntiles, const long
       if (issued[k] > seen[k]) mbar_wait(&full[k], (unsigned)(seen[k] & 1), kWaitLimit);
     sc->done = 2;
     sc->fail = 5;
-    if (cta_only) {
-      sc[1].done = 2;
-      sc[1].fail = 5;
-    }
   }
   // a segmented batch reduces the rows' own products per RVE instead
   if (node_dot) return;
-  if (cta_only) {  // the single-reduction PCG forms the totals in its vector kernel
-    typename Partial<T>::type bt[1];
-    block_total_acc<T, 1>(v, bt);
-    if (threadIdx.x == 0) reinterpret_cast<typename Partial<T>::type*>(partials)[blockIdx.x] = bt[0];
-    return;
-  }
   double tot[1];
   if (last_block_total<T, 1>(v, partials, &sc->count_a, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -554,7 +518,7 @@ int spmv_config(Context* c, Grids& g) {
 }
 template <typename T>
 void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* partials, PcgScalars* sc,
-                 double* node_dot = nullptr, int cta_only = 0) {
+                 double* node_dot = nullptr) {
   using V = typename Vec4<T>::type;
   const bool f32 = std::is_same<T, float>::value;
   if (g.sym) {
@@ -564,7 +528,7 @@ void launch_spmv(Context* c, const Grids& g, const void* p, void* q, double* par
   const long long* off = f32 ? c->d_blob_off32 : c->d_blob_off64;
   const unsigned char* blob = f32 ? c->d_blob32 : c->d_blob64;
   const int cap = blob_cap<T>(c);
-#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot, g.keep, cta_only
+#define TG_SPMV_ARGS c->ntiles, off, blob, cap, (const V*)p, (V*)q, partials, sc, c->d_status, node_dot, g.keep
   if (g.warp_release) {
     if (g.stages == 3)
       pcg_spmv_wr_kernel<T, 3><<<g.spmv, 256, g.spmv_smem, c->stream>>>(TG_SPMV_ARGS);
@@ -982,17 +946,35 @@ int pcg_vectors(Context* c, int precision) {
   return precision == TG_MIXED ? ensure_vectors<float>(c, precision) : ensure_vectors<double>(c, precision);
 }
 
+int spmv_grid_for(Context* c, long long cap32) {
+  const size_t cap = (size_t)((cap32 + 127) / 128 * 128);
+  const int nst = c->spmv_stages == 3 ? 3 : 2;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess) return 0;
+  if ((size_t)nst * cap + 1024 > (size_t)optin) return 0;
+  auto kern = c->spmv_warp_release ? (nst == 3 ? pcg_spmv_wr_kernel<float, 3> : pcg_spmv_wr_kernel<float, 2>)
+                                   : (nst == 3 ? pcg_spmv_kernel<float, 3> : pcg_spmv_kernel<float, 2>);
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes) !=
+          cudaSuccess)
+    return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, (size_t)nst * cap) != cudaSuccess) return 0;
+  return c->num_sms * per_sm;
+}
+
 int spmv_plan(Context* c, int precision, SpmvPlan& P) {
   P = grids(c);
   return precision == TG_MIXED ? spmv_config<float>(c, P) : spmv_config<double>(c, P);
 }
 
 void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void* q, double* partials, PcgScalars* sc,
-              double* node_dot, int cta_only) {
+              double* node_dot) {
   if (precision == TG_MIXED)
-    launch_spmv<float>(c, P, p, q, partials, sc, node_dot, cta_only);
+    launch_spmv<float>(c, P, p, q, partials, sc, node_dot);
   else
-    launch_spmv<double>(c, P, p, q, partials, sc, node_dot, cta_only);
+    launch_spmv<double>(c, P, p, q, partials, sc, node_dot);
 }
 
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,

@@ -325,6 +325,22 @@ __device__ __forceinline__ void spmv_tile_rows(const unsigned char* base, int la
   }
 }
 
+// Whether a product launch has nothing to do (the solve is over), decided
+// by one thread and the same for every thread of the CTA.  For the
+// single-reduction PCG (handoff) block 0 first hands the state the last
+// vector kernel wrote (scalars[1]) over to the one the next vector kernel
+// reads (scalars[0]); the flag is read from scalars[1], which no kernel
+// rewrites while a product runs except on a stage timeout.
+__device__ __forceinline__ bool skip_launch(PcgScalars* sc, int handoff) {
+  __shared__ int skip;
+  if (threadIdx.x == 0) {
+    if (handoff && blockIdx.x == 0) sc[0] = sc[1];
+    skip = ((volatile PcgScalars*)(handoff ? sc + 1 : sc))->done != 0;
+  }
+  __syncthreads();
+  return skip != 0;
+}
+
 // ---- grid-wide barrier of a cooperative launch ---------------------------
 constexpr int kBarrierLimit = 1 << 24;  // polls before a grid barrier is declared broken
 

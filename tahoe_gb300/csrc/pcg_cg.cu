@@ -4,8 +4,7 @@
 // (J. Comput. Appl. Math. 25 (1989) 153-168), two kernels per iteration and
 // no grid-wide synchronisation inside either of them:
 //
-//   product  w = A u; each CTA writes its partial of u.w
-//            (pcg_spmv_kernel with CTA partials only)
+//   product  w = A u; each CTA (one per SM) writes its partial of u.w
 //   vector   every CTA forms delta = u.w, gamma = r.u and r.r from the CTA
 //            partials of the two kernels before it (visible through the
 //            kernel boundary), in the same fixed order in every CTA; tests
@@ -47,45 +46,162 @@ namespace tg {
 namespace {
 
 constexpr int kCgChunk = 16;       // iterations per graph replay
-constexpr int kCgThreads = 256;
-constexpr int kDeltaCap = 2048;    // product CTAs (the persistent product grid is far smaller)
 constexpr int kVecCap = 1024;      // vector-kernel CTAs
-// partials (doubles): product u.w at [0, kDeltaCap); then two buffers of
-// {r.u [kVecCap], r.r [kVecCap]}
-constexpr int kCgPartials = kDeltaCap + 4 * kVecCap;
+constexpr int kCtaCap = 1024;      // product CTAs
+// partials (8-byte slots): two buffers of the vector kernel's {r.u
+// [kVecCap], r.r [kVecCap]}, then the product's CTA partials [kCtaCap]
+constexpr int kCgPartials = 4 * kVecCap;
 
-// One node per thread per pass: with 4 (FP32) or 2 (FP64) CTAs of 256
-// threads per SM, 1024 / 512 nodes are in flight per SM, enough to cover the
-// L2 latency of the vector pass (its vectors stay L2-resident).
+// Programmatic dependent launch: a kernel lets the next one in the stream
+// launch its CTAs as its own exit (launch_dependents), and a kernel that
+// consumes the previous one's results waits for that grid's completion and
+// memory (wait; a no-op when launched without the dependency).  Each kernel
+// of the iteration does the work that does not depend on the previous one
+// first -- the product stages its first matrix tiles, the vector kernel
+// loads its nodes' vectors -- so that work overlaps the previous kernel's
+// last CTAs and the launch gap.  A kernel releases its dependents only after
+// its own wait: released earlier, the next vector kernel could start while
+// the one before the product was still writing the vectors it preloads
+// (seen on meshes small enough for all three grids to be resident at once).
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// The product: w = A u and the CTA partials of u.w on a persistent grid of
+// 256-thread CTAs (as many as fit, a few per SM).  CTA b streams tiles b,
+// b + G, ... through a ring of NST shared-memory stages filled by bulk
+// copies on mbarriers, issued NST - 1 tiles ahead; eight warps take each
+// tile's rows (8 lanes per row).  The CTA's u.w is reduced in a fixed order
+// into its partial.  Every wait is bounded; a timeout flags the solve broken
+// down in both scalar states and drains the copies in flight.  (Measured on
+// C2: four such CTAs per SM stream the matrix faster than one CTA of four
+// groups sharing the SM's tiles, and faster than tiles pulled from a global
+// counter; the spread of finishing times is per SM, not per tile count.)
+template <typename T, int NST>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
+    pcg_cg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off, const unsigned char* __restrict__ blob,
+                       int cap, int keep, const typename Vec4<T>::type* __restrict__ p,
+                       typename Vec4<T>::type* __restrict__ q, typename Partial<T>::type* __restrict__ cta_part,
+                       PcgScalars* sc, int* status) {
+  using P = typename Partial<T>::type;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[NST];
+  __shared__ int abort_flag;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NST; ++k) mbar_init(&bars[k], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  const int t0 = blockIdx.x, G = gridDim.x;
+  int issued = 0;  // positions issued (thread 0)
+  auto issue = [&](int t) {
+    const int st = issued % NST;
+    ++issued;
+    const long long o0 = blob_off[t], o1 = blob_off[t + 1];
+    const unsigned bytes = (unsigned)(o1 - o0);
+    mbar_expect_tx(&bars[st], bytes);
+    if (keep < 0)
+      bulk_copy(smem + (size_t)st * cap, blob + o0, bytes, &bars[st]);
+    else
+      bulk_copy_hint(smem + (size_t)st * cap, blob + o0, bytes, &bars[st],
+                     t < keep ? l2_policy_evict_last() : l2_policy_evict_first());
+  };
+  // the first tiles (the matrix does not depend on the last vector kernel)
+  if (threadIdx.x == 0)
+    for (int k = 0; k < NST - 1 && t0 + k * G < ntiles; ++k) issue(t0 + k * G);
+  griddep_wait();  // u and the scalars of the last vector kernel
+  griddep_launch();
+  if (skip_launch(sc, 1)) {
+    if (threadIdx.x == 0)  // the staged copies complete before the CTA leaves
+      for (int q2 = 0; q2 < issued; ++q2) mbar_wait(&bars[q2 % NST], (unsigned)((q2 / NST) & 1), kWaitLimit);
+    return;
+  }
+  Acc<T> v;
+  int it = 0;
+  bool stuck = false;
+  for (int t = t0; t < ntiles; ++it, t += G) {
+    const int s = it % NST;
+    const int tn = t + (NST - 1) * G;
+    if (threadIdx.x == 0 && tn < ntiles) {
+      fence_async_smem();  // the stage was last read through generic loads
+      issue(tn);
+    }
+    if (!mbar_wait(&bars[s], (unsigned)((it / NST) & 1), kWaitLimit)) {
+      if (lane == 0) atomicOr(&abort_flag, 1);
+    }
+    __syncthreads();
+    if (abort_flag) {
+      stuck = true;
+      break;
+    }
+    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v, nullptr);
+    __syncthreads();  // stage s is free for the copy issued next iteration
+  }
+  if (stuck && threadIdx.x == 0) {
+    // a staged tile never completed: record it, drain the copies still in
+    // flight (bounded waits) and flag the solve broken down
+    atomicOr(status, kStatusWaitTimeout);
+    for (int q2 = it; q2 < issued; ++q2) mbar_wait(&bars[q2 % NST], (unsigned)((q2 / NST) & 1), kWaitLimit);
+    sc[0].done = sc[1].done = 2;
+    sc[0].fail = sc[1].fail = 5;
+  }
+  Acc<T> vv[1] = {v};
+  P bt[1];
+  block_total_acc<T, 1>(vv, bt);
+  if (threadIdx.x == 0) cta_part[blockIdx.x] = bt[0];
+}
+
+// One CTA per SM, one node per thread per pass: 1024 (FP32, 64 registers)
+// or 512 (FP64) nodes in flight per SM cover the L2 latency of the vector
+// pass (its vectors stay L2-resident), and one CTA per SM keeps the partials
+// every CTA sums at the start few (one per SM).
 template <typename T>
-struct CgUnroll {
-  static constexpr int value = 1;
-  static constexpr int ctas_per_sm = sizeof(T) == 4 ? 4 : 2;
+struct CgShape {
+  static constexpr int threads = sizeof(T) == 4 ? 1024 : 512;
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kCgThreads, CgUnroll<T>::ctas_per_sm) pcg_cg_vector_kernel(
+__global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
     int nnd, const T* __restrict__ minv, typename Vec4<T>::type* __restrict__ x,
     typename Vec4<T>::type* __restrict__ r, typename Vec4<T>::type* __restrict__ u,
     typename Vec4<T>::type* __restrict__ p, typename Vec4<T>::type* __restrict__ s,
-    const typename Vec4<T>::type* __restrict__ w, const double* __restrict__ dpart, int ndp, double* vpart,
-    PcgScalars* sc) {
+    const typename Vec4<T>::type* __restrict__ w, const typename Partial<T>::type* __restrict__ dpart, int ndp,
+    double* vpart, PcgScalars* sc) {
   using V = typename Vec4<T>::type;
   using P = typename Partial<T>::type;
-  constexpr int U = CgUnroll<T>::value;
   __shared__ double coef[2];  // alpha, beta
   __shared__ int go;
+  // the first pass's node vectors: the product this kernel waits for writes
+  // none of them, and the vector kernel before it has completed (the product
+  // released this kernel only after its own wait for it)
+  const int n0 = blockIdx.x * blockDim.x + threadIdx.x;
+  V u0, p0, s0, x0, r0;
+  T B0[9];
+  if (n0 < nnd) {
+    u0 = u[n0];
+    p0 = p[n0];
+    s0 = s[n0];
+    x0 = x[n0];
+    r0 = r[n0];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) B0[m] = minv[(long long)n0 * 9 + m];
+  }
+  griddep_wait();  // w, the CTA partials and the scalars of the product
+  griddep_launch();
   if (((volatile PcgScalars*)sc)->done) return;
+  V w0;
+  if (n0 < nnd) w0 = w[n0];  // in flight while the scalars are formed
   const int it = sc->iters;  // updates done so far: the same in every CTA (scalars[0] is not written here)
-  const P* dp = reinterpret_cast<const P*>(dpart);
-  const P* prev = reinterpret_cast<const P*>(vpart + kDeltaCap + (size_t)(it & 1) * 2 * kVecCap);
-  P* next = reinterpret_cast<P*>(vpart + kDeltaCap + (size_t)((it + 1) & 1) * 2 * kVecCap);
+  const P* prev = reinterpret_cast<const P*>(vpart + (size_t)(it & 1) * 2 * kVecCap);
+  P* next = reinterpret_cast<P*>(vpart + (size_t)((it + 1) & 1) * 2 * kVecCap);
   {
     // totals of the product's u.w and the last vector kernel's r.u, r.r:
     // thread-strided sums in a fixed order, then the fixed block tree, in
     // the accumulator's arithmetic (compensated FP32 in the FP32 form)
     Acc<T> a[3];
-    for (int b = threadIdx.x; b < ndp; b += blockDim.x) acc_merge(a[0], dp[b]);
+    for (int b = threadIdx.x; b < ndp; b += blockDim.x) acc_merge(a[0], dpart[b]);
     if (it > 0)
       for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         acc_merge(a[1], prev[b]);
@@ -108,16 +224,22 @@ __global__ void __launch_bounds__(kCgThreads, CgUnroll<T>::ctas_per_sm) pcg_cg_v
       } else if (it >= o.max_it) {
         done = 3;
       } else {
-        double den = delta;
+        // alpha = gamma / (delta - beta gamma / alpha_old) with beta =
+        // gamma / gamma_old, as gamma t / (delta t - gamma^2), t = gamma_old
+        // alpha_old: one division on the dependent chain (FP64 division is
+        // long on GB300), beta's beside it
+        double num = gamma, den = delta;
         if (it > 0) {
-          beta = gamma / o.rz;  // o.rz, o.alpha: the last update's gamma and alpha
-          den = delta - beta * gamma / o.alpha;
+          const double t = o.rz * o.alpha;  // o.rz, o.alpha: the last update's gamma and alpha
+          beta = gamma / o.rz;
+          num = gamma * t;
+          den = delta * t - gamma * gamma;
         }
         if (!(den > 0.0) || !isfinite(den)) {
           done = 2;
           fail = isfinite(den) ? 2 : 3;
         } else {
-          alpha = gamma / den;
+          alpha = num / den;
         }
       }
       coef[0] = alpha;
@@ -145,53 +267,40 @@ __global__ void __launch_bounds__(kCgThreads, CgUnroll<T>::ctas_per_sm) pcg_cg_v
   const T a_ = T(coef[0]), b_ = T(coef[1]);
   const bool first = it == 0;
   Acc<T> acc[2];
-  const int step = gridDim.x * blockDim.x * U;
-  for (int base = blockIdx.x * blockDim.x * U + threadIdx.x; base < nnd; base += step) {
-    V un[U], wn[U], pn[U], sn[U], xn[U], rn[U];
-    T B[U][9];
-#pragma unroll
-    for (int k = 0; k < U; ++k) {
-      const int n = base + k * blockDim.x;
-      if (n < nnd) {
-        un[k] = u[n];
-        wn[k] = w[n];
-        pn[k] = p[n];
-        sn[k] = s[n];
-        xn[k] = x[n];
-        rn[k] = r[n];
-#pragma unroll
-        for (int m = 0; m < 9; ++m) B[k][m] = minv[(long long)n * 9 + m];
-      }
+  auto update = [&](int n, const V& un, const V& wn, const V& pn, const V& sn, const V& xn, const V& rn,
+                    const T (&B)[9]) {
+    V pv, sv;
+    if (first) {  // p = u, s = w (p and s hold nothing yet)
+      pv = un;
+      sv = wn;
+    } else {
+      pv = mk<V, T>(un.x + b_ * pn.x, un.y + b_ * pn.y, un.z + b_ * pn.z);
+      sv = mk<V, T>(wn.x + b_ * sn.x, wn.y + b_ * sn.y, wn.z + b_ * sn.z);
     }
+    const T rx = rn.x - a_ * sv.x, ry = rn.y - a_ * sv.y, rz = rn.z - a_ * sv.z;
+    const T zx = B[0] * rx + B[1] * ry + B[2] * rz;
+    const T zy = B[3] * rx + B[4] * ry + B[5] * rz;
+    const T zz = B[6] * rx + B[7] * ry + B[8] * rz;
+    p[n] = pv;
+    s[n] = sv;
+    x[n] = mk<V, T>(xn.x + a_ * pv.x, xn.y + a_ * pv.y, xn.z + a_ * pv.z);
+    r[n] = mk<V, T>(rx, ry, rz);
+    u[n] = mk<V, T>(zx, zy, zz);
+    acc[0].add_prod(rx, zx);
+    acc[0].add_prod(ry, zy);
+    acc[0].add_prod(rz, zz);
+    acc[1].add_prod(rx, rx);
+    acc[1].add_prod(ry, ry);
+    acc[1].add_prod(rz, rz);
+  };
+  const int step = gridDim.x * blockDim.x;
+  if (n0 < nnd) update(n0, u0, w0, p0, s0, x0, r0, B0);
+  for (int n = n0 + step; n < nnd; n += step) {
+    const V un = u[n], wn = w[n], pn = p[n], sn = s[n], xn = x[n], rn = r[n];
+    T B[9];
 #pragma unroll
-    for (int k = 0; k < U; ++k) {
-      const int n = base + k * blockDim.x;
-      if (n < nnd) {
-        V pv, sv;
-        if (first) {  // p = u, s = w (p and s hold nothing yet)
-          pv = un[k];
-          sv = wn[k];
-        } else {
-          pv = mk<V, T>(un[k].x + b_ * pn[k].x, un[k].y + b_ * pn[k].y, un[k].z + b_ * pn[k].z);
-          sv = mk<V, T>(wn[k].x + b_ * sn[k].x, wn[k].y + b_ * sn[k].y, wn[k].z + b_ * sn[k].z);
-        }
-        const T rx = rn[k].x - a_ * sv.x, ry = rn[k].y - a_ * sv.y, rz = rn[k].z - a_ * sv.z;
-        const T zx = B[k][0] * rx + B[k][1] * ry + B[k][2] * rz;
-        const T zy = B[k][3] * rx + B[k][4] * ry + B[k][5] * rz;
-        const T zz = B[k][6] * rx + B[k][7] * ry + B[k][8] * rz;
-        p[n] = pv;
-        s[n] = sv;
-        x[n] = mk<V, T>(xn[k].x + a_ * pv.x, xn[k].y + a_ * pv.y, xn[k].z + a_ * pv.z);
-        r[n] = mk<V, T>(rx, ry, rz);
-        u[n] = mk<V, T>(zx, zy, zz);
-        acc[0].add_prod(rx, zx);
-        acc[0].add_prod(ry, zy);
-        acc[0].add_prod(rz, zz);
-        acc[1].add_prod(rx, rx);
-        acc[1].add_prod(ry, ry);
-        acc[1].add_prod(rz, rz);
-      }
-    }
+    for (int m = 0; m < 9; ++m) B[m] = minv[(long long)n * 9 + m];
+    update(n, un, wn, pn, sn, xn, rn, B);
   }
   P bt[2];
   block_total_acc<T, 2>(acc, bt);
@@ -205,38 +314,114 @@ __global__ void __launch_bounds__(kCgThreads, CgUnroll<T>::ctas_per_sm) pcg_cg_v
 template <typename T>
 int vec_grid(Context* c, int* grid) {
   int per_sm = 0;
-  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_cg_vector_kernel<T>, kCgThreads, 0),
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_cg_vector_kernel<T>, CgShape<T>::threads, 0),
           "occupancy"))
     return TG_ERR_CUDA;
-  const int per = kCgThreads * CgUnroll<T>::value;
+  const int per = CgShape<T>::threads;
   *grid = std::max(1, std::min({(c->nnd + per - 1) / per, c->num_sms * std::max(per_sm, 1), kVecCap}));
+  return TG_OK;
+}
+
+// Launch shape of the product: a ring of the context's stages (2 or 3, 2 if
+// 3 do not fit) over the largest tile, as many CTAs as are resident.
+struct CgProduct {
+  int grid = 0, nst = 2, cap = 0, keep = -1;
+  size_t smem = 0;
+  void* fn = nullptr;
+};
+
+template <typename T>
+int product_shape(Context* c, CgProduct& pr) {
+  const bool f32 = std::is_same<T, float>::value;
+  pr.cap = (int)(((f32 ? c->blob_cap32 : c->blob_cap64) + 127) / 128 * 128);
+  int optin = 0;
+  if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
+    return TG_ERR_CUDA;
+  pr.nst = c->spmv_stages == 3 && 3 * (size_t)pr.cap + 1024 <= (size_t)optin ? 3 : 2;
+  pr.fn = pr.nst == 3 ? reinterpret_cast<void*>(pcg_cg_spmv_kernel<T, 3>)
+                      : reinterpret_cast<void*>(pcg_cg_spmv_kernel<T, 2>);
+  pr.smem = (size_t)pr.nst * pr.cap;
+  cudaFuncAttributes fa;
+  if (!ok(c, cudaFuncGetAttributes(&fa, pr.fn), "function attributes")) return TG_ERR_CUDA;
+  if (pr.smem + fa.sharedSizeBytes + 1024 > (size_t)optin) {
+    c->err = "single-reduction PCG: tile ring does not fit in shared memory";
+    return TG_ERR_CAPACITY;
+  }
+  // one value for every caller: other contexts may configure and launch it
+  if (!ok(c, cudaFuncSetAttribute(pr.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
+          "smem attribute"))
+    return TG_ERR_CUDA;
+  int per_sm = 0;
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pr.fn, 256, pr.smem), "occupancy"))
+    return TG_ERR_CUDA;
+  if (per_sm < 1) {
+    c->err = "single-reduction PCG: product tile does not fit";
+    return TG_ERR_CAPACITY;
+  }
+  pr.grid = std::max(1, std::min({c->ntiles, c->num_sms * per_sm, kCtaCap}));
+  pr.keep = -1;
+  if (c->l2_keep >= 0) {
+    const std::vector<long long>& off = f32 ? c->h_blob_off32 : c->h_blob_off64;
+    int t = 0;
+    while (t < c->ntiles && off[t + 1] <= c->l2_keep) ++t;
+    pr.keep = t;
+  }
   return TG_OK;
 }
 
 template <typename T>
 int capture(Context* c, int precision, const T* minv) {
   using V = typename Vec4<T>::type;
-  SpmvPlan plan;
-  int s = spmv_plan(c, precision, plan);
+  using P = typename Partial<T>::type;
+  CgProduct pr;
+  int s = product_shape<T>(c, pr);
   if (s) return s;
-  if (plan.sym || plan.spmv > kDeltaCap) {
-    c->err = "single-reduction PCG: product launch shape out of range";
-    return TG_ERR_CAPACITY;
-  }
   int nv = 0;
   s = vec_grid<T>(c, &nv);
   if (s) return s;
+  int ntiles = c->ntiles;
+  const long long* off = std::is_same<T, float>::value ? c->d_blob_off32 : c->d_blob_off64;
+  const unsigned char* blob = std::is_same<T, float>::value ? c->d_blob32 : c->d_blob64;
+  P* cta_part = reinterpret_cast<P*>(c->d_partials + kCgPartials);
+  const V* pu = (const V*)c->d_z;
+  V* qw = (V*)c->d_q;
+  PcgScalars* sc = c->d_pcg;
+  int* status = c->d_status;
+  int cap = pr.cap, keep = pr.keep;
+  void* args[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &cta_part, &sc, &status};
+  int nnd = c->nnd, ndp = pr.grid;
+  const T* mv = minv;
+  V *x = (V*)c->d_x, *r = (V*)c->d_r, *u = (V*)c->d_z, *p = (V*)c->d_p, *sv = (V*)c->d_cg_s;
+  const V* w = (const V*)c->d_q;
+  const P* dpart = cta_part;
+  double* vpart = c->d_partials;
+  void* vargs[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc};
+  // every launch after the first of the chunk depends programmatically on
+  // the one before it
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t pc = {};
+  pc.gridDim = dim3(pr.grid);
+  pc.blockDim = dim3(256);
+  pc.dynamicSmemBytes = pr.smem;
+  pc.stream = c->stream;
+  cudaLaunchConfig_t vc = {};
+  vc.gridDim = dim3(nv);
+  vc.blockDim = dim3(CgShape<T>::threads);
+  vc.dynamicSmemBytes = 0;
+  vc.stream = c->stream;
+  vc.attrs = at;
+  vc.numAttrs = c->cg_pdl ? 1 : 0;
   cudaGraph_t graph;
   if (!ok(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return TG_ERR_CUDA;
   cudaError_t le = cudaSuccess;
   for (int k = 0; k < kCgChunk && le == cudaSuccess; ++k) {
-    spmv_run(c, precision, plan, c->d_z, c->d_q, c->d_partials, c->d_pcg, nullptr, 1);
-    le = cudaGetLastError();
+    pc.attrs = at;
+    pc.numAttrs = (k > 0 && c->cg_pdl) ? 1 : 0;
+    le = cudaLaunchKernelExC(&pc, pr.fn, args);
     if (le != cudaSuccess) break;
-    pcg_cg_vector_kernel<T><<<nv, kCgThreads, 0, c->stream>>>(c->nnd, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z,
-                                                              (V*)c->d_p, (V*)c->d_cg_s, (const V*)c->d_q,
-                                                              c->d_partials, plan.spmv, c->d_partials, c->d_pcg);
-    le = cudaGetLastError();
+    le = cudaLaunchKernelExC(&vc, reinterpret_cast<const void*>(pcg_cg_vector_kernel<T>), vargs);
   }
   const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
   if (!ok(c, le, "capture launch") || !ok(c, ee, "end capture")) {
@@ -253,8 +438,8 @@ template <typename T>
 int solve_cg_t(Context* c, int precision, const double4_32a* d_rhs, double rel_tol, int max_it, int precond,
                int* iters, double* rel_res) {
   using V = typename Vec4<T>::type;
-  static_assert(kCgPartials <= 8192, "partials buffer");
-  if (c->partials_cap * 2 < kCgPartials) {
+  static_assert(kCgPartials + kCtaCap <= 8192, "partials buffer");
+  if (c->partials_cap * 2 < kCgPartials + kCtaCap) {
     c->err = "single-reduction PCG: partials buffer too small";
     return TG_ERR_CAPACITY;
   }

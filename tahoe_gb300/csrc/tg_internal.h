@@ -242,6 +242,7 @@ struct Context {
   void* d_cg_s = nullptr;  // s = A p by recurrence (single-reduction PCG), in the solve's precision
   int cg_s_precision = -1;
   int pcg_form = 1;        // 1: single-vector solves on full storage run the single-reduction PCG (pcg_cg.cu)
+  int cg_pdl = 1;           // its kernels launch with programmatic dependencies
   cudaGraphExec_t cg_graph = nullptr;  // captured chunk of the single-reduction PCG
   int cg_graph_key = -1;
   int pcg_vec_precision = -1;
@@ -316,6 +317,9 @@ void build_block_pattern(int nnd, int nel, const int* conn, std::vector<int>& ro
 void build_contrib_map(int nnd, int nel, const int* conn, const std::vector<int>& rowptr,
                        const std::vector<int>& col, std::vector<int>& cptr, std::vector<int>& contrib);
 int build_tiles(Context* c, int tile_blocks);
+// CTAs of the full-storage product's persistent grid for FP32 tiles of at
+// most cap32 bytes (0 if the ring does not fit) (krylov.cu)
+int spmv_grid_for(Context* c, long long cap32);
 void drop_graphs(Context* c);  // captured Krylov iterations (their launches bake in the product's shape)
 int ensure_blob(Context* c, int precision);
 
@@ -341,13 +345,12 @@ int pcg_solve_segmented(Context* c, const double4_32a* d_rhs, double rel_tol, in
                         double* rel_res);
 void seg_free(Context* c);  // graph and bookkeeping (buffers go back with the mesh)
 int pcg_vectors(Context* c, int precision);  // x r z p q of the solve's precision (krylov.cu)
-// the single-vector product for other solvers (segpcg.cu, pcg_cg.cu): plan
-// once per mesh/precision, launch on (p, q); node_dot (nnd, may be NULL)
-// receives each row's p.q; cta_only: each CTA writes its partial p.q to
-// partials[CTA] and no total is formed
+// the single-vector product for other solvers (segpcg.cu): plan once per
+// mesh/precision, launch on (p, q); node_dot (nnd, may be NULL) receives
+// each row's p.q
 int spmv_plan(Context* c, int precision, SpmvPlan& P);
 void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void* q, double* partials, PcgScalars* sc,
-              double* node_dot, int cta_only = 0);
+              double* node_dot);
 void sym_free(Context* c);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----

@@ -479,8 +479,9 @@ class Context:
         self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")
 
     def pcg_form(self, form):
-        """Recurrences of the single-vector PCG: 1 single-reduction
-        (default), 0 textbook."""
+        """Recurrences of the single-vector PCG: 1 single-reduction with
+        programmatic launch dependencies (default), 2 the same without them,
+        0 textbook."""
         self._chk(self.L.tg_pcg_form(self.h, int(form)), "tg_pcg_form")
         self.form = int(form)
 

@@ -66,6 +66,21 @@ def test_forms_reach_the_same_solution(precision, precond):
 
 
 @pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+def test_programmatic_launch_dependencies_leave_the_iterates_bitwise_unchanged(precision):
+    m = _model()
+    c, R = _system(m, precision, lib.PRECOND_BLOCK_JACOBI)
+    out = []
+    for form in (1, 2, 1):
+        c.pcg_form(form)
+        out.append(c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_BLOCK_JACOBI))
+    for du, its, rr, rc in out:
+        assert rc == 0
+        assert its == out[0][1]
+        assert np.array_equal(du, out[0][0])
+    c.pcg_form(1)
+
+
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
 def test_single_reduction_form_is_bitwise_repeatable(precision):
     m = _model()
     c, R = _system(m, precision, lib.PRECOND_JACOBI)
