@@ -84,7 +84,7 @@ def spmv_roofline(ctx, precision):
     b = (workloads.spmv_bytes_sym if sym else workloads.spmv_bytes)(ctx.block_nnz, ctx.nnd, s_val)
     peak, kind = peaks()
     ach = b / (ms * 1e-3) / 1e9
-    return {"kernel": "pcg_spmv_sym_kernel" if sym else "pcg_spmv_kernel", "storage": "symmetric" if sym else "full",
+    return {"kernel": ctx.product_kernel(), "storage": "symmetric" if sym else "full",
             "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
             "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": int(b), "ms_per_launch": round(ms, 4)}
 
@@ -378,15 +378,19 @@ def run_ours(args):
     s_val = 4 if prec == lib.MIXED else 8
     nnzb = ctx.block_nnz
     sym = bool(getattr(ctx, "sym_mode", 0))
-    prof = "pcg_spmv_sym_c2_64cubed.md" if sym else "pcg_spmv_c2_64cubed.md"
+    product = ctx.product_kernel()
+    cg = product == "pcg_cg_spmv_kernel"
+    prof = {"pcg_spmv_sym_kernel": "pcg_spmv_sym_c2_64cubed.md", "pcg_cg_spmv_kernel": "pcg_cg_spmv_c2_64cubed.md"}.get(
+        product, "pcg_spmv_c2_64cubed.md")
     bytes_spmv = (workloads.spmv_bytes_sym if sym else workloads.spmv_bytes)(nnzb, nnd, s_val)
     peak, peak_kind = peaks()
     achieved = bytes_spmv / (t_spmv * 1e-3) / 1e9
     elements_per_s = mesh.nel / ((t_tan + t_asm) * 1e-3)
     # the other HBM-bound kernels of the step, same peak and byte model
     other_rooflines = {}
-    for name, b, t in (("assemble_kernel", workloads.assembly_bytes(mesh.nel, nnzb, nnd, s_val), t_asm),
-                       ("pcg_update_kernel", workloads.update_bytes(nnd, s_val), t_upd)):
+    vec = ("pcg_cg_vector_kernel", workloads.cg_vector_bytes(nnd, s_val), t_upd) if cg else \
+        ("pcg_update_kernel", workloads.update_bytes(nnd, s_val), t_upd)
+    for name, b, t in (("assemble_kernel", workloads.assembly_bytes(mesh.nel, nnzb, nnd, s_val), t_asm), vec):
         a = b / (t * 1e-3) / 1e9
         other_rooflines[name] = {"bound": "hbm", "achieved": round(a, 1), "peak": peak, "unit": "GB/s",
                                  "frac": round(a / peak, 4), "algorithmic_bytes": int(b), "ms_per_launch": round(t, 5)}
@@ -409,9 +413,10 @@ def run_ours(args):
         "pcg_iterations_per_step": float(np.mean(pcg_its)),
         "predictor_pcg_iterations": pred_its,
         "elements_assembled_per_s": round(elements_per_s, 1),
-        "kernel_ms": {"pcg_spmv": round(t_spmv, 5), "pcg_update": round(t_upd, 5), "tangent": round(t_tan, 4),
+        "pcg_form": "single-reduction (Chronopoulos-Gear), programmatic launch" if cg else "textbook",
+        "kernel_ms": {"pcg_product": round(t_spmv, 5), "pcg_vector": round(t_upd, 5), "tangent": round(t_tan, 4),
                       "assembly": round(t_asm, 4), "residual": round(t_res, 4)},
-        "roofline": {"kernel": "pcg_spmv_sym_kernel" if sym else "pcg_spmv_kernel",
+        "roofline": {"kernel": product,
                      "storage": "symmetric" if sym else "full", "bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "algorithmic_bytes": int(bytes_spmv),

@@ -418,8 +418,9 @@ int tg_tuning_get(const tg_context* ctx, int* tile_blocks, int* stages, int* tan
 int tg_timer_start(tg_context* ctx);
 int tg_timer_stop(tg_context* ctx, double* ms);
 /* average device time of `reps` standalone launches of one hot kernel on the
- * current state: 0 PCG SpMV, 1 PCG vector update, 2 element tangent,
- * 3 assembly, 4 element residual (+gather) */
+ * current state: 0 PCG product, 1 PCG vector kernel (the kernels of the form
+ * the single-vector solve runs, tg_pcg_form), 2 element tangent, 3 assembly,
+ * 4 element residual (+gather) */
 int tg_time_kernel(tg_context* ctx, int which, int reps, double* ms_per_launch);
 
 #ifdef __cplusplus

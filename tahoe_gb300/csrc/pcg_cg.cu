@@ -490,7 +490,95 @@ int solve_cg_t(Context* c, int precision, const double4_32a* d_rhs, double rel_t
   return pcg_finish(c, c->h_pcg[last], iters, rel_res);
 }
 
+// Average device time of standalone launches of one kernel of the form
+// (which 0: product, 1: vector kernel) on the current tangent, each launch
+// doing the same work: the solve's vectors and scalars are set up from R as
+// for a solve, the product's partials come from one product launch, and the
+// scalars are reset to the first iteration before every vector launch.
+template <typename T>
+int time_cg_t(Context* c, int precision, int which, int reps, double* ms) {
+  using V = typename Vec4<T>::type;
+  using P = typename Partial<T>::type;
+  int s = pcg_vectors(c, precision);
+  if (s) return s;
+  if (!c->d_cg_s || c->cg_s_precision != precision) {
+    if (c->d_cg_s) dfree(c, c->d_cg_s);
+    c->d_cg_s = nullptr;
+    V* v = nullptr;
+    if (!dalloc(c, &v, (size_t)c->nnd)) return TG_ERR_OOM;
+    c->d_cg_s = v;
+    c->cg_s_precision = precision;
+    cg_free(c);
+  }
+  const T* minv = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
+  s = pcg_start(c, precision, c->d_R, minv, 1e-30, 1 << 30);
+  if (s) return s;
+  PcgScalars h;
+  if (!ok(c, cudaMemcpyAsync(&h, c->d_pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c->stream), "scalars") ||
+      !ok(c, cudaStreamSynchronize(c->stream), "sync"))
+    return TG_ERR_CUDA;
+  h.done = 0;
+  h.iters = 0;
+  CgProduct pr;
+  s = product_shape<T>(c, pr);
+  if (s) return s;
+  int nv = 0;
+  s = vec_grid<T>(c, &nv);
+  if (s) return s;
+  int ntiles = c->ntiles, cap = pr.cap, keep = pr.keep, nnd = c->nnd, ndp = pr.grid;
+  const long long* off = std::is_same<T, float>::value ? c->d_blob_off32 : c->d_blob_off64;
+  const unsigned char* blob = std::is_same<T, float>::value ? c->d_blob32 : c->d_blob64;
+  P* cta_part = reinterpret_cast<P*>(c->d_partials + kCgPartials);
+  const P* dpart = cta_part;
+  const V* pu = (const V*)c->d_z;
+  V* qw = (V*)c->d_q;
+  PcgScalars* sc = c->d_pcg;
+  int* status = c->d_status;
+  const T* mv = minv;
+  V *x = (V*)c->d_x, *r = (V*)c->d_r, *u = (V*)c->d_z, *p = (V*)c->d_p, *sv = (V*)c->d_cg_s;
+  const V* w = (const V*)c->d_q;
+  double* vpart = c->d_partials;
+  void* pargs[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &cta_part, &sc, &status};
+  void* vargs[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc};
+  const void* vfn = reinterpret_cast<const void*>(pcg_cg_vector_kernel<T>);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double total = 0.0;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < reps + 1 && e == cudaSuccess; ++k) {
+    // both scalar states at the first iteration (the product hands [1] to [0])
+    cudaMemcpyAsync(c->d_pcg, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->d_pcg + 1, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream);
+    if (which == 1 && k == 0) {  // the product's partials for the vector launches
+      e = cudaLaunchKernel(pr.fn, dim3(pr.grid), dim3(256), pargs, pr.smem, c->stream);
+      continue;
+    }
+    cudaEventRecord(a, c->stream);
+    e = which == 0 ? cudaLaunchKernel(pr.fn, dim3(pr.grid), dim3(256), pargs, pr.smem, c->stream)
+                   : cudaLaunchKernel(vfn, dim3(nv), dim3(CgShape<T>::threads), vargs, 0, c->stream);
+    cudaEventRecord(b, c->stream);
+    c->launches++;
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    if (which == 1 || k > 0) total += t;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = total / reps;
+  if (!ok(c, e, "time_cg_kernel")) return TG_ERR_CUDA;
+  return ok(c, cudaGetLastError(), "time_cg_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
 }  // namespace
+
+int time_cg_kernel(Context* c, int which, int reps, double* ms) {
+  if (c->tangent_precision == TG_MIXED) return time_cg_t<float>(c, TG_MIXED, which, reps, ms);
+  if (c->tangent_precision == TG_FP64) return time_cg_t<double>(c, TG_FP64, which, reps, ms);
+  c->err = "form the tangent first";
+  return TG_ERR_ARG;
+}
 
 void cg_free(Context* c) {
   if (c->cg_graph) cudaGraphExecDestroy(c->cg_graph);

@@ -385,6 +385,7 @@ int pcg_finish(Context* c, const PcgScalars& h, int* iters, double* rel_res);
 int pcg_solve_cg(Context* c, int precision, const double4_32a* d_rhs, double rel_tol, int max_it, int precond,
                  int* iters, double* rel_res);
 void cg_free(Context* c);  // the captured iterations
+int time_cg_kernel(Context* c, int which, int reps, double* ms);  // 0 product, 1 vector kernel
 // PCG with every work vector, partial sum and scalar in caller scratch
 constexpr size_t kScratchScalarBytes = 256;
 constexpr size_t kScratchPartialBytes = 32768;

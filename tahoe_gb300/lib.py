@@ -168,6 +168,17 @@ class Context:
             raise TahoeError(rc, "tg_create", "no CUDA device or driver")
         self.h = h
         self.nnd = self.nel = self.neq = 0
+        self.form = 1            # tg_pcg_form default
+        self.l2_keep = 16 << 20  # tg_spmv_l2_keep default
+        self.sym_mode = 0
+
+    def product_kernel(self):
+        """Name of the kernel the single-vector solve multiplies with."""
+        if self.sym_mode and not getattr(self, "composed", False):
+            return "pcg_spmv_sym_kernel"
+        if self.form in (1, 2) and not getattr(self, "composed", False):
+            return "pcg_cg_spmv_kernel"
+        return "pcg_spmv_kernel"
 
     def close(self):
         if getattr(self, "h", None):

@@ -89,6 +89,14 @@ def assembly_bytes(nel, nnzb, nnd, s_val):
     return nel * 36 * 12 * s_val + nel * 64 * 4 + (nnzb + 1) * 4 + nnzb * 9 * s_val + nnzb * 4 + nnd * 18 * s_val
 
 
+def cg_vector_bytes(nnd, s_val):
+    """Algorithmic bytes of one vector kernel of the single-reduction PCG:
+    u, w, p, s, x, r and the 3x3 preconditioner block read, p, s, x, r and u
+    written (vectors padded to 4 lanes)."""
+    s_vec = 4 * s_val
+    return nnd * (6 * s_vec + 9 * s_val) + nnd * 5 * s_vec
+
+
 def update_bytes(nnd, s_val):
     """Algorithmic bytes of one PCG vector update: p, q, x, r and the 3x3
     preconditioner block read, x, r, z and the next p written (vectors padded
