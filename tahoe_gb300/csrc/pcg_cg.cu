@@ -190,27 +190,42 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
   }
   griddep_wait();  // w, the CTA partials and the scalars of the product
   griddep_launch();
-  if (((volatile PcgScalars*)sc)->done) return;
+  // one round trip for everything the scalars need: the state (read by one
+  // thread -- every warp of the grid loading the same line would queue at
+  // one L2 slice; scalars[0] is not written while this kernel runs, so every
+  // CTA reads the same), w, the product's partials and both buffers of the
+  // last vector kernel's partials (which one is the last depends on the
+  // iteration)
+  __shared__ PcgScalars so;  // kept in shared memory: registers stay free for the vector pass
+  if (threadIdx.x == 0) so = *sc;
   V w0;
   if (n0 < nnd) w0 = w[n0];  // in flight while the scalars are formed
-  const int it = sc->iters;  // updates done so far: the same in every CTA (scalars[0] is not written here)
-  const P* prev = reinterpret_cast<const P*>(vpart + (size_t)(it & 1) * 2 * kVecCap);
+  const int nb = gridDim.x;  // at most one partial of each buffer per thread
+  P g0{}, g1{}, q0{}, q1{};
+  if ((int)threadIdx.x < nb) {
+    g0 = reinterpret_cast<const P*>(vpart)[threadIdx.x];
+    q0 = reinterpret_cast<const P*>(vpart)[kVecCap + threadIdx.x];
+    g1 = reinterpret_cast<const P*>(vpart)[2 * kVecCap + threadIdx.x];
+    q1 = reinterpret_cast<const P*>(vpart)[3 * kVecCap + threadIdx.x];
+  }
+  Acc<T> a[3];
+  for (int b = threadIdx.x; b < ndp; b += blockDim.x) acc_merge(a[0], dpart[b]);
+  __syncthreads();
+  if (so.done) return;
+  const int it = so.iters;  // updates done so far
   P* next = reinterpret_cast<P*>(vpart + (size_t)((it + 1) & 1) * 2 * kVecCap);
   {
     // totals of the product's u.w and the last vector kernel's r.u, r.r:
     // thread-strided sums in a fixed order, then the fixed block tree, in
     // the accumulator's arithmetic (compensated FP32 in the FP32 form)
-    Acc<T> a[3];
-    for (int b = threadIdx.x; b < ndp; b += blockDim.x) acc_merge(a[0], dpart[b]);
-    if (it > 0)
-      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-        acc_merge(a[1], prev[b]);
-        acc_merge(a[2], prev[kVecCap + b]);
-      }
+    if (it > 0 && (int)threadIdx.x < nb) {
+      acc_merge(a[1], (it & 1) ? g1 : g0);
+      acc_merge(a[2], (it & 1) ? q1 : q0);
+    }
     P tot[3];
     block_total_acc<T, 3>(a, tot);
     if (threadIdx.x == 0) {
-      PcgScalars o = *sc;
+      PcgScalars o = so;
       const double delta = partial_value(tot[0]);
       const double gamma = it > 0 ? partial_value(tot[1]) : o.rz;
       const double rr = it > 0 ? partial_value(tot[2]) : o.rr;
@@ -318,7 +333,9 @@ int vec_grid(Context* c, int* grid) {
           "occupancy"))
     return TG_ERR_CUDA;
   const int per = CgShape<T>::threads;
-  *grid = std::max(1, std::min({(c->nnd + per - 1) / per, c->num_sms * std::max(per_sm, 1), kVecCap}));
+  // at most one CTA per thread of a CTA: each thread loads at most one of
+  // the previous vector kernel's partials of each kind
+  *grid = std::max(1, std::min({(c->nnd + per - 1) / per, c->num_sms * std::max(per_sm, 1), kVecCap, per}));
   return TG_OK;
 }
 
