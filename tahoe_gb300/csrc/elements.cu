@@ -678,6 +678,8 @@ __device__ __forceinline__ void slot_pair(int slot, int& a, int& b) {
 // UL: the updated-Lagrangian gradients and weight (compiled only into the
 // instantiation that needs them, so the other formulations keep their
 // register budget)
+constexpr int kTanH = 21;  // per (point, node): D B_b (18 values) and sigma grad N_b (3)
+
 template <typename T, int kTanElems, bool UL>
 __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const double* __restrict__ X, int nnd,
                                                               const int* __restrict__ conn,
@@ -691,6 +693,8 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
   __shared__ T sS[kTanElems][8][6];     // per point Cauchy stress (scaled, TL only)
   __shared__ T sW[kTanElems][8];        // per point w det J (B-bar mean gradients)
   __shared__ T sM[kTanElems][3][8];     // element-mean gradients (B-bar)
+  // dynamic: [kTanElems][8 points][8 nodes][kTanH] per-node products h_b
+  extern __shared__ __align__(16) unsigned char tan_dyn[];
   const int tid = threadIdx.x;
   const int e0 = blockIdx.x * kTanElems;
 
@@ -816,20 +820,19 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
     __syncthreads();
   }
 
-  const int le = tid / kSlots, slot = tid - le * kSlots;
-  const int e = e0 + le;
-  if (e >= nel) return;
-  int a, b;
-  slot_pair(slot, a, b);
+  // Per (element, point, node b), once: h_b = D B_b (6 x 3; with the B-bar
+  // correction of node b's columns) and the geometric term's sigma grad N_b
+  // (3).  Every node-pair slot (a, b) then only contracts with node a's
+  // gradients: the h_b a slot used to form for itself are shared by the
+  // slots of the same b (54 of the ~93 FMA a slot spent per point).
   const bool tl = mt.formulation != TG_SMALL_STRAIN;  // geometric stiffness (TL and UL)
-  T K[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) K[k] = T(0);
-  for (int ip = 0; ip < 8; ++ip) {
-    const T ga[3] = {sG[le][ip][0][a], sG[le][ip][1][a], sG[le][ip][2][a]};
-    const T gb[3] = {sG[le][ip][0][b], sG[le][ip][1][b], sG[le][ip][2][b]};
-    const T* D = sD[le][ip];
-    // h[V][j] = sum_n D[V][vgt(j,n)] gb[n];  K(i,j) += sum_m ga[m] h[vgt(i,m)][j]
+  T(*sH)[8][8][kTanH] = reinterpret_cast<T(*)[8][8][kTanH]>(tan_dyn);
+  for (int item = tid; item < kTanElems * 64; item += blockDim.x) {
+    const int hl = item >> 6, ip = (item >> 3) & 7, b = item & 7;
+    if (e0 + hl >= nel) continue;
+    const T gb[3] = {sG[hl][ip][0][b], sG[hl][ip][1][b], sG[hl][ip][2][b]};
+    const T* D = sD[hl][ip];
+    // h[V][j] = sum_n D[V][vgt(j,n)] gb[n]
     T h[6][3];
 #pragma unroll
     for (int V = 0; V < 6; ++V)
@@ -838,30 +841,54 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
         h[V][j] = D[V * 6 + vgt(j, 0)] * gb[0] + D[V * 6 + vgt(j, 1)] * gb[1] + D[V * 6 + vgt(j, 2)] * gb[2];
     if (bbar) {
       // B-bar columns: normal rows plus f = (mean - grad)/3 (Hughes 4.5.11-16)
-      const T fa[3] = {(sM[le][0][a] - ga[0]) / T(3), (sM[le][1][a] - ga[1]) / T(3), (sM[le][2][a] - ga[2]) / T(3)};
-      const T fb[3] = {(sM[le][0][b] - gb[0]) / T(3), (sM[le][1][b] - gb[1]) / T(3), (sM[le][2][b] - gb[2]) / T(3)};
+      const T fb[3] = {(sM[hl][0][b] - gb[0]) / T(3), (sM[hl][1][b] - gb[1]) / T(3), (sM[hl][2][b] - gb[2]) / T(3)};
 #pragma unroll
       for (int V = 0; V < 6; ++V) {
         const T ds = D[V * 6 + 0] + D[V * 6 + 1] + D[V * 6 + 2];
 #pragma unroll
         for (int j = 0; j < 3; ++j) h[V][j] += fb[j] * ds;
       }
+    }
+    T* out = sH[hl][ip][b];
+#pragma unroll
+    for (int V = 0; V < 6; ++V)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) out[V * 3 + j] = h[V][j];
+    if (tl) {
+      const T* sp = sS[hl][ip];
+      out[18] = sp[0] * gb[0] + sp[5] * gb[1] + sp[4] * gb[2];
+      out[19] = sp[5] * gb[0] + sp[1] * gb[1] + sp[3] * gb[2];
+      out[20] = sp[4] * gb[0] + sp[3] * gb[1] + sp[2] * gb[2];
+    }
+  }
+  __syncthreads();
+
+  const int le = tid / kSlots, slot = tid - le * kSlots;
+  const int e = e0 + le;
+  if (e >= nel) return;
+  int a, b;
+  slot_pair(slot, a, b);
+  T K[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) K[k] = T(0);
+  for (int ip = 0; ip < 8; ++ip) {
+    const T ga[3] = {sG[le][ip][0][a], sG[le][ip][1][a], sG[le][ip][2][a]};
+    const T* h = sH[le][ip][b];
+    // K(i,j) += sum_m ga[m] h[vgt(i,m)][j]
+    if (bbar) {
+      const T fa[3] = {(sM[le][0][a] - ga[0]) / T(3), (sM[le][1][a] - ga[1]) / T(3), (sM[le][2][a] - ga[2]) / T(3)};
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) K[i * 3 + j] += fa[i] * (h[0][j] + h[1][j] + h[2][j]);
+        for (int j = 0; j < 3; ++j) K[i * 3 + j] += fa[i] * (h[0 * 3 + j] + h[1 * 3 + j] + h[2 * 3 + j]);
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        K[i * 3 + j] += ga[0] * h[vgt(i, 0)][j] + ga[1] * h[vgt(i, 1)][j] + ga[2] * h[vgt(i, 2)][j];
+        K[i * 3 + j] += ga[0] * h[vgt(i, 0) * 3 + j] + ga[1] * h[vgt(i, 1) * 3 + j] + ga[2] * h[vgt(i, 2) * 3 + j];
     if (tl) {
-      const T* s = sS[le][ip];
-      const T sg0 = s[0] * gb[0] + s[5] * gb[1] + s[4] * gb[2];
-      const T sg1 = s[5] * gb[0] + s[1] * gb[1] + s[3] * gb[2];
-      const T sg2 = s[4] * gb[0] + s[3] * gb[1] + s[2] * gb[2];
-      const T geo = ga[0] * sg0 + ga[1] * sg1 + ga[2] * sg2;
+      const T geo = ga[0] * h[18] + ga[1] * h[19] + ga[2] * h[20];
       K[0] += geo;
       K[4] += geo;
       K[8] += geo;
@@ -1035,15 +1062,25 @@ int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out) {
   return ok(c, cudaGetLastError(), "nodal_stress_kernel") ? TG_OK : TG_ERR_CUDA;
 }
 
+template <typename T, int EPB, bool UL>
+void launch_tangent_t(Context* c, T* Ke) {
+  const int grid = (c->nel + EPB - 1) / EPB;
+  const size_t dyn = (size_t)EPB * 64 * kTanH * sizeof(T);
+  // the per-node products exceed the default dynamic shared memory for some
+  // shapes; the attribute belongs to the function on the current device
+  // (the same value for every caller), set at every launch -- a tangent is
+  // formed once per Newton iteration
+  cudaFuncSetAttribute(tangent_kernel<T, EPB, UL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  tangent_kernel<T, EPB, UL><<<grid, EPB * kSlots, dyn, c->stream>>>(
+      c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats, j2view(c), Ke, c->d_status);
+}
+
 template <int EPB, bool UL>
 void launch_tangent_form(Context* c, int precision) {
-  const int grid = (c->nel + EPB - 1) / EPB;
   if (precision == TG_MIXED)
-    tangent_kernel<float, EPB, UL><<<grid, EPB * kSlots, 0, c->stream>>>(
-        c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats, j2view(c), c->d_Ke32, c->d_status);
+    launch_tangent_t<float, EPB, UL>(c, c->d_Ke32);
   else
-    tangent_kernel<double, EPB, UL><<<grid, EPB * kSlots, 0, c->stream>>>(
-        c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats, j2view(c), c->d_Ke64, c->d_status);
+    launch_tangent_t<double, EPB, UL>(c, c->d_Ke64);
 }
 
 template <int EPB>
