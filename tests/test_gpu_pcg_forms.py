@@ -124,3 +124,59 @@ def test_single_reduction_form_converges_within_the_first_chunk():
     c.pcg_form(0)
     du0, its0, rr0, rc0 = c.pcg(R, rel_tol=0.3, max_it=20000, precond=lib.PRECOND_BLOCK_JACOBI)
     assert rc0 == 0 and abs(its0 - its) <= 1
+
+
+def _iso_C(E=1.0, nu=0.3):
+    mu = 0.5 * E / (1.0 + nu)
+    lam = 2.0 * mu * nu / (1.0 - 2.0 * nu)
+    C = np.zeros((6, 6))
+    C[:3, :3] = lam
+    C[np.arange(3), np.arange(3)] += 2.0 * mu
+    C[np.arange(3, 6), np.arange(3, 6)] = mu
+    return C
+
+
+def _small_strain_system(C, precision):
+    mesh = BoxMesh(8, 8, 8, jitter=0.2, seed=7)
+    m = SolidModel(mesh.X, mesh.conn, "small_strain", {"kind": "ss_hookean", "C": C.reshape(36)})
+    for node in mesh.face_nodes(2, 0):
+        for d in range(3):
+            m.add_kbc(node, d)
+    for node in mesh.face_nodes(2, 1):
+        m.add_kbc(node, 2, -0.01, True)
+    m.set_schedule([(0.0, 1.0)])
+    m.setup()
+    c = m.ctx
+    u = np.zeros((mesh.nnd, 3))
+    u[mesh.face_nodes(2, 1), 2] = -0.01
+    c.set_u(u)
+    c.set_iteration(-1)
+    R, _ = c.residual()
+    c.tangent(precision)
+    return c, R
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+def test_iteration_limit_is_reported_not_raised(form, precision):
+    c, R = _small_strain_system(_iso_C(), precision)
+    c.pcg_form(form)
+    du, its, rr, rc = c.pcg(R, rel_tol=1e-14, max_it=5, precond=lib.PRECOND_JACOBI)
+    assert rc == -6  # TG_ERR_NOT_CONVERGED
+    assert its == 5
+    assert 0.0 < rr < 1.0
+    c.pcg_form(1)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+def test_indefinite_operator_breaks_down(form, precision):
+    # a negative-definite stiffness: the first curvature p.Ap (u.Au in the
+    # single-reduction form) is negative, and both forms stop with it
+    c, R = _small_strain_system(-_iso_C(), precision)
+    c.pcg_form(form)
+    with pytest.raises(lib.TahoeError) as ei:
+        c.pcg(R, rel_tol=1e-8, max_it=100, precond=lib.PRECOND_JACOBI)
+    assert ei.value.code == -5  # TG_ERR_NAN: breakdown
+    assert "indefinite" in str(ei.value)
+    c.pcg_form(1)
