@@ -138,6 +138,13 @@ int tg_set_iteration(tg_context* ctx, int iteration);
  * SolverT.cpp:446).  R_out (neq) may be NULL (kept on the device); norm_out
  * receives ||R||_2 (SolverT::Residual, SolverT.cpp:848). */
 int tg_form_residual(tg_context* ctx, double* R_out, double* norm_out);
+/* the same in the arithmetic of a Newton driver of the given precision:
+ * TG_FP64 as tg_form_residual; TG_MIXED forms the element forces of a
+ * total-Lagrangian group whose blocks are all Simo in double-float arithmetic
+ * on the FP32 pipe (pairs of floats, 48 significant bits: the error bounds of
+ * the FP64 operations with 2^-48 for 2^-53, FP32's exponent range), the
+ * other groups in FP64.  The gather, R and its norm stay FP64. */
+int tg_form_residual_precision(tg_context* ctx, int precision, double* R_out, double* norm_out);
 /* element stiffness + deterministic CSR assembly + preconditioner in the
  * given precision, device resident (SolidElementT::ElementLHSDriver,
  * SolidElementT.cpp:1100 + MSRMatrixT::Assemble, MSRMatrixT.cpp:66) */
@@ -209,7 +216,9 @@ typedef struct tg_newton_params {
   double abs_tol;       /* NLSolver abs_tolerance */
   double div_tol;       /* NLSolver divergence_tolerance */
   int max_iterations;   /* NLSolver max_iterations */
-  int precision;        /* tg_precision */
+  int precision;        /* tg_precision: TG_MIXED runs FP32 tangents and Krylov
+                           vectors with FP64 scalars, and residuals in the
+                           arithmetic of tg_form_residual_precision */
   int precond;          /* tg_precond */
   double lin_rel_tol;   /* inner PCG relative tolerance */
   int lin_max_it;       /* inner PCG iteration cap */
@@ -420,7 +429,8 @@ int tg_timer_stop(tg_context* ctx, double* ms);
 /* average device time of `reps` standalone launches of one hot kernel on the
  * current state: 0 PCG product, 1 PCG vector kernel (the kernels of the form
  * the single-vector solve runs, tg_pcg_form), 2 element tangent, 3 assembly,
- * 4 element residual (+gather) */
+ * 4 element residual (+gather) in FP64, 5 the same in the mixed form's
+ * arithmetic (tg_form_residual_precision) */
 int tg_time_kernel(tg_context* ctx, int which, int reps, double* ms_per_launch);
 
 #ifdef __cplusplus

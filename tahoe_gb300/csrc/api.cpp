@@ -167,6 +167,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->d_Ke32 = nullptr;
   c->d_Ke64 = nullptr;
   c->d_geo = nullptr;
+  c->d_geo_ff = nullptr;
   c->d_xyz = nullptr;
   c->d_blob32 = c->d_blob64 = nullptr;
   c->nseg = 0;
@@ -700,9 +701,13 @@ int tg_traction_forces(int nnd, const double* X, int nel, const int* conn, int n
 }
 
 int tg_form_residual(tg_context* c, double* R_out, double* norm_out) {
-  if (!c || c->nnd <= 0) return TG_ERR_ARG;
+  return tg_form_residual_precision(c, TG_FP64, R_out, norm_out);
+}
+
+int tg_form_residual_precision(tg_context* c, int precision, double* R_out, double* norm_out) {
+  if (!c || c->nnd <= 0 || (precision != TG_FP64 && precision != TG_MIXED)) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
-  int s = launch_residual(c);
+  int s = launch_residual(c, precision == TG_MIXED ? kResidualDoubleFloat : kResidualFP64);
   if (s) return s;
   if (!ok(c, cudaMemcpyAsync(c->h_resid, c->d_resid, sizeof(ResidScalars), cudaMemcpyDeviceToHost, c->stream), "norm"))
     return TG_ERR_CUDA;

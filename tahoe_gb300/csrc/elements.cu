@@ -23,6 +23,7 @@
 
 #include <type_traits>
 
+#include "ff.cuh"
 #include "tg_internal.h"
 
 namespace tg {
@@ -949,8 +950,14 @@ J2View j2view(Context* c) {
 // Reference-configuration shape-function gradients and w det J of every
 // point (the element geometry does not change over a mesh's life: the
 // residual reads them instead of re-forming Jacobians on the FP64 pipe).
+// Formed in FP64 and stored as FP64 planes, or as double-float planes
+// (float2 hi, lo) for the double-float residual.
+__device__ __forceinline__ void put_geo(double* p, double v) { *p = v; }
+__device__ __forceinline__ void put_geo(float2* p, double v) { *p = ff::to_float2(ff::from_double(v)); }
+
+template <typename G>
 __global__ void geometry_kernel(const double* __restrict__ X, int nnd, const int* __restrict__ conn, int nel,
-                                double* __restrict__ geo) {
+                                G* __restrict__ geo) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nip = (long long)nel * 8;
   if (k >= nip) return;
@@ -969,28 +976,51 @@ __global__ void geometry_kernel(const double* __restrict__ X, int nnd, const int
 #pragma unroll
   for (int l = 0; l < 3; ++l)
 #pragma unroll
-    for (int a = 0; a < 8; ++a) geo[(l * 8 + a) * nip + k] = g[l][a];
-  geo[24 * nip + k] = d;
+    for (int a = 0; a < 8; ++a) put_geo(&geo[(l * 8 + a) * nip + k], g[l][a]);
+  put_geo(&geo[24 * nip + k], d);
 }
 
-int residual_impl(Context* c, int commit_state, double* d_ip_sig = nullptr) {
-  if (!c->d_geo) {
-    // formed on first use after a mesh change; without room for it the
-    // kernel forms the gradients itself (bitwise the same values)
-    const size_t n = (size_t)c->nel * 8 * 25;
-    double* g = nullptr;
-    if (cudaMallocAsync((void**)&g, n * sizeof(double), c->stream) == cudaSuccess &&
-        cudaStreamSynchronize(c->stream) == cudaSuccess) {
-      c->allocations.push_back(g);
-      const long long nip = (long long)c->nel * 8;
-      geometry_kernel<<<(unsigned)((nip + 255) / 256), 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->nel, g);
-      c->launches++;
-      if (!ok(c, cudaGetLastError(), "geometry_kernel")) return TG_ERR_CUDA;
-      c->d_geo = g;
-    } else {
-      cudaGetLastError();
-    }
+// the geometry planes of the mesh, formed on first use after a mesh change;
+// without room for them the slot stays empty and the caller goes without
+template <typename G>
+int geometry_planes(Context* c, G*& slot) {
+  if (slot) return TG_OK;
+  const size_t n = (size_t)c->nel * 8 * kGeoPlanes;
+  G* g = nullptr;
+  if (cudaMallocAsync((void**)&g, n * sizeof(G), c->stream) == cudaSuccess &&
+      cudaStreamSynchronize(c->stream) == cudaSuccess) {
+    c->allocations.push_back(g);
+    const long long nip = (long long)c->nel * 8;
+    geometry_kernel<G><<<(unsigned)((nip + 255) / 256), 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->nel, g);
+    c->launches++;
+    if (!ok(c, cudaGetLastError(), "geometry_kernel")) return TG_ERR_CUDA;
+    slot = g;
+  } else {
+    cudaGetLastError();
   }
+  return TG_OK;
+}
+
+// The double-float residual covers the total-Lagrangian Simo group (every
+// block Simo); the other formulations and materials keep the FP64 kernel.
+bool ff_residual_applies(const Context* c) {
+  if (c->mats.formulation != TG_TOTAL_LAGRANGIAN || c->nel <= 0) return false;
+  const int nb = c->have_blocks ? c->mats.nblocks : 1;
+  for (int b = 0; b < nb; ++b)
+    if (c->mats.m[b].kind != TG_MAT_FS_SIMO) return false;
+  return true;
+}
+
+int residual_impl(Context* c, int commit_state, double* d_ip_sig = nullptr, int arith = kResidualFP64) {
+  if (arith == kResidualDoubleFloat && !d_ip_sig && ff_residual_applies(c)) {
+    const int s = geometry_planes(c, c->d_geo_ff);
+    if (s) return s;
+    if (c->d_geo_ff) return launch_residual_ff(c, c->d_geo_ff);
+  }
+  // without room for the planes the kernel forms the gradients itself
+  // (bitwise the same values)
+  const int s = geometry_planes(c, c->d_geo);
+  if (s) return s;
   const int grid = (c->nel + kResElems - 1) / kResElems;
   residual_kernel<<<grid, 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats,
                                                j2view(c), c->iteration, commit_state, c->d_fint, c->d_status,
@@ -1001,12 +1031,12 @@ int residual_impl(Context* c, int commit_state, double* d_ip_sig = nullptr) {
 
 }  // namespace
 
-int launch_residual_commit(Context* c, int commit);
-int launch_residual(Context* c) { return launch_residual_commit(c, 1); }
-int launch_residual_nocommit(Context* c) { return launch_residual_commit(c, 0); }
+int launch_residual_commit(Context* c, int commit, int arith);
+int launch_residual(Context* c, int arith) { return launch_residual_commit(c, 1, arith); }
+int launch_residual_nocommit(Context* c, int arith) { return launch_residual_commit(c, 0, arith); }
 
-int launch_residual_commit(Context* c, int commit) {
-  int s = residual_impl(c, commit);
+int launch_residual_commit(Context* c, int commit, int arith) {
+  int s = residual_impl(c, commit, nullptr, arith);
   if (s) return s;
   const int grid = std::min((c->nnd + 255) / 256, c->partials_cap);
   gather_residual_kernel<<<grid, 256, 0, c->stream>>>(c->nnd, c->d_node_elem_ptr, c->d_node_elem, c->d_fint,

@@ -44,9 +44,16 @@ int check_status(Context* c) {
   return TG_ERR_NAN;
 }
 
+// arithmetic of the residuals a Newton driver forms: the mixed-precision
+// form's are double-float (48 significant bits, on the FP32 pipe), the FP64
+// form's are FP64
+int residual_arith(const tg_newton_params* P) {
+  return P->precision == TG_MIXED ? kResidualDoubleFloat : kResidualFP64;
+}
+
 // residual on the device; returns its norm
-int residual_norm(Context* c, double* norm) {
-  int s = launch_residual(c);
+int residual_norm(Context* c, double* norm, int arith) {
+  int s = launch_residual(c, arith);
   if (s) return s;
   if (!ok(c, cudaMemcpyAsync(c->h_resid, c->d_resid, sizeof(ResidScalars), cudaMemcpyDeviceToHost, c->stream), "norm"))
     return TG_ERR_CUDA;
@@ -414,7 +421,7 @@ int newton_iteration(Context* c, const tg_newton_params* P, double* err, int* it
   if (s) return s;
   c->iteration += 1;
   if (tm) tm->start(c->stream);
-  s = residual_norm(c, err);
+  s = residual_norm(c, err, residual_arith(P));
   if (tm) r->ms_residual += tm->stop(c->stream);
   return s;
 }
@@ -453,7 +460,7 @@ int tg_newton_solve(tg_context* c, const tg_newton_params* P, tg_newton_report* 
   c->iteration = -1;
   tm.start(c->stream);
   double err0 = 0.0;
-  int s = residual_norm(c, &err0);
+  int s = residual_norm(c, &err0, residual_arith(P));
   r.ms_residual += tm.stop(c->stream);
   r.error0 = r.error = err0;
   if (s) {
@@ -513,7 +520,7 @@ int predict(tg_context* c, int n, const int* idx, const double* val, const doubl
   if (set_device(c)) return TG_ERR_CUDA;
   if (pcg_iterations) *pcg_iterations = 0;
   // R(u_old) without committing history, tangent at u_old
-  int s = launch_residual_nocommit(c);
+  int s = launch_residual_nocommit(c, residual_arith(P));
   if (!s) s = check_status(c);
   if (!s) s = form_tangent(c, P->precision);
   if (s) return s;
@@ -655,7 +662,7 @@ int tg_newton_solve_segmented(tg_context* c, const tg_newton_params* P, tg_newto
   std::vector<double> n0(ns), nk(ns);
   double err0 = 0.0;
   tm.start(c->stream);
-  int s = residual_norm(c, &err0);
+  int s = residual_norm(c, &err0, residual_arith(P));
   if (!s) s = tg_segment_residual_norms(c, n0.data());
   r.ms_residual += tm.stop(c->stream);
   r.error0 = r.error = err0;
@@ -790,7 +797,7 @@ int tg_timer_stop(tg_context* c, double* ms) {
 }
 
 int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
-  if (!c || reps <= 0 || !ms || which < 0 || which > 4) return TG_ERR_ARG;
+  if (!c || reps <= 0 || !ms || which < 0 || which > 5) return TG_ERR_ARG;
   if (set_device(c)) return TG_ERR_CUDA;
   if (which <= 1) return time_pcg_kernel(c, which, reps, ms);
   if ((which == 2 || which == 3) && c->tangent_precision < 0) {
@@ -809,7 +816,7 @@ int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
       s = launch_assemble(c, c->tangent_precision);
       if (!s && sym_active(c)) s = sym_convert(c, c->tangent_precision);
     }
-    else s = launch_residual(c);
+    else s = launch_residual(c, which == 5 ? kResidualDoubleFloat : kResidualFP64);
     cudaEventRecord(b, c->stream);
     cudaEventSynchronize(b);
     float e = 0.f;

@@ -210,6 +210,7 @@ struct Context {
   float* d_minv32 = nullptr;    // 18*nnd: Jacobi then block-Jacobi
   double* d_minv64 = nullptr;
   double* d_geo = nullptr;      // 25 planes over nel*8 points: dN/dX (3x8), w det J (residual)
+  float2* d_geo_ff = nullptr;   // the same planes as double-floats (hi, lo), for the double-float residual
   double* d_xyz = nullptr;      // nnd*3: staging of caller (x, y, z) nodal arrays
   float* d_Ke32 = nullptr;      // nel*432: 36 upper node-pair blocks, rows padded to 4
   double* d_Ke64 = nullptr;
@@ -354,7 +355,15 @@ void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void*
 void sym_free(Context* c);
 
 // ---- kernel launchers (elements.cu / assembly.cu / krylov.cu) ----
-int launch_residual(Context* c);          // fint per element + gather + norm
+// Arithmetic of the element residual: FP64, or double-float on the FP32 pipe
+// (about 48 significant bits; total-Lagrangian Simo groups, the others stay
+// FP64).  Chosen by the caller: the mixed-precision Newton drivers use
+// double-float, everything else FP64.
+enum : int { kResidualFP64 = 0, kResidualDoubleFloat = 1 };
+constexpr int kGeoPlanes = 25;  // per point: dN_a/dX_l (24), w det J
+int launch_residual(Context* c, int arith = kResidualFP64);  // fint per element + gather + norm
+// the total-Lagrangian Simo element forces in double-float (residual_ff.cu)
+int launch_residual_ff(Context* c, const float2* d_geo_ff);
 int launch_tangent(Context* c, int precision);   // Ke per element
 int launch_assemble(Context* c, int precision);
 int launch_blob_structure(Context* c, int precision);
@@ -392,7 +401,7 @@ constexpr size_t kScratchPartialBytes = 32768;
 size_t pcg_scratch_bytes(const Context* c);
 int pcg_solve_scratch(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
                       int max_it, int precond, int* iters, double* rel_res);
-int launch_residual_nocommit(Context* c);
+int launch_residual_nocommit(Context* c, int arith = kResidualFP64);
 // output pass (no history written): per point the Cauchy stress and the J2
 // material output (alpha, von Mises, pressure) into d_ip_sig (nel*8*9), the
 // extrapolated, element-averaged nodal values into d_out (nnd*9)

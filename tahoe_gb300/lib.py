@@ -62,6 +62,7 @@ _SIGS = {
                                              ctypes.POINTER(ctypes.c_longlong)]),
     "tg_set_iteration": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_form_residual": (ctypes.c_int, [_vp, _dp, _dp]),
+    "tg_form_residual_precision": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
     "tg_form_tangent": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_get_tangent_csr": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "tg_element_dump": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
@@ -265,10 +266,16 @@ class Context:
         self._chk(self.L.tg_set_iteration(self.h, int(it)), "tg_set_iteration")
 
     # ---- element group ----
-    def residual(self, want_vector=True):
+    def residual(self, want_vector=True, precision=None):
+        """R and ||R||: FP64 (tg_form_residual), or in the arithmetic of the
+        Newton drivers of `precision` (tg_form_residual_precision)."""
         R = np.zeros(self.neq) if want_vector else None
         nrm = ctypes.c_double(0)
-        self._chk(self.L.tg_form_residual(self.h, _d(R), ctypes.byref(nrm)), "tg_form_residual")
+        if precision is None:
+            self._chk(self.L.tg_form_residual(self.h, _d(R), ctypes.byref(nrm)), "tg_form_residual")
+        else:
+            self._chk(self.L.tg_form_residual_precision(self.h, int(precision), _d(R), ctypes.byref(nrm)),
+                      "tg_form_residual_precision")
         return R, nrm.value
 
     def tangent(self, precision):
