@@ -9,8 +9,9 @@ dataset exists).
 A timed step is one Newton iteration of that load step from its start state
 (the prescribed-increment predictor's): FP32 element tangent + deterministic
 block-CSR assembly + Jacobi PCG (the reference's diagonal_matrix; FP32
-vectors, FP64 dots) to the inner tolerance 1e-4 + update + FP64 element
-residual and norm.  Every step starts from the same device snapshot, so the K
+vectors, compensated dot products, FP64 scalars) to the inner tolerance 1e-4
++ update + element residual (double-float element forces, FP64 gather) and
+norm.  Every step starts from the same device snapshot, so the K
 steps do identical work.  The metric is the Newton-step time (ms per
 iteration, lower is better).  Inputs stay resident in HBM; the block-CSR
 matrix (about 290 MB) is larger than the 129 MB L2, so no flush is needed
@@ -201,7 +202,7 @@ def setup_c2(device, precision, precond):
     pred_its = model.apply_step(C2_T, (precision, precond, LIN_TOL))
     ctx = model.ctx
     ctx.set_iteration(-1)
-    ctx.residual(want_vector=False)
+    ctx.residual(want_vector=False, precision=precision)
     ctx.checkpoint()
     return mesh, model, ctx, pred_its
 
@@ -357,7 +358,7 @@ def run_ours(args):
     for _ in range(args.steps):
         ctx.set_u(u_in)
         ctx.set_iteration(-1)
-        ctx.residual(want_vector=False)
+        ctx.residual(want_vector=False, precision=prec)
         ctx.newton_iteration(precision=prec, precond=precond, lin_rel_tol=LIN_TOL)
         ctx.get_u(out=u_out)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -365,7 +366,7 @@ def run_ours(args):
     # back to the step-start snapshot for the kernel timings below
     ctx.set_u(u0)
     ctx.set_iteration(-1)
-    ctx.residual(want_vector=False)
+    ctx.residual(want_vector=False, precision=prec)
     ctx.checkpoint()
 
     # per-kernel device times (CUDA events on the context stream)
@@ -765,6 +766,7 @@ def run_kernel_only(args):
     ctx.set_iteration(-1)
     ctx.residual(want_vector=False)
     ctx.tangent(prec)
+    ctx.time_kernel(KERNELS[args.kernel], 1)  # warm-up: forms what the kernel's first use forms
     ms = ctx.time_kernel(KERNELS[args.kernel], args.launches)
     print(json.dumps({"kernel": args.kernel, "n": args.n, "precision": args.precision, "launches": args.launches,
                       "ms_per_launch": ms, "block_nnz": ctx.block_nnz, "nodes": mesh.nnd, "elements": mesh.nel}))

@@ -680,21 +680,43 @@ __device__ __forceinline__ void slot_pair(int slot, int& a, int& b) {
 // instantiation that needs them, so the other formulations keep their
 // register budget)
 constexpr int kTanH = 21;  // per (point, node): D B_b (18 values) and sigma grad N_b (3)
+// Per-element stride of the h_b tile: 64 x kTanH values and 64 bytes, so the
+// tiles of consecutive elements start 16 banks apart.  A warp of the slot
+// phase holds lanes of two elements (36 slots each); with a stride of a
+// multiple of 32 banks, lanes of both reading the same node b collided.
+template <typename T>
+__host__ __device__ constexpr int tan_h_stride() {
+  return 64 * kTanH + 64 / (int)sizeof(T);
+}
+
+// CTAs per SM the FP32 tangent is compiled for (72 registers at 8 elements
+// per CTA, a few spilled): the per-point phase runs on 64 of the 288 threads
+// while the others wait at its barrier, so resident CTAs, whose phases
+// interleave, set the throughput.  Measured on the 64^3 block: 0.60 ms at two
+// CTAs per SM, 0.49 ms at three; the per-point phase kept in registers (its
+// moduli formed in shared memory instead, to avoid the spills: 0.52 ms); 7
+// elements per CTA at 80 registers: 0.57 ms.  The FP64 tangent keeps the
+// compiler's choice.
+template <typename T>
+constexpr int kTanMinBlocks = sizeof(T) == 4 ? 3 : 1;
 
 template <typename T, int kTanElems, bool UL>
-__global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const double* __restrict__ X, int nnd,
+__global__ void __launch_bounds__(kTanElems * kSlots, kTanMinBlocks<T>) tangent_kernel(const double* __restrict__ X, int nnd,
                                                               const int* __restrict__ conn,
                                                               const int8_t* __restrict__ blk, int nel,
                                                               const double4_32a* __restrict__ u, MatTable mt,
                                                               J2View j2, T* __restrict__ Ke, int* status) {
   __shared__ T sX[kTanElems][8][3];
   __shared__ T sU[kTanElems][8][3];
-  __shared__ T sG[kTanElems][8][3][8];  // per point spatial gradients
+  // per point spatial gradients; the ninth point row is padding that puts
+  // consecutive elements 24 banks apart (see tan_h_stride)
+  __shared__ T sG[kTanElems][9][3][8];
   __shared__ T sD[kTanElems][8][36];    // per point moduli (scaled)
   __shared__ T sS[kTanElems][8][6];     // per point Cauchy stress (scaled, TL only)
   __shared__ T sW[kTanElems][8];        // per point w det J (B-bar mean gradients)
   __shared__ T sM[kTanElems][3][8];     // element-mean gradients (B-bar)
-  // dynamic: [kTanElems][8 points][8 nodes][kTanH] per-node products h_b
+  // dynamic: per element (stride tan_h_stride) [8 points][8 nodes][kTanH]
+  // per-node products h_b
   extern __shared__ __align__(16) unsigned char tan_dyn[];
   const int tid = threadIdx.x;
   const int e0 = blockIdx.x * kTanElems;
@@ -827,7 +849,8 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
   // gradients: the h_b a slot used to form for itself are shared by the
   // slots of the same b (54 of the ~93 FMA a slot spent per point).
   const bool tl = mt.formulation != TG_SMALL_STRAIN;  // geometric stiffness (TL and UL)
-  T(*sH)[8][8][kTanH] = reinterpret_cast<T(*)[8][8][kTanH]>(tan_dyn);
+  T* const sH = reinterpret_cast<T*>(tan_dyn);
+  auto h_at = [&](int el, int ip, int b) { return sH + el * tan_h_stride<T>() + (ip * 8 + b) * kTanH; };
   for (int item = tid; item < kTanElems * 64; item += blockDim.x) {
     const int hl = item >> 6, ip = (item >> 3) & 7, b = item & 7;
     if (e0 + hl >= nel) continue;
@@ -850,7 +873,7 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
         for (int j = 0; j < 3; ++j) h[V][j] += fb[j] * ds;
       }
     }
-    T* out = sH[hl][ip][b];
+    T* out = h_at(hl, ip, b);
 #pragma unroll
     for (int V = 0; V < 6; ++V)
 #pragma unroll
@@ -874,7 +897,7 @@ __global__ void __launch_bounds__(kTanElems * kSlots) tangent_kernel(const doubl
   for (int k = 0; k < 9; ++k) K[k] = T(0);
   for (int ip = 0; ip < 8; ++ip) {
     const T ga[3] = {sG[le][ip][0][a], sG[le][ip][1][a], sG[le][ip][2][a]};
-    const T* h = sH[le][ip][b];
+    const T* h = h_at(le, ip, b);
     // K(i,j) += sum_m ga[m] h[vgt(i,m)][j]
     if (bbar) {
       const T fa[3] = {(sM[le][0][a] - ga[0]) / T(3), (sM[le][1][a] - ga[1]) / T(3), (sM[le][2][a] - ga[2]) / T(3)};
@@ -1095,12 +1118,15 @@ int launch_nodal_stress(Context* c, double* d_ip_sig, double* d_out) {
 template <typename T, int EPB, bool UL>
 void launch_tangent_t(Context* c, T* Ke) {
   const int grid = (c->nel + EPB - 1) / EPB;
-  const size_t dyn = (size_t)EPB * 64 * kTanH * sizeof(T);
+  const size_t dyn = (size_t)EPB * tan_h_stride<T>() * sizeof(T);
   // the per-node products exceed the default dynamic shared memory for some
   // shapes; the attribute belongs to the function on the current device
   // (the same value for every caller), set at every launch -- a tangent is
   // formed once per Newton iteration
   cudaFuncSetAttribute(tangent_kernel<T, EPB, UL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  // three CTAs of 8 elements hold about 190 KB of shared memory
+  cudaFuncSetAttribute(tangent_kernel<T, EPB, UL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
   tangent_kernel<T, EPB, UL><<<grid, EPB * kSlots, dyn, c->stream>>>(
       c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats, j2view(c), Ke, c->d_status);
 }
