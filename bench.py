@@ -317,6 +317,8 @@ def run_ours(args):
     prec = lib.MIXED if args.precision == "mixed" else lib.FP64
     precond = lib.PRECOND_BLOCK_JACOBI if args.precond == "block" else lib.PRECOND_JACOBI
     mesh, model, ctx, pred_its = setup_c2(local, prec, precond)
+    if args.form is not None:
+        ctx.pcg_form(args.form)
     tuning = None
     if not args.no_tune:
         # launch shapes picked by the autotuner on this mesh and state
@@ -383,16 +385,19 @@ def run_ours(args):
     nnzb = ctx.block_nnz
     sym = bool(getattr(ctx, "sym_mode", 0))
     product = ctx.product_kernel()
-    cg = product == "pcg_cg_spmv_kernel"
-    prof = {"pcg_spmv_sym_kernel": "pcg_spmv_sym_c2_64cubed.md", "pcg_cg_spmv_kernel": "pcg_cg_spmv_c2_64cubed.md"}.get(
-        product, "pcg_spmv_c2_64cubed.md")
-    bytes_spmv = (workloads.spmv_bytes_sym if sym else workloads.spmv_bytes)(nnzb, nnd, s_val)
+    push = product == "pcg_cg_push_kernel"
+    cg = product == "pcg_cg_spmv_kernel" or push
+    prof = {"pcg_spmv_sym_kernel": "pcg_spmv_sym_c2_64cubed.md", "pcg_cg_spmv_kernel": "pcg_cg_spmv_c2_64cubed.md",
+            "pcg_cg_push_kernel": "pcg_cg_push_c2_64cubed.md"}.get(product, "pcg_spmv_c2_64cubed.md")
+    bytes_spmv = (workloads.spmv_bytes_push if push else workloads.spmv_bytes_sym if sym else
+                  workloads.spmv_bytes)(nnzb, nnd, s_val)
     peak, peak_kind = peaks()
     achieved = bytes_spmv / (t_spmv * 1e-3) / 1e9
     elements_per_s = mesh.nel / ((t_tan + t_asm) * 1e-3)
     # the other HBM-bound kernels of the step, same peak and byte model
     other_rooflines = {}
-    vec = ("pcg_cg_vector_kernel", workloads.cg_vector_bytes(nnd, s_val), t_upd) if cg else \
+    vec = ("pcg_cg_vector_kernel", workloads.cg_vector_bytes_push(nnzb, nnd, s_val) if push else
+           workloads.cg_vector_bytes(nnd, s_val), t_upd) if cg else \
         ("pcg_update_kernel", workloads.update_bytes(nnd, s_val), t_upd)
     for name, b, t in (("assemble_kernel", workloads.assembly_bytes(mesh.nel, nnzb, nnd, s_val), t_asm), vec):
         a = b / (t * 1e-3) / 1e9
@@ -417,7 +422,10 @@ def run_ours(args):
         "pcg_iterations_per_step": float(np.mean(pcg_its)),
         "predictor_pcg_iterations": pred_its,
         "elements_assembled_per_s": round(elements_per_s, 1),
-        "pcg_form": "single-reduction (Chronopoulos-Gear), programmatic launch" if cg else "textbook",
+        "pcg_form": {0: "textbook", 1: "single-reduction (Chronopoulos-Gear), programmatic launch",
+                     2: "single-reduction (Chronopoulos-Gear)",
+                     3: "single-reduction (Chronopoulos-Gear), programmatic launch, symmetric push storage"}.get(
+                         getattr(ctx, "form", 1), "textbook"),
         "kernel_ms": {"pcg_product": round(t_spmv, 5), "pcg_vector": round(t_upd, 5), "tangent": round(t_tan, 4),
                       "assembly": round(t_asm, 4), "residual": round(t_res, 4),
                       "residual_fp64": round(t_res64, 4)},
@@ -766,6 +774,8 @@ def run_kernel_only(args):
     ctx.set_iteration(-1)
     ctx.residual(want_vector=False)
     ctx.tangent(prec)
+    if args.form is not None:
+        ctx.pcg_form(args.form)
     ctx.time_kernel(KERNELS[args.kernel], 1)  # warm-up: forms what the kernel's first use forms
     ms = ctx.time_kernel(KERNELS[args.kernel], args.launches)
     print(json.dumps({"kernel": args.kernel, "n": args.n, "precision": args.precision, "launches": args.launches,
@@ -783,6 +793,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes, no autotuning")
     ap.add_argument("--kernel", choices=sorted(KERNELS), help="time standalone launches of one kernel only")
+    ap.add_argument("--form", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="single-vector PCG form (tg_pcg_form); default the library's")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--n", type=int, default=64, help="mesh size per side for --kernel")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])

@@ -395,8 +395,15 @@ int tg_spmv_release(tg_context* ctx, int per_warp);
  * last-block reduction; vector update with a grid barrier between its two
  * passes).  All solve the same (block-)Jacobi CG system to the same
  * tolerance; forms 1 and 2 take bitwise the same iterates, form 0 differs
- * from them by rounding.  The symmetric format, segmented batches and the
- * no-allocation entry point use their own kernels. */
+ * from them by rounding.  form = 3: form 1 on the symmetric push storage --
+ * the product streams the upper node blocks only (about 55 % of the full
+ * storage's bytes) and stores each off-diagonal block's transposed product
+ * in a slot of its lower row, which the vector kernel adds in a fixed order
+ * (bitwise repeatable; it differs from form 1 by rounding).  The storage is
+ * built on the device on first use after a mesh change and its values are
+ * copied from every new assembly.  The symmetric format of
+ * tg_spmv_symmetric, segmented batches and the no-allocation entry point use
+ * their own kernels. */
 int tg_pcg_form(tg_context* ctx, int form);
 /* L2 priorities of the streamed matrix.  bytes >= 0: the leading whole
  * tiles within `bytes` of the matrix storage are copied with evict_last

@@ -179,6 +179,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->d_row_tile = nullptr;
   c->d_tile_row = nullptr;
   c->sym = SymStore{};  // its buffers went back to the pool with the mesh
+  c->push = PushStore{};
   c->d_minv32 = nullptr;
   c->d_minv64 = nullptr;
   c->d_block = nullptr;
@@ -473,12 +474,14 @@ int tg_spmv_release(tg_context* c, int per_warp) {
 }
 
 int tg_pcg_form(tg_context* c, int form) {
-  if (!c || form < 0 || form > 2) return TG_ERR_ARG;
+  if (!c || form < 0 || form > 3) return TG_ERR_ARG;
   c->pcg_form = form == 0 ? 0 : 1;
-  const int pdl = form == 1 ? 1 : 0;
-  if (pdl != c->cg_pdl) {
+  const int pdl = form == 1 || form == 3 ? 1 : 0;
+  const int push = form == 3 ? 1 : 0;
+  if (pdl != c->cg_pdl || push != c->cg_push) {
     c->cg_pdl = pdl;
-    drop_graphs(c);  // the captured chunk bakes in its launch dependencies
+    c->cg_push = push;
+    drop_graphs(c);  // the captured chunk bakes in its launch dependencies and storage
   }
   return TG_OK;
 }

@@ -223,6 +223,38 @@ __device__ __forceinline__ uint64_t l2_policy_evict_last() {
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
   return pol;
 }
+// global stores and loads of node vectors with an L2 cache policy
+__device__ __forceinline__ void st_hint(float4* p, const float4& v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_hint(double4_32a* p, const double4_32a& v, uint64_t pol) {
+  double* d = reinterpret_cast<double*>(p);
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(d), "d"(v.x), "d"(v.y), "l"(pol)
+               : "memory");
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(d + 2), "d"(v.z), "d"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ float4 ld_hint(const float4* p, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double4_32a ld_hint(const double4_32a* p, uint64_t pol) {
+  double4_32a v;
+  const double* d = reinterpret_cast<const double*>(p);
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(d), "l"(pol));
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.z), "=d"(v.w) : "l"(d + 2), "l"(pol));
+  return v;
+}
+// drops a 128-byte L2 line without writing it back (its data is dead)
+__device__ __forceinline__ void l2_discard(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
 __device__ __forceinline__ void bulk_copy_hint(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar,
                                                uint64_t pol) {
   asm volatile(

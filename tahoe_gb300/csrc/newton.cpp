@@ -110,6 +110,7 @@ int form_tangent(Context* c, int precision) {
   }
   int s = launch_tangent(c, precision);
   if (!s) s = launch_assemble(c, precision);
+  if (!s) ++c->tangent_serial;
   // the symmetric stream format of the single-vector product
   if (!s && sym_active(c)) s = sym_convert(c, precision);
   if (!s) s = check_status(c);
@@ -814,6 +815,7 @@ int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
     if (which == 2) s = launch_tangent(c, c->tangent_precision);
     else if (which == 3) {
       s = launch_assemble(c, c->tangent_precision);
+      if (!s) ++c->tangent_serial;
       if (!s && sym_active(c)) s = sym_convert(c, c->tangent_precision);
     }
     else s = launch_residual(c, which == 5 ? kResidualDoubleFloat : kResidualFP64);

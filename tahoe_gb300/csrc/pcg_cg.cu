@@ -66,39 +66,135 @@ constexpr int kCgPartials = 4 * kVecCap;
 __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-// The product: w = A u and the CTA partials of u.w on a persistent grid of
-// 256-thread CTAs (as many as fit, a few per SM).  CTA b streams tiles b,
+// The rows of one staged tile of the symmetric push storage (pushfmt.cu):
+// LPR lanes per row, each taking every LPR-th upper block of the row, the
+// first K of them with every load issued before any use.  A block adds
+// A_IJ u_J to the row's upper sum y_I; an off-diagonal block also stores
+// A_IJ^T u_I at its push slot (row J's share of the product, added by the
+// vector kernel).  The row's first block is its diagonal (its first lane),
+// so u.w of the whole matrix is the sum over rows of u_I.(2 y_I - A_II u_I).
+template <typename T, int LPR>
+__device__ __forceinline__ void push_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
+                                               const typename Vec4<T>::type* __restrict__ uv,
+                                               typename Vec4<T>::type* __restrict__ wup,
+                                               typename Vec4<T>::type* __restrict__ push, Acc<T>& dot) {
+  using V = typename Vec4<T>::type;
+  constexpr int RPW = 32 / LPR;  // rows per warp pass
+  constexpr int K = 4;
+  const int sub = lane % LPR, grp = lane / LPR;
+  const int* hdr = reinterpret_cast<const int*>(base);
+  const int r0 = hdr[0], nrows = hdr[1], nb = hdr[2], ps = hdr[3];
+  const int* rp = hdr + 4;
+  const int* cl = rp + ceil4(nrows + 1);
+  const int* sl = cl + ceil4(nb);
+  const T* pl = reinterpret_cast<const T*>(sl + ceil4(nb));
+  // the pushes stay in L2 for the vector kernel that reads them next
+  const uint64_t keep = l2_policy_evict_last();
+  for (int li = warp * RPW + grp; li - grp < nrows; li += nwarps * RPW) {
+    const bool live = li < nrows;
+    const int I = r0 + li;
+    V ui = mk<V, T>(T(0), T(0), T(0));
+    if (live) ui = uv[I];
+    const int e0 = live ? rp[li] : 0, e1 = live ? rp[li + 1] : 0;
+    T a0 = T(0), a1 = T(0), a2 = T(0), d0 = T(0), d1 = T(0), d2 = T(0);
+    auto block = [&](int j, const V& uj) {
+      const T* vv = pl + j;
+      const T m0 = vv[0 * ps], m1 = vv[1 * ps], m2 = vv[2 * ps], m3 = vv[3 * ps], m4 = vv[4 * ps],
+              m5 = vv[5 * ps], m6 = vv[6 * ps], m7 = vv[7 * ps], m8 = vv[8 * ps];
+      const T b0 = m0 * uj.x + m1 * uj.y + m2 * uj.z;
+      const T b1 = m3 * uj.x + m4 * uj.y + m5 * uj.z;
+      const T b2 = m6 * uj.x + m7 * uj.y + m8 * uj.z;
+      a0 += b0;
+      a1 += b1;
+      a2 += b2;
+      if (j == e0) {
+        d0 = b0;
+        d1 = b1;
+        d2 = b2;
+      } else {
+        st_hint(push + sl[j],
+                mk<V, T>(m0 * ui.x + m3 * ui.y + m6 * ui.z, m1 * ui.x + m4 * ui.y + m7 * ui.z,
+                         m2 * ui.x + m5 * ui.y + m8 * ui.z),
+                keep);
+      }
+    };
+    {
+      int Jk[K];
+      V pk[K];
+#pragma unroll
+      for (int u = 0; u < K; ++u) {
+        const int j = e0 + sub + LPR * u;
+        Jk[u] = j < e1 ? cl[j] : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < K; ++u)
+        if (Jk[u] >= 0) pk[u] = uv[Jk[u]];
+#pragma unroll
+      for (int u = 0; u < K; ++u)
+        if (Jk[u] >= 0) block(e0 + sub + LPR * u, pk[u]);
+    }
+    for (int j = e0 + sub + LPR * K; j < e1; j += LPR) block(j, uv[cl[j]]);
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (live && sub == 0) {
+      wup[I] = mk<V, T>(a0, a1, a2);
+      dot.add_prod(ui.x, T(2) * a0 - d0);
+      dot.add_prod(ui.y, T(2) * a1 - d1);
+      dot.add_prod(ui.z, T(2) * a2 - d2);
+    }
+  }
+}
+
+constexpr int kPushLanes = 4;  // lanes per row of the push product (upper rows hold about 14 blocks)
+constexpr bool kPushDiscard = true;  // read push lines are dropped from L2 without write-back
+
+// The product on a persistent grid of 256-thread CTAs (as many as fit, a
+// few per SM): w = A u and the CTA partials of u.w, with the matrix in the
+// full storage (PUSH false) or the symmetric push storage (PUSH true: w holds
+// the upper part, push the lower part's slots).  CTA b streams tiles b,
 // b + G, ... through a ring of NST shared-memory stages filled by bulk
-// copies on mbarriers, issued NST - 1 tiles ahead; eight warps take each
-// tile's rows (8 lanes per row).  The CTA's u.w is reduced in a fixed order
-// into its partial.  Every wait is bounded; a timeout flags the solve broken
-// down in both scalar states and drains the copies in flight.  (Measured on
-// C2: four such CTAs per SM stream the matrix faster than one CTA of four
-// groups sharing the SM's tiles, and faster than tiles pulled from a global
+// copies on mbarriers (each stage refilled as soon as every warp is done with
+// it); eight warps take each tile's rows.  The CTA's u.w is reduced in a
+// fixed order into its partial.
+// Every wait is bounded; a timeout flags the solve broken down in both
+// scalar states and drains the copies in flight.  (Measured on C2: four
+// such CTAs per SM stream the matrix faster than one CTA of four groups
+// sharing the SM's tiles, and faster than tiles pulled from a global
 // counter; the spread of finishing times is per SM, not per tile count.)
-template <typename T, int NST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
-    pcg_cg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off, const unsigned char* __restrict__ blob,
-                       int cap, int keep, const typename Vec4<T>::type* __restrict__ p,
-                       typename Vec4<T>::type* __restrict__ q, typename Partial<T>::type* __restrict__ cta_part,
-                       PcgScalars* sc, int* status) {
+template <typename T, int NST, bool PUSH>
+__device__ __forceinline__ void cg_product(int ntiles, const long long* __restrict__ blob_off,
+                                           const unsigned char* __restrict__ blob, int cap, int keep,
+                                           const typename Vec4<T>::type* __restrict__ p,
+                                           typename Vec4<T>::type* __restrict__ q,
+                                           typename Vec4<T>::type* __restrict__ push,
+                                           typename Partial<T>::type* __restrict__ cta_part, PcgScalars* sc,
+                                           int* status) {
   using P = typename Partial<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
+  __shared__ int released[NST];  // warps done with the stage, over the whole launch
+  __shared__ int nissued[NST];   // copies issued into the stage
   __shared__ int abort_flag;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NST; ++k) mbar_init(&bars[k], 1);
+    for (int k = 0; k < NST; ++k) {
+      mbar_init(&bars[k], 1);
+      released[k] = 0;
+      nissued[k] = 0;
+    }
     fence_mbar_init();
     abort_flag = 0;
   }
   __syncthreads();
   const int t0 = blockIdx.x, G = gridDim.x;
-  int issued = 0;  // positions issued (thread 0)
-  auto issue = [&](int t) {
-    const int st = issued % NST;
-    ++issued;
+  // tile t into stage st (one thread)
+  auto issue = [&](int t, int st) {
+    nissued[st] += 1;
     const long long o0 = blob_off[t], o1 = blob_off[t + 1];
     const unsigned bytes = (unsigned)(o1 - o0);
     mbar_expect_tx(&bars[st], bytes);
@@ -108,42 +204,59 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
       bulk_copy_hint(smem + (size_t)st * cap, blob + o0, bytes, &bars[st],
                      t < keep ? l2_policy_evict_last() : l2_policy_evict_first());
   };
-  // the first tiles (the matrix does not depend on the last vector kernel)
+  // copies still in flight complete before the CTA leaves (bounded waits;
+  // at most one copy per stage can be pending)
+  auto drain = [&]() {
+#pragma unroll
+    for (int k = 0; k < NST; ++k)
+      if (nissued[k] > 0) mbar_wait(&bars[k], (unsigned)((nissued[k] - 1) & 1), kWaitLimit);
+  };
+  // the first NST tiles (the matrix does not depend on the last vector kernel)
   if (threadIdx.x == 0)
-    for (int k = 0; k < NST - 1 && t0 + k * G < ntiles; ++k) issue(t0 + k * G);
+    for (int k = 0; k < NST && t0 + k * G < ntiles; ++k) issue(t0 + k * G, k);
   griddep_wait();  // u and the scalars of the last vector kernel
   griddep_launch();
   if (skip_launch(sc, 1)) {
-    if (threadIdx.x == 0)  // the staged copies complete before the CTA leaves
-      for (int q2 = 0; q2 < issued; ++q2) mbar_wait(&bars[q2 % NST], (unsigned)((q2 / NST) & 1), kWaitLimit);
+    if (threadIdx.x == 0) drain();
     return;
   }
+  // Each warp takes its rows of every staged tile without waiting for the
+  // other warps: the warp that finishes a stage last refills it with the
+  // CTA's tile NST positions ahead (release: each warp's reads of the stage
+  // happen before its count; the last counter orders them before the bulk
+  // copy through the proxy fence).  A CTA barrier per tile made every warp
+  // wait for the slowest one (the largest stall of the product).
   Acc<T> v;
   int it = 0;
-  bool stuck = false;
   for (int t = t0; t < ntiles; ++it, t += G) {
     const int s = it % NST;
-    const int tn = t + (NST - 1) * G;
-    if (threadIdx.x == 0 && tn < ntiles) {
-      fence_async_smem();  // the stage was last read through generic loads
-      issue(tn);
+    if (!mbar_wait(&bars[s], (unsigned)((it / NST) & 1), kWaitLimit)) atomicOr(&abort_flag, 1);
+    __syncwarp();
+    if (*(volatile int*)&abort_flag) break;
+    if (PUSH)
+      push_tile_rows<T, kPushLanes>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, push, v);
+    else
+      spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v, nullptr);
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      const int done = atomicAdd(&released[s], 1);
+      if (done == (it / NST + 1) * nwarps - 1) {  // the last warp of this use of the stage
+        __threadfence_block();
+        const int tn = t + NST * G;
+        if (tn < ntiles) {
+          fence_async_smem();  // the stage was last read through generic loads
+          issue(tn, s);
+        }
+      }
     }
-    if (!mbar_wait(&bars[s], (unsigned)((it / NST) & 1), kWaitLimit)) {
-      if (lane == 0) atomicOr(&abort_flag, 1);
-    }
-    __syncthreads();
-    if (abort_flag) {
-      stuck = true;
-      break;
-    }
-    spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v, nullptr);
-    __syncthreads();  // stage s is free for the copy issued next iteration
   }
-  if (stuck && threadIdx.x == 0) {
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0) {
     // a staged tile never completed: record it, drain the copies still in
-    // flight (bounded waits) and flag the solve broken down
+    // flight and flag the solve broken down
     atomicOr(status, kStatusWaitTimeout);
-    for (int q2 = it; q2 < issued; ++q2) mbar_wait(&bars[q2 % NST], (unsigned)((q2 / NST) & 1), kWaitLimit);
+    drain();
     sc[0].done = sc[1].done = 2;
     sc[0].fail = sc[1].fail = 5;
   }
@@ -151,6 +264,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
   P bt[1];
   block_total_acc<T, 1>(vv, bt);
   if (threadIdx.x == 0) cta_part[blockIdx.x] = bt[0];
+}
+
+template <typename T, int NST>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
+    pcg_cg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off, const unsigned char* __restrict__ blob,
+                       int cap, int keep, const typename Vec4<T>::type* __restrict__ p,
+                       typename Vec4<T>::type* __restrict__ q, typename Vec4<T>::type* __restrict__ push,
+                       typename Partial<T>::type* __restrict__ cta_part, PcgScalars* sc, int* status) {
+  cg_product<T, NST, false>(ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, sc, status);
+}
+
+template <typename T, int NST>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
+    pcg_cg_push_kernel(int ntiles, const long long* __restrict__ blob_off, const unsigned char* __restrict__ blob,
+                       int cap, int keep, const typename Vec4<T>::type* __restrict__ p,
+                       typename Vec4<T>::type* __restrict__ q, typename Vec4<T>::type* __restrict__ push,
+                       typename Partial<T>::type* __restrict__ cta_part, PcgScalars* sc, int* status) {
+  cg_product<T, NST, true>(ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, sc, status);
 }
 
 // One CTA per SM, one node per thread per pass: 1024 (FP32, 64 registers)
@@ -162,15 +293,58 @@ struct CgShape {
   static constexpr int threads = sizeof(T) == 4 ? 1024 : 512;
 };
 
-template <typename T>
+//
+// With the symmetric push storage (PUSH) the product's w holds the upper
+// part of A u only: a node's w is completed here from its push slots, added
+// in slot order, with the dofs of prescribed rows left out (the stored upper
+// blocks keep their prescribed columns, whose transposes would reach them).
+template <typename T, bool PUSH>
 __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
     int nnd, const T* __restrict__ minv, typename Vec4<T>::type* __restrict__ x,
     typename Vec4<T>::type* __restrict__ r, typename Vec4<T>::type* __restrict__ u,
     typename Vec4<T>::type* __restrict__ p, typename Vec4<T>::type* __restrict__ s,
     const typename Vec4<T>::type* __restrict__ w, const typename Partial<T>::type* __restrict__ dpart, int ndp,
-    double* vpart, PcgScalars* sc) {
+    double* vpart, PcgScalars* sc, const typename Vec4<T>::type* __restrict__ push, const int* __restrict__ lptr,
+    const uint8_t* __restrict__ mask, int pstride) {
   using V = typename Vec4<T>::type;
   using P = typename Partial<T>::type;
+  // w of node n: the product's value, plus the pushed lower part
+  // Node n's pushes are rank planes of pstride slots, read coalesced and in
+  // rank order.  Read, a plane line is dead until the next product writes it:
+  // once all eight nodes of a 128-byte line have their values (the warp
+  // converges first), the first of them discards the line, so the L2 never
+  // writes dead pushes back to DRAM.  Called by whole warps (n < nnd or not).
+  auto w_of = [&](int n) {
+    V wv = mk<V, T>(T(0), T(0), T(0));
+    if (n < nnd) wv = w[n];
+    if (PUSH) {
+      const uint64_t keep = l2_policy_evict_last();
+      T s0 = T(0), s1 = T(0), s2 = T(0);
+      const int cnt = n < nnd ? lptr[n + 1] - lptr[n] : 0;
+#pragma unroll 4
+      for (int k = 0; k < cnt; ++k) {
+        const V pv = ld_hint(push + ((long long)k * pstride + n), keep);
+        s0 += pv.x;
+        s1 += pv.y;
+        s2 += pv.z;
+      }
+      if (n < nnd) {
+        const uint8_t m = mask[n];
+        wv = mk<V, T>(wv.x + ((m & 1) ? s0 : T(0)), wv.y + ((m & 2) ? s1 : T(0)), wv.z + ((m & 4) ? s2 : T(0)));
+      }
+      if (kPushDiscard) {
+        // the line's largest rank count, over its eight nodes (one warp)
+        int lc = cnt;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) lc = max(lc, __shfl_xor_sync(0xffffffffu, lc, o));
+        __syncwarp();
+        constexpr int kLine = 128 / (int)sizeof(V);  // slots per line
+        if ((n % kLine) == 0)
+          for (int k = 0; k < lc; ++k) l2_discard(push + ((long long)k * pstride + n));
+      }
+    }
+    return wv;
+  };
   __shared__ double coef[2];  // alpha, beta
   __shared__ int go;
   // the first pass's node vectors: the product this kernel waits for writes
@@ -199,7 +373,7 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
   __shared__ PcgScalars so;  // kept in shared memory: registers stay free for the vector pass
   if (threadIdx.x == 0) so = *sc;
   V w0;
-  if (n0 < nnd) w0 = w[n0];  // in flight while the scalars are formed
+  w0 = w_of(n0);  // in flight while the scalars are formed
   const int nb = gridDim.x;  // at most one partial of each buffer per thread
   P g0{}, g1{}, q0{}, q1{};
   if ((int)threadIdx.x < nb) {
@@ -308,14 +482,17 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
     acc[1].add_prod(ry, ry);
     acc[1].add_prod(rz, rz);
   };
-  const int step = gridDim.x * blockDim.x;
+  const int step = gridDim.x * blockDim.x;  // a multiple of 32: warps stay whole
   if (n0 < nnd) update(n0, u0, w0, p0, s0, x0, r0, B0);
-  for (int n = n0 + step; n < nnd; n += step) {
-    const V un = u[n], wn = w[n], pn = p[n], sn = s[n], xn = x[n], rn = r[n];
-    T B[9];
+  for (int n = n0 + step; n - (int)(threadIdx.x & 31) < nnd; n += step) {
+    const V wn = w_of(n);
+    if (n < nnd) {
+      const V un = u[n], pn = p[n], sn = s[n], xn = x[n], rn = r[n];
+      T B[9];
 #pragma unroll
-    for (int m = 0; m < 9; ++m) B[m] = minv[(long long)n * 9 + m];
-    update(n, un, wn, pn, sn, xn, rn, B);
+      for (int m = 0; m < 9; ++m) B[m] = minv[(long long)n * 9 + m];
+      update(n, un, wn, pn, sn, xn, rn, B);
+    }
   }
   P bt[2];
   block_total_acc<T, 2>(acc, bt);
@@ -326,16 +503,59 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
 }
 
 // as many CTAs as are resident at once (grid-stride over the nodes)
-template <typename T>
+template <typename T, bool PUSH>
 int vec_grid(Context* c, int* grid) {
   int per_sm = 0;
-  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_cg_vector_kernel<T>, CgShape<T>::threads, 0),
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_cg_vector_kernel<T, PUSH>,
+                                                           CgShape<T>::threads, 0),
           "occupancy"))
     return TG_ERR_CUDA;
   const int per = CgShape<T>::threads;
   // at most one CTA per thread of a CTA: each thread loads at most one of
   // the previous vector kernel's partials of each kind
   *grid = std::max(1, std::min({(c->nnd + per - 1) / per, c->num_sms * std::max(per_sm, 1), kVecCap, per}));
+  return TG_OK;
+}
+
+// The matrix storage the product streams: the full-storage tiles, or the
+// symmetric push storage (tg_pcg_form 3) with its push buffer and slot
+// pointers; the push storage's values are brought up to the last assembly.
+template <typename T>
+struct CgStore {
+  bool push = false;
+  int ntiles = 0;
+  long long cap = 0;
+  const std::vector<long long>* h_off = nullptr;
+  const long long* off = nullptr;
+  const unsigned char* blob = nullptr;
+  typename Vec4<T>::type* pushbuf = nullptr;
+  const int* lptr = nullptr;
+  int pstride = 0;
+};
+
+template <typename T>
+int cg_store(Context* c, CgStore<T>& st) {
+  const bool f32 = std::is_same<T, float>::value;
+  st.push = c->cg_push != 0;
+  if (!st.push) {
+    st.ntiles = c->ntiles;
+    st.cap = f32 ? c->blob_cap32 : c->blob_cap64;
+    st.h_off = f32 ? &c->h_blob_off32 : &c->h_blob_off64;
+    st.off = f32 ? c->d_blob_off32 : c->d_blob_off64;
+    st.blob = f32 ? c->d_blob32 : c->d_blob64;
+    return TG_OK;
+  }
+  const int s = push_prepare(c, f32 ? TG_MIXED : TG_FP64);
+  if (s) return s;
+  const PushStore& ps = c->push;
+  st.ntiles = ps.ntiles;
+  st.cap = f32 ? ps.cap32 : ps.cap64;
+  st.h_off = f32 ? &ps.h_off32 : &ps.h_off64;
+  st.off = f32 ? ps.d_off32 : ps.d_off64;
+  st.blob = f32 ? ps.d_blob32 : ps.d_blob64;
+  st.pushbuf = reinterpret_cast<typename Vec4<T>::type*>(f32 ? ps.d_push32 : ps.d_push64);
+  st.lptr = ps.d_lptr;
+  st.pstride = ps.pstride;
   return TG_OK;
 }
 
@@ -348,15 +568,18 @@ struct CgProduct {
 };
 
 template <typename T>
-int product_shape(Context* c, CgProduct& pr) {
-  const bool f32 = std::is_same<T, float>::value;
-  pr.cap = (int)(((f32 ? c->blob_cap32 : c->blob_cap64) + 127) / 128 * 128);
+int product_shape(Context* c, const CgStore<T>& st, CgProduct& pr) {
+  pr.cap = (int)((st.cap + 127) / 128 * 128);
   int optin = 0;
   if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
     return TG_ERR_CUDA;
   pr.nst = c->spmv_stages == 3 && 3 * (size_t)pr.cap + 1024 <= (size_t)optin ? 3 : 2;
-  pr.fn = pr.nst == 3 ? reinterpret_cast<void*>(pcg_cg_spmv_kernel<T, 3>)
-                      : reinterpret_cast<void*>(pcg_cg_spmv_kernel<T, 2>);
+  if (st.push)
+    pr.fn = pr.nst == 3 ? reinterpret_cast<void*>(pcg_cg_push_kernel<T, 3>)
+                        : reinterpret_cast<void*>(pcg_cg_push_kernel<T, 2>);
+  else
+    pr.fn = pr.nst == 3 ? reinterpret_cast<void*>(pcg_cg_spmv_kernel<T, 3>)
+                        : reinterpret_cast<void*>(pcg_cg_spmv_kernel<T, 2>);
   pr.smem = (size_t)pr.nst * pr.cap;
   cudaFuncAttributes fa;
   if (!ok(c, cudaFuncGetAttributes(&fa, pr.fn), "function attributes")) return TG_ERR_CUDA;
@@ -375,44 +598,92 @@ int product_shape(Context* c, CgProduct& pr) {
     c->err = "single-reduction PCG: product tile does not fit";
     return TG_ERR_CAPACITY;
   }
-  pr.grid = std::max(1, std::min({c->ntiles, c->num_sms * per_sm, kCtaCap}));
+  pr.grid = std::max(1, std::min({st.ntiles, c->num_sms * per_sm, kCtaCap}));
   pr.keep = -1;
   if (c->l2_keep >= 0) {
-    const std::vector<long long>& off = f32 ? c->h_blob_off32 : c->h_blob_off64;
+    const std::vector<long long>& off = *st.h_off;
     int t = 0;
-    while (t < c->ntiles && off[t + 1] <= c->l2_keep) ++t;
+    while (t < st.ntiles && off[t + 1] <= c->l2_keep) ++t;
     pr.keep = t;
   }
   return TG_OK;
 }
 
+// the two kernels' arguments for one storage
 template <typename T>
-int capture(Context* c, int precision, const T* minv) {
+struct CgArgs {
   using V = typename Vec4<T>::type;
   using P = typename Partial<T>::type;
+  int ntiles, cap, keep, nnd, ndp;
+  const long long* off;
+  const unsigned char* blob;
+  const V* pu;
+  V* qw;
+  V* pushw;
+  const V* pushr;
+  P* cta_part;
+  const P* dpart;
+  PcgScalars* sc;
+  int* status;
+  const T* mv;
+  V *x, *r, *u, *p, *sv;
+  const V* w;
+  double* vpart;
+  const int* lptr;
+  const uint8_t* mask;
+  int pstride;
+  void* pargs[11];
+  void* vargs[16];
+  const void* vfn;
+  CgArgs(Context* c, const CgStore<T>& st, const CgProduct& pr, const T* minv) {
+    ntiles = st.ntiles;
+    cap = pr.cap;
+    keep = pr.keep;
+    nnd = c->nnd;
+    ndp = pr.grid;
+    off = st.off;
+    blob = st.blob;
+    pu = (const V*)c->d_z;
+    qw = (V*)c->d_q;
+    pushw = st.pushbuf;
+    pushr = st.pushbuf;
+    cta_part = reinterpret_cast<P*>(c->d_partials + kCgPartials);
+    dpart = cta_part;
+    sc = c->d_pcg;
+    status = c->d_status;
+    mv = minv;
+    x = (V*)c->d_x;
+    r = (V*)c->d_r;
+    u = (V*)c->d_z;
+    p = (V*)c->d_p;
+    sv = (V*)c->d_cg_s;
+    w = (const V*)c->d_q;
+    vpart = c->d_partials;
+    lptr = st.lptr;
+    mask = c->d_mask;
+    pstride = st.pstride;
+    void* pa[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &pushw, &cta_part, &sc, &status};
+    void* va[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc, &pushr, &lptr, &mask, &pstride};
+    std::memcpy(pargs, pa, sizeof(pa));
+    std::memcpy(vargs, va, sizeof(va));
+    vfn = st.push ? reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, true>)
+                  : reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, false>);
+  }
+  CgArgs(const CgArgs&) = delete;
+};
+
+template <typename T>
+int capture(Context* c, int precision, const T* minv) {
+  CgStore<T> st;
+  int s = cg_store<T>(c, st);
+  if (s) return s;
   CgProduct pr;
-  int s = product_shape<T>(c, pr);
+  s = product_shape<T>(c, st, pr);
   if (s) return s;
   int nv = 0;
-  s = vec_grid<T>(c, &nv);
+  s = st.push ? vec_grid<T, true>(c, &nv) : vec_grid<T, false>(c, &nv);
   if (s) return s;
-  int ntiles = c->ntiles;
-  const long long* off = std::is_same<T, float>::value ? c->d_blob_off32 : c->d_blob_off64;
-  const unsigned char* blob = std::is_same<T, float>::value ? c->d_blob32 : c->d_blob64;
-  P* cta_part = reinterpret_cast<P*>(c->d_partials + kCgPartials);
-  const V* pu = (const V*)c->d_z;
-  V* qw = (V*)c->d_q;
-  PcgScalars* sc = c->d_pcg;
-  int* status = c->d_status;
-  int cap = pr.cap, keep = pr.keep;
-  void* args[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &cta_part, &sc, &status};
-  int nnd = c->nnd, ndp = pr.grid;
-  const T* mv = minv;
-  V *x = (V*)c->d_x, *r = (V*)c->d_r, *u = (V*)c->d_z, *p = (V*)c->d_p, *sv = (V*)c->d_cg_s;
-  const V* w = (const V*)c->d_q;
-  const P* dpart = cta_part;
-  double* vpart = c->d_partials;
-  void* vargs[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc};
+  CgArgs<T> A(c, st, pr, minv);
   // every launch after the first of the chunk depends programmatically on
   // the one before it
   cudaLaunchAttribute at[1];
@@ -436,9 +707,9 @@ int capture(Context* c, int precision, const T* minv) {
   for (int k = 0; k < kCgChunk && le == cudaSuccess; ++k) {
     pc.attrs = at;
     pc.numAttrs = (k > 0 && c->cg_pdl) ? 1 : 0;
-    le = cudaLaunchKernelExC(&pc, pr.fn, args);
+    le = cudaLaunchKernelExC(&pc, pr.fn, A.pargs);
     if (le != cudaSuccess) break;
-    le = cudaLaunchKernelExC(&vc, reinterpret_cast<const void*>(pcg_cg_vector_kernel<T>), vargs);
+    le = cudaLaunchKernelExC(&vc, A.vfn, A.vargs);
   }
   const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
   if (!ok(c, le, "capture launch") || !ok(c, ee, "end capture")) {
@@ -479,7 +750,13 @@ int solve_cg_t(Context* c, int precision, const double4_32a* d_rhs, double rel_t
   if (!ok(c, cudaMemcpyAsync(c->d_pcg + 1, c->d_pcg, sizeof(PcgScalars), cudaMemcpyDeviceToDevice, c->stream),
           "scalars"))
     return TG_ERR_CUDA;
-  const int key = precision * 2 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0);
+  if (c->cg_push) {
+    // the push storage's values follow the last assembly (a no-op when
+    // they already do; the captured graph reads the same buffers)
+    s = push_prepare(c, precision);
+    if (s) return s;
+  }
+  const int key = precision * 4 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0) + (c->cg_push ? 2 : 0);
   if (!c->cg_graph || c->cg_graph_key != key) {
     s = capture<T>(c, precision, minv);
     if (s) return s;
@@ -536,28 +813,19 @@ int time_cg_t(Context* c, int precision, int which, int reps, double* ms) {
     return TG_ERR_CUDA;
   h.done = 0;
   h.iters = 0;
+  CgStore<T> st;
+  s = cg_store<T>(c, st);
+  if (s) return s;
   CgProduct pr;
-  s = product_shape<T>(c, pr);
+  s = product_shape<T>(c, st, pr);
   if (s) return s;
   int nv = 0;
-  s = vec_grid<T>(c, &nv);
+  s = st.push ? vec_grid<T, true>(c, &nv) : vec_grid<T, false>(c, &nv);
   if (s) return s;
-  int ntiles = c->ntiles, cap = pr.cap, keep = pr.keep, nnd = c->nnd, ndp = pr.grid;
-  const long long* off = std::is_same<T, float>::value ? c->d_blob_off32 : c->d_blob_off64;
-  const unsigned char* blob = std::is_same<T, float>::value ? c->d_blob32 : c->d_blob64;
-  P* cta_part = reinterpret_cast<P*>(c->d_partials + kCgPartials);
-  const P* dpart = cta_part;
-  const V* pu = (const V*)c->d_z;
-  V* qw = (V*)c->d_q;
-  PcgScalars* sc = c->d_pcg;
-  int* status = c->d_status;
-  const T* mv = minv;
-  V *x = (V*)c->d_x, *r = (V*)c->d_r, *u = (V*)c->d_z, *p = (V*)c->d_p, *sv = (V*)c->d_cg_s;
-  const V* w = (const V*)c->d_q;
-  double* vpart = c->d_partials;
-  void* pargs[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &cta_part, &sc, &status};
-  void* vargs[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc};
-  const void* vfn = reinterpret_cast<const void*>(pcg_cg_vector_kernel<T>);
+  CgArgs<T> A(c, st, pr, minv);
+  void** pargs = A.pargs;
+  void** vargs = A.vargs;
+  const void* vfn = A.vfn;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);

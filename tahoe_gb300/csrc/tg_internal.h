@@ -95,6 +95,36 @@ struct SymStore {
   double* d_v8_64 = nullptr;
   double* d_v1_64 = nullptr;
 };
+// Symmetric push storage of the single-reduction PCG product (pushfmt.cu,
+// pcg_cg.cu): the upper node blocks of every row, its diagonal first, in
+// tile-contiguous ranges {header (first row, rows, blocks, plane stride),
+// local row pointers, columns, push slots, nine value planes}.  The product
+// adds A_IJ u_J into row I and stores A_IJ^T u_I (J > I) at the block's push
+// slot, k pstride + J with k the rank of I among row J's lower columns; the
+// vector kernel adds row J's lptr[J+1] - lptr[J] slots in rank order.  Built on the device from the
+// node-block CSR (composed meshes included), values converted from the
+// full-storage tiles after every assembly.
+struct PushStore {
+  bool built = false;
+  int ntiles = 0;
+  long long nu = 0, nl = 0;  // upper blocks (diagonals included), pushed blocks
+  int kmax = 0;              // largest lower count of a row: rank planes of pstride push slots
+  int pstride = 0;           // nnd rounded up to 8 (128-byte aligned planes)
+  long long cap32 = 0, cap64 = 0;  // largest tile, bytes
+  std::vector<long long> h_off32, h_off64;
+  long long* d_off32 = nullptr;
+  long long* d_off64 = nullptr;
+  unsigned char* d_blob32 = nullptr;
+  unsigned char* d_blob64 = nullptr;
+  int* d_tile_row = nullptr;  // ntiles+1 first row of each tile
+  int* d_row_tile = nullptr;  // nnd
+  int* d_urow = nullptr;      // nnd+1 first upper block of each row
+  int* d_diag = nullptr;      // nnd position of each row's diagonal in the full CSR
+  int* d_lptr = nullptr;      // nnd+1 first push slot of each row
+  void* d_push32 = nullptr;   // kmax*pstride float4
+  void* d_push64 = nullptr;   // kmax*pstride double4
+  long long serial32 = -1, serial64 = -1;  // tangent serial of the converted values
+};
 struct SegScalars;
 struct SegControl;
 // Per-RVE Krylov solves of a segmented batch (segpcg.cu): node chunks of
@@ -190,6 +220,9 @@ struct Context {
   bool seg_tolerate = false;        // a breakdown of some RVEs is reported per RVE, not as an error
   int sym_tile_blocks = 512;   // upper blocks per tile of the symmetric format
   SymStore sym;
+  PushStore push;
+  int cg_push = 0;              // single-reduction PCG on the symmetric push storage (tg_pcg_form 3)
+  long long tangent_serial = 0; // assemblies so far (values of derived storages follow it)
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
   std::vector<int> h_rowptr, h_col;
@@ -394,6 +427,10 @@ int pcg_finish(Context* c, const PcgScalars& h, int* iters, double* rel_res);
 int pcg_solve_cg(Context* c, int precision, const double4_32a* d_rhs, double rel_tol, int max_it, int precond,
                  int* iters, double* rel_res);
 void cg_free(Context* c);  // the captured iterations
+// symmetric push storage: structure (once per mesh) and values of the last
+// assembly in the given precision (pushfmt.cu)
+int push_prepare(Context* c, int precision);
+void push_free(Context* c);
 int time_cg_kernel(Context* c, int which, int reps, double* ms);  // 0 product, 1 vector kernel
 // PCG with every work vector, partial sum and scalar in caller scratch
 constexpr size_t kScratchScalarBytes = 256;

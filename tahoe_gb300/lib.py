@@ -177,6 +177,8 @@ class Context:
         """Name of the kernel the single-vector solve multiplies with."""
         if self.sym_mode and not getattr(self, "composed", False):
             return "pcg_spmv_sym_kernel"
+        if self.form == 3 and not getattr(self, "composed", False):
+            return "pcg_cg_push_kernel"
         if self.form in (1, 2) and not getattr(self, "composed", False):
             return "pcg_cg_spmv_kernel"
         return "pcg_spmv_kernel"
@@ -499,7 +501,7 @@ class Context:
     def pcg_form(self, form):
         """Recurrences of the single-vector PCG: 1 single-reduction with
         programmatic launch dependencies (default), 2 the same without them,
-        0 textbook."""
+        0 textbook, 3 form 1 on the symmetric push storage."""
         self._chk(self.L.tg_pcg_form(self.h, int(form)), "tg_pcg_form")
         self.form = int(form)
 

@@ -81,6 +81,26 @@ def spmv_bytes_sym(nnzb, nnd, s_val):
     return nu * (9 * s_val + 4) + nl * 8 + 2 * (nnd + 1) * 4 + 2 * nnd * s_vec + nnd
 
 
+def spmv_bytes_push(nnzb, nnd, s_val):
+    """Algorithmic bytes of one product on the symmetric push storage: the
+    nu = (nnzb + nnd) / 2 upper blocks (nine values, a column index, a push
+    slot), the row pointers, the gathered vector once, the upper part of the
+    product and the nl = (nnzb - nnd) / 2 pushed transposed products written
+    (vectors padded to 4 lanes)."""
+    s_vec = 4 * s_val
+    nu, nl = (nnzb + nnd) // 2, (nnzb - nnd) // 2
+    return nu * (9 * s_val + 8) + (nnd + 1) * 4 + 2 * nnd * s_vec + nl * s_vec
+
+
+def cg_vector_bytes_push(nnzb, nnd, s_val):
+    """The single-reduction vector kernel on the push storage: the bytes of
+    cg_vector_bytes plus the nl pushed products, the slot pointers and the
+    dof mask read."""
+    s_vec = 4 * s_val
+    nl = (nnzb - nnd) // 2
+    return cg_vector_bytes(nnd, s_val) + nl * s_vec + (nnd + 1) * 4 + nnd
+
+
 def assembly_bytes(nel, nnzb, nnd, s_val):
     """Algorithmic bytes of one assembly launch: element blocks (36 blocks of
     3 rows padded to 4 values per element) read once, the 64 contribution

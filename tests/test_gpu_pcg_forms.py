@@ -5,10 +5,13 @@ tg_pcg_form selects the textbook recurrences (form 0: product with a
 last-block reduction, vector update with a grid barrier) or the single-
 reduction recurrences of Chronopoulos & Gear (form 1, the default: the
 product writes CTA partials, every CTA of the vector kernel forms the
-iteration's scalars from them).  Both solve the same (block-)Jacobi CG
-system, so they reach the same solution to the solve's tolerance; each is
-bitwise repeatable.  tg_spmv_l2_keep only changes cache priorities of the
-bulk copies, so every setting gives bitwise the same iterates.
+iteration's scalars from them); form 3 runs form 1 on the symmetric push
+storage (upper node blocks streamed, transposed products pushed to the lower
+rows' slots and added by the vector kernel).  All solve the same
+(block-)Jacobi CG system, so they reach the same solution to the solve's
+tolerance; each is bitwise repeatable.  tg_spmv_l2_keep only changes cache
+priorities of the bulk copies, so every setting gives bitwise the same
+iterates.
 """
 import numpy as np
 import pytest
@@ -51,18 +54,20 @@ def test_forms_reach_the_same_solution(precision, precond):
     c, R = _system(m, precision, precond)
     tol = 1e-7 if precision == lib.MIXED else 1e-10
     sol = {}
-    for form in (0, 1):
+    for form in (0, 1, 3):
         c.pcg_form(form)
         du, its, rr, rc = c.pcg(R, rel_tol=tol, max_it=20000, precond=precond)
         assert rc == 0, form
         assert rr <= tol, (form, rr)
         sol[form] = (du, its)
     scale = np.abs(sol[0][0]).max()
-    # both are within the tolerance of the exact solution of the same system
+    # all are within the tolerance of the exact solution of the same system
     bound = 2e-4 if precision == lib.MIXED else 1e-6
-    assert np.abs(sol[1][0] - sol[0][0]).max() <= bound * scale
-    # the same Krylov method: iteration counts within a few percent
-    assert abs(sol[1][1] - sol[0][1]) <= max(3, 0.05 * sol[0][1])
+    for form in (1, 3):
+        assert np.abs(sol[form][0] - sol[0][0]).max() <= bound * scale, form
+        # the same Krylov method: iteration counts within a few percent
+        assert abs(sol[form][1] - sol[0][1]) <= max(3, 0.05 * sol[0][1]), form
+    c.pcg_form(1)
 
 
 @pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
@@ -80,16 +85,44 @@ def test_programmatic_launch_dependencies_leave_the_iterates_bitwise_unchanged(p
     c.pcg_form(1)
 
 
+@pytest.mark.parametrize("form", [1, 3])
 @pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
-def test_single_reduction_form_is_bitwise_repeatable(precision):
+def test_single_reduction_form_is_bitwise_repeatable(precision, form):
     m = _model()
     c, R = _system(m, precision, lib.PRECOND_JACOBI)
-    c.pcg_form(1)
+    c.pcg_form(form)
     a = c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_JACOBI)
     b = c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_JACOBI)
     assert a[3] == 0 and b[3] == 0
     assert a[1] == b[1]
     assert np.array_equal(a[0], b[0])
+    c.pcg_form(1)
+
+
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+def test_push_storage_follows_every_assembly(precision):
+    """The push storage's values are copied from each new assembly: after a
+    second tangent at another state (and a form switch in between), form 3
+    solves the new system as form 1 does."""
+    m = _model()
+    c, R = _system(m, precision, lib.PRECOND_BLOCK_JACOBI)
+    c.pcg_form(3)
+    c.pcg(R, rel_tol=1e-8, max_it=20000, precond=lib.PRECOND_BLOCK_JACOBI)
+    u = c.get_u()
+    c.set_u(u * 1.5)
+    R2, _ = c.residual()
+    c.tangent(precision)
+    sol = {}
+    for form in (1, 3):
+        c.pcg_form(form)
+        du, its, rr, rc = c.pcg(R2, rel_tol=1e-9, max_it=20000, precond=lib.PRECOND_BLOCK_JACOBI)
+        assert rc == 0
+        sol[form] = (du, its)
+    scale = np.abs(sol[1][0]).max()
+    bound = 2e-4 if precision == lib.MIXED else 1e-6
+    assert np.abs(sol[3][0] - sol[1][0]).max() <= bound * scale
+    assert abs(sol[3][1] - sol[1][1]) <= max(3, 0.05 * sol[1][1])
+    c.pcg_form(1)
 
 
 def test_l2_priorities_leave_the_iterates_bitwise_unchanged():
@@ -97,7 +130,7 @@ def test_l2_priorities_leave_the_iterates_bitwise_unchanged():
     c, R = _system(m, lib.MIXED, lib.PRECOND_JACOBI)
     nbytes = c.block_nnz * 40
     ref = None
-    for form in (1, 0):
+    for form in (1, 0, 3):
         c.pcg_form(form)
         ref = None
         for keep in (-1, 0, 1 << 20, nbytes // 3, 4 * nbytes):
@@ -109,6 +142,7 @@ def test_l2_priorities_leave_the_iterates_bitwise_unchanged():
             assert its == ref[1], (form, keep)
             assert np.array_equal(du, ref[0]), (form, keep)
     c.spmv_l2_keep(16 << 20)
+    c.pcg_form(1)
 
 
 def test_single_reduction_form_converges_within_the_first_chunk():
@@ -156,7 +190,7 @@ def _small_strain_system(C, precision):
     return c, R
 
 
-@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("form", [0, 1, 3])
 @pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
 def test_iteration_limit_is_reported_not_raised(form, precision):
     c, R = _small_strain_system(_iso_C(), precision)
@@ -168,7 +202,7 @@ def test_iteration_limit_is_reported_not_raised(form, precision):
     c.pcg_form(1)
 
 
-@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("form", [0, 1, 3])
 @pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
 def test_indefinite_operator_breaks_down(form, precision):
     # a negative-definite stiffness: the first curvature p.Ap (u.Au in the
