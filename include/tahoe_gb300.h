@@ -382,9 +382,10 @@ int tg_spmv_config(tg_context* ctx, int tile_blocks, int stages);
  * barrier after each staged tile; 1 each warp releases the stage on an
  * mbarrier and moves on (results are bitwise the same) */
 int tg_spmv_release(tg_context* ctx, int per_warp);
-/* Recurrences of the single-vector PCG (both precisions, full block
- * storage).  form = 1 (default): the single-reduction form of Chronopoulos &
- * Gear -- per iteration one product kernel (w = A u, CTA partials of u.w) and
+/* Recurrences and matrix storage of the single-vector PCG (both
+ * precisions).  form = 1: the single-reduction form of Chronopoulos & Gear on
+ * the full block storage -- per iteration one product kernel (w = A u, CTA
+ * partials of u.w) and
  * one vector kernel whose CTAs each form the iteration's scalars from the
  * partials and run one fused pass over p, s, x, r, u; no grid barrier and no
  * atomic in either kernel; each kernel launches with a programmatic
@@ -395,16 +396,19 @@ int tg_spmv_release(tg_context* ctx, int per_warp);
  * last-block reduction; vector update with a grid barrier between its two
  * passes).  All solve the same (block-)Jacobi CG system to the same
  * tolerance; forms 1 and 2 take bitwise the same iterates, form 0 differs
- * from them by rounding.  form = 3: form 1 on the symmetric push storage --
- * the product streams the upper node blocks only (about 55 % of the full
- * storage's bytes) and stores each off-diagonal block's transposed product
- * in a slot of its lower row, which the vector kernel adds in a fixed order
- * (bitwise repeatable; it differs from form 1 by rounding).  The storage is
- * built on the device on first use after a mesh change and its values are
- * copied from every new assembly.  The symmetric format of
- * tg_spmv_symmetric, segmented batches and the no-allocation entry point use
- * their own kernels. */
+ * from them by rounding.  form = 3: form 1 on the symmetric push storage -- the product streams the upper node blocks only (about 55 % of
+ * the full storage's bytes) and stores each off-diagonal block's transposed
+ * product in a slot of its lower row, which the vector kernel adds in a fixed
+ * order (bitwise repeatable; it differs from form 1 by rounding).  The
+ * storage is built on the device on first use after a mesh change and its
+ * values are copied from every new assembly.  form = -1 (default): form 3
+ * on meshes of at least one million block nonzeros, form 1 below (where the
+ * one-time build of the push storage is not amortised).  The symmetric
+ * format of tg_spmv_symmetric, segmented batches and the no-allocation entry
+ * point use their own kernels. */
 int tg_pcg_form(tg_context* ctx, int form);
+/* the form the next single-vector solve runs on the current mesh (0..3) */
+int tg_pcg_form_get(const tg_context* ctx, int* form);
 /* L2 priorities of the streamed matrix.  bytes >= 0: the leading whole
  * tiles within `bytes` of the matrix storage are copied with evict_last
  * (kept in the L2 from one product to the next) and the rest with

@@ -474,15 +474,26 @@ int tg_spmv_release(tg_context* c, int per_warp) {
 }
 
 int tg_pcg_form(tg_context* c, int form) {
-  if (!c || form < 0 || form > 3) return TG_ERR_ARG;
+  if (!c || form < -1 || form > 3) return TG_ERR_ARG;
   c->pcg_form = form == 0 ? 0 : 1;
-  const int pdl = form == 1 || form == 3 ? 1 : 0;
-  const int push = form == 3 ? 1 : 0;
+  const int pdl = form == 2 ? 0 : 1;
+  const int push = form == 3 ? 1 : form == -1 ? -1 : 0;
   if (pdl != c->cg_pdl || push != c->cg_push) {
     c->cg_pdl = pdl;
     c->cg_push = push;
     drop_graphs(c);  // the captured chunk bakes in its launch dependencies and storage
   }
+  return TG_OK;
+}
+
+int tg_pcg_form_get(const tg_context* c, int* form) {
+  if (!c || !form) return TG_ERR_ARG;
+  if (c->pcg_form == 0)
+    *form = 0;
+  else if (!c->cg_pdl)
+    *form = 2;
+  else
+    *form = push_active(c) ? 3 : 1;
   return TG_OK;
 }
 

@@ -536,7 +536,7 @@ struct CgStore {
 template <typename T>
 int cg_store(Context* c, CgStore<T>& st) {
   const bool f32 = std::is_same<T, float>::value;
-  st.push = c->cg_push != 0;
+  st.push = push_active(c);
   if (!st.push) {
     st.ntiles = c->ntiles;
     st.cap = f32 ? c->blob_cap32 : c->blob_cap64;
@@ -750,13 +750,13 @@ int solve_cg_t(Context* c, int precision, const double4_32a* d_rhs, double rel_t
   if (!ok(c, cudaMemcpyAsync(c->d_pcg + 1, c->d_pcg, sizeof(PcgScalars), cudaMemcpyDeviceToDevice, c->stream),
           "scalars"))
     return TG_ERR_CUDA;
-  if (c->cg_push) {
+  if (push_active(c)) {
     // the push storage's values follow the last assembly (a no-op when
     // they already do; the captured graph reads the same buffers)
     s = push_prepare(c, precision);
     if (s) return s;
   }
-  const int key = precision * 4 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0) + (c->cg_push ? 2 : 0);
+  const int key = precision * 4 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0) + (push_active(c) ? 2 : 0);
   if (!c->cg_graph || c->cg_graph_key != key) {
     s = capture<T>(c, precision, minv);
     if (s) return s;

@@ -44,7 +44,11 @@ namespace tg {
 
 namespace {
 
-constexpr int kPushTileBlocks = 576;  // upper blocks per tile: two FP32 stages of four CTAs fit an SM
+// upper blocks per tile.  C2 (64^3), Newton step with 2 stages of four CTAs
+// per SM: 256 -> 36.7 ms, 320 -> 33.7, 384 -> 32.0, 448 -> 30.7, 512 -> 30.65,
+// 576 -> 32.6; dealing the rows of a tile to the warps from a rotating first
+// warp changed nothing
+constexpr int kPushTileBlocks = 512;
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;         // items per thread of a scan block
 

@@ -221,7 +221,11 @@ struct Context {
   int sym_tile_blocks = 512;   // upper blocks per tile of the symmetric format
   SymStore sym;
   PushStore push;
-  int cg_push = 0;              // single-reduction PCG on the symmetric push storage (tg_pcg_form 3)
+  // single-reduction PCG on the symmetric push storage: 1 (tg_pcg_form 3), 0
+  // (forms 1, 2), -1 automatic (the default: the push storage for meshes of
+  // at least kPushAutoBlocks block nonzeros, whose product amortises its
+  // build; the full storage below)
+  int cg_push = -1;
   long long tangent_serial = 0; // assemblies so far (values of derived storages follow it)
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
@@ -275,7 +279,7 @@ struct Context {
   void* d_q = nullptr;
   void* d_cg_s = nullptr;  // s = A p by recurrence (single-reduction PCG), in the solve's precision
   int cg_s_precision = -1;
-  int pcg_form = 1;        // 1: single-vector solves on full storage run the single-reduction PCG (pcg_cg.cu)
+  int pcg_form = 1;        // 1: single-vector solves run the single-reduction PCG (pcg_cg.cu)
   int cg_pdl = 1;           // its kernels launch with programmatic dependencies
   cudaGraphExec_t cg_graph = nullptr;  // captured chunk of the single-reduction PCG
   int cg_graph_key = -1;
@@ -430,6 +434,10 @@ void cg_free(Context* c);  // the captured iterations
 // symmetric push storage: structure (once per mesh) and values of the last
 // assembly in the given precision (pushfmt.cu)
 int push_prepare(Context* c, int precision);
+constexpr long long kPushAutoBlocks = 1000000;
+inline bool push_active(const Context* c) {
+  return c->cg_push > 0 || (c->cg_push < 0 && c->nnzb >= kPushAutoBlocks);
+}
 void push_free(Context* c);
 int time_cg_kernel(Context* c, int which, int reps, double* ms);  // 0 product, 1 vector kernel
 // PCG with every work vector, partial sum and scalar in caller scratch

@@ -94,6 +94,7 @@ _SIGS = {
     "tg_spmv_release": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tg_spmv_l2_keep": (ctypes.c_int, [_vp, ctypes.c_longlong]),
     "tg_pcg_form": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tg_pcg_form_get": (ctypes.c_int, [_vp, _ip]),
     "tg_tuning_get": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "tg_set_segments": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip]),
     "tg_segment_residual_norms": (ctypes.c_int, [_vp, _dp]),
@@ -169,7 +170,7 @@ class Context:
             raise TahoeError(rc, "tg_create", "no CUDA device or driver")
         self.h = h
         self.nnd = self.nel = self.neq = 0
-        self.form = 1            # tg_pcg_form default
+        self.form = -1           # tg_pcg_form default (automatic)
         self.l2_keep = 16 << 20  # tg_spmv_l2_keep default
         self.sym_mode = 0
 
@@ -177,9 +178,10 @@ class Context:
         """Name of the kernel the single-vector solve multiplies with."""
         if self.sym_mode and not getattr(self, "composed", False):
             return "pcg_spmv_sym_kernel"
-        if self.form == 3 and not getattr(self, "composed", False):
+        form = self.effective_form()
+        if form == 3 and not getattr(self, "composed", False):
             return "pcg_cg_push_kernel"
-        if self.form in (1, 2) and not getattr(self, "composed", False):
+        if form in (1, 2) and not getattr(self, "composed", False):
             return "pcg_cg_spmv_kernel"
         return "pcg_spmv_kernel"
 
@@ -499,11 +501,19 @@ class Context:
         self._chk(self.L.tg_spmv_release(self.h, int(per_warp)), "tg_spmv_release")
 
     def pcg_form(self, form):
-        """Recurrences of the single-vector PCG: 1 single-reduction with
-        programmatic launch dependencies (default), 2 the same without them,
-        0 textbook, 3 form 1 on the symmetric push storage."""
+        """Recurrences of the single-vector PCG: 3 single-reduction with
+        programmatic launch dependencies on the symmetric push storage, 1 the
+        same on the full storage, 2 form 1 without programmatic dependencies,
+        0 textbook, -1 (default) form 3 on meshes of at least a million block
+        nonzeros and form 1 below."""
         self._chk(self.L.tg_pcg_form(self.h, int(form)), "tg_pcg_form")
         self.form = int(form)
+
+    def effective_form(self):
+        """The form the next single-vector solve runs on the current mesh."""
+        f = ctypes.c_int(0)
+        self._chk(self.L.tg_pcg_form_get(self.h, ctypes.byref(f)), "tg_pcg_form_get")
+        return f.value
 
     def spmv_l2_keep(self, nbytes):
         """Matrix bytes the streamed product keeps in the L2 (evict_last;

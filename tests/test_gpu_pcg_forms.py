@@ -214,3 +214,22 @@ def test_indefinite_operator_breaks_down(form, precision):
     assert ei.value.code == -5  # TG_ERR_NAN: breakdown
     assert "indefinite" in str(ei.value)
     c.pcg_form(1)
+
+
+def test_default_form_follows_mesh_size():
+    """The default (-1) runs the push storage on meshes of at least a million
+    block nonzeros and the full storage below; an explicit form holds on any
+    mesh."""
+    small = _model(6)
+    c = small.ctx
+    assert c.effective_form() == 1
+    c.pcg_form(3)
+    assert c.effective_form() == 3
+    c.pcg_form(2)
+    assert c.effective_form() == 2
+    c.pcg_form(-1)
+    assert c.effective_form() == 1
+    big = _model(40)  # 68,921 nodes, about 1.7 M block nonzeros
+    assert big.ctx.block_nnz >= 1_000_000
+    assert big.ctx.effective_form() == 3
+    assert big.ctx.product_kernel() == "pcg_cg_push_kernel"
