@@ -81,13 +81,18 @@ def spmv_roofline(ctx, precision):
     from tahoe_gb300 import lib, workloads
     ms = ctx.time_kernel(0, 20)
     s_val = 4 if precision == lib.MIXED else 8
-    sym = getattr(ctx, "sym_mode", 0) and not getattr(ctx, "composed", False)
-    b = (workloads.spmv_bytes_sym if sym else workloads.spmv_bytes)(ctx.block_nnz, ctx.nnd, s_val)
+    product = ctx.product_kernel()
+    push = product == "pcg_cg_push_kernel"
+    sym = product == "pcg_spmv_sym_kernel"
+    b = (workloads.spmv_bytes_push if push else workloads.spmv_bytes_sym if sym else
+         workloads.spmv_bytes)(ctx.block_nnz, ctx.nnd, s_val)
     peak, kind = peaks()
     ach = b / (ms * 1e-3) / 1e9
-    return {"kernel": ctx.product_kernel(), "storage": "symmetric" if sym else "full",
+    return {"kernel": product, "storage": "symmetric push" if push else "symmetric" if sym else "full",
             "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": int(b), "ms_per_launch": round(ms, 4)}
+            "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": int(b),
+            "l2_intermediate_bytes": int(workloads.push_l2_bytes(ctx.block_nnz, ctx.nnd, s_val)) if push else 0,
+            "ms_per_launch": round(ms, 4)}
 
 
 class ClockSampler:
@@ -436,9 +441,10 @@ def run_ours(args):
                       "assembly": round(t_asm, 4), "residual": round(t_res, 4),
                       "residual_fp64": round(t_res64, 4)},
         "roofline": {"kernel": product,
-                     "storage": "symmetric" if sym else "full", "bound": "hbm", "achieved": round(achieved, 1),
+                     "storage": "symmetric push" if push else "symmetric" if sym else "full", "bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "algorithmic_bytes": int(bytes_spmv),
+                     "l2_intermediate_bytes": int(workloads.push_l2_bytes(nnzb, nnd, s_val)) if push else 0,
                      "traffic": profiled_traffic(prof) if prec == lib.MIXED else None,
                      "traffic_source": "committed ncu capture of this kernel on this workload (profiles/%s), not "
                                        "measured in this run" % prof},

@@ -82,23 +82,29 @@ def spmv_bytes_sym(nnzb, nnd, s_val):
 
 
 def spmv_bytes_push(nnzb, nnd, s_val):
-    """Algorithmic bytes of one product on the symmetric push storage: the
-    nu = (nnzb + nnd) / 2 upper blocks (nine values, a column index, a push
-    slot), the row pointers, the gathered vector once, the upper part of the
-    product and the nl = (nnzb - nnd) / 2 pushed transposed products written
-    (vectors padded to 4 lanes)."""
+    """Algorithmic DRAM bytes of one product on the symmetric push storage:
+    the nu = (nnzb + nnd) / 2 upper blocks (nine values, a column index, a
+    push slot), the row pointers, the gathered vector once and the upper part
+    of the product written (vectors padded to 4 lanes).  The transposed
+    products it pushes (push_l2_bytes) are an L2 intermediate by design:
+    written with evict_last, read by the next kernel and dropped without
+    write-back."""
     s_vec = 4 * s_val
-    nu, nl = (nnzb + nnd) // 2, (nnzb - nnd) // 2
-    return nu * (9 * s_val + 8) + (nnd + 1) * 4 + 2 * nnd * s_vec + nl * s_vec
+    nu = (nnzb + nnd) // 2
+    return nu * (9 * s_val + 8) + (nnd + 1) * 4 + 2 * nnd * s_vec
+
+
+def push_l2_bytes(nnzb, nnd, s_val):
+    """Bytes of the nl = (nnzb - nnd) / 2 pushed products, written by the
+    product and read by the vector kernel through the L2."""
+    return (nnzb - nnd) // 2 * 4 * s_val
 
 
 def cg_vector_bytes_push(nnzb, nnd, s_val):
-    """The single-reduction vector kernel on the push storage: the bytes of
-    cg_vector_bytes plus the nl pushed products, the slot pointers and the
-    dof mask read."""
-    s_vec = 4 * s_val
-    nl = (nnzb - nnd) // 2
-    return cg_vector_bytes(nnd, s_val) + nl * s_vec + (nnd + 1) * 4 + nnd
+    """Algorithmic DRAM bytes of the single-reduction vector kernel on the
+    push storage: those of cg_vector_bytes plus the slot pointers and the
+    dof mask (the pushed products come from the L2, push_l2_bytes)."""
+    return cg_vector_bytes(nnd, s_val) + (nnd + 1) * 4 + nnd
 
 
 def assembly_bytes(nel, nnzb, nnd, s_val):

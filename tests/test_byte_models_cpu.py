@@ -34,3 +34,17 @@ def test_profiled_traffic_matches_the_byte_model():
     assert m, "summary carries the traffic line bench.py reads"
     traffic = int(m.group(1))
     assert abs(traffic / workloads.spmv_bytes(NNZB, NND, 4) - 1.0) < 0.02
+
+
+def test_push_profile_traffic_matches_the_dram_model():
+    # the push storage's product: DRAM traffic of the committed capture within
+    # 1 % of the DRAM model (its pushed products stay in the L2 and are
+    # counted apart)
+    with open(os.path.join(ROOT, "profiles", "pcg_cg_push_c2_64cubed.md")) as f:
+        m = re.search(r"^traffic_bytes_per_launch: (\d+)$", f.read(), re.M)
+    assert m
+    traffic = int(m.group(1))
+    assert abs(traffic / workloads.spmv_bytes_push(NNZB, NND, 4) - 1.0) < 0.01
+    nu, nl = (NNZB + NND) // 2, (NNZB - NND) // 2
+    assert workloads.push_l2_bytes(NNZB, NND, 4) == nl * 16
+    assert workloads.spmv_bytes_push(NNZB, NND, 4) == nu * 44 + (NND + 1) * 4 + 2 * NND * 16
