@@ -82,7 +82,7 @@ def spmv_roofline(ctx, precision):
     ms = ctx.time_kernel(0, 20)
     s_val = 4 if precision == lib.MIXED else 8
     product = ctx.product_kernel()
-    push = product == "pcg_cg_push_kernel"
+    push = product in ("pcg_cg_push_kernel", "pcg_seg_push_kernel")
     sym = product == "pcg_spmv_sym_kernel"
     b = (workloads.spmv_bytes_push if push else workloads.spmv_bytes_sym if sym else
          workloads.spmv_bytes)(ctx.block_nnz, ctx.nnd, s_val)
@@ -92,7 +92,10 @@ def spmv_roofline(ctx, precision):
             "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
             "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": int(b),
             "l2_intermediate_bytes": int(workloads.push_l2_bytes(ctx.block_nnz, ctx.nnd, s_val)) if push else 0,
-            "ms_per_launch": round(ms, 4)}
+            "ms_per_launch": round(ms, 4),
+            "note": "algorithmic bytes are the DRAM bytes of the push storage's stream; its pushed products "
+                    "(l2_intermediate_bytes) stay in L2 where they fit and also cross DRAM where they do not, "
+                    "so the fraction is a lower bound on a mesh that large" if push else ""}
 
 
 class ClockSampler:

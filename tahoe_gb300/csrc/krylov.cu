@@ -852,7 +852,9 @@ int time_pcg_t(Context* c, int which, int reps, double* ms) {
 }
 
 int time_pcg_kernel(Context* c, int which, int reps, double* ms) {
-  // the kernels the solve runs: the single-reduction form's own pair
+  // the kernels the solve runs: the single-reduction form's own pair, or
+  // the product of a segmented batch on the push storage
+  if (c->nseg > 0 && which == 0 && push_active(c)) return time_seg_push(c, reps, ms);
   if (c->pcg_form == 1 && !sym_active(c) && c->nseg == 0) return time_cg_kernel(c, which, reps, ms);
   if (c->tangent_precision == TG_MIXED) return time_pcg_t<float>(c, which, reps, ms);
   if (c->tangent_precision == TG_FP64) return time_pcg_t<double>(c, which, reps, ms);

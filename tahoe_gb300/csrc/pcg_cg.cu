@@ -73,11 +73,15 @@ __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wa
 // A_IJ^T u_I at its push slot (row J's share of the product, added by the
 // vector kernel).  The row's first block is its diagonal (its first lane),
 // so u.w of the whole matrix is the sum over rows of u_I.(2 y_I - A_II u_I).
+//
+// With node_dot (a segmented batch) the row's own u_I.(2 y_I - A_II u_I) is
+// written per node instead of accumulated (the batch reduces it per RVE).
 template <typename T, int LPR>
 __device__ __forceinline__ void push_tile_rows(const unsigned char* base, int lane, int warp, int nwarps,
                                                const typename Vec4<T>::type* __restrict__ uv,
                                                typename Vec4<T>::type* __restrict__ wup,
-                                               typename Vec4<T>::type* __restrict__ push, Acc<T>& dot) {
+                                               typename Vec4<T>::type* __restrict__ push, Acc<T>& dot,
+                                               double* __restrict__ node_dot) {
   using V = typename Vec4<T>::type;
   constexpr int RPW = 32 / LPR;  // rows per warp pass
   constexpr int K = 4;
@@ -142,9 +146,17 @@ __device__ __forceinline__ void push_tile_rows(const unsigned char* base, int la
     }
     if (live && sub == 0) {
       wup[I] = mk<V, T>(a0, a1, a2);
-      dot.add_prod(ui.x, T(2) * a0 - d0);
-      dot.add_prod(ui.y, T(2) * a1 - d1);
-      dot.add_prod(ui.z, T(2) * a2 - d2);
+      if (node_dot) {
+        Acc<T> d;
+        d.add_prod(ui.x, T(2) * a0 - d0);
+        d.add_prod(ui.y, T(2) * a1 - d1);
+        d.add_prod(ui.z, T(2) * a2 - d2);
+        node_dot[I] = d.value();
+      } else {
+        dot.add_prod(ui.x, T(2) * a0 - d0);
+        dot.add_prod(ui.y, T(2) * a1 - d1);
+        dot.add_prod(ui.z, T(2) * a2 - d2);
+      }
     }
   }
 }
@@ -165,14 +177,18 @@ constexpr bool kPushDiscard = true;  // read push lines are dropped from L2 with
 // such CTAs per SM stream the matrix faster than one CTA of four groups
 // sharing the SM's tiles, and faster than tiles pulled from a global
 // counter; the spread of finishing times is per SM, not per tile count.)
-template <typename T, int NST, bool PUSH>
+//
+// SEG: the product of a segmented batch's per-RVE solves -- sc is the
+// batch's gate (its done flag ends the launch at once), each row's own z.w
+// goes to node_dot, and no CTA partial is written.
+template <typename T, int NST, bool PUSH, bool SEG>
 __device__ __forceinline__ void cg_product(int ntiles, const long long* __restrict__ blob_off,
                                            const unsigned char* __restrict__ blob, int cap, int keep,
                                            const typename Vec4<T>::type* __restrict__ p,
                                            typename Vec4<T>::type* __restrict__ q,
                                            typename Vec4<T>::type* __restrict__ push,
-                                           typename Partial<T>::type* __restrict__ cta_part, PcgScalars* sc,
-                                           int* status) {
+                                           typename Partial<T>::type* __restrict__ cta_part,
+                                           double* __restrict__ node_dot, PcgScalars* sc, int* status) {
   using P = typename Partial<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
@@ -216,7 +232,7 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
     for (int k = 0; k < NST && t0 + k * G < ntiles; ++k) issue(t0 + k * G, k);
   griddep_wait();  // u and the scalars of the last vector kernel
   griddep_launch();
-  if (skip_launch(sc, 1)) {
+  if (skip_launch(sc, SEG ? 0 : 1)) {
     if (threadIdx.x == 0) drain();
     return;
   }
@@ -234,9 +250,10 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
     __syncwarp();
     if (*(volatile int*)&abort_flag) break;
     if (PUSH)
-      push_tile_rows<T, kPushLanes>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, push, v);
+      push_tile_rows<T, kPushLanes>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, push, v,
+                                    SEG ? node_dot : nullptr);
     else
-      spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v, nullptr);
+      spmv_tile_rows<T>(smem + (size_t)s * cap, lane, warp, nwarps, p, q, v, SEG ? node_dot : nullptr);
     __syncwarp();
     if (lane == 0) {
       __threadfence_block();
@@ -257,32 +274,45 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
     // flight and flag the solve broken down
     atomicOr(status, kStatusWaitTimeout);
     drain();
-    sc[0].done = sc[1].done = 2;
-    sc[0].fail = sc[1].fail = 5;
+    if (SEG) {
+      sc->done = 2;
+      sc->fail = 5;
+    } else {
+      sc[0].done = sc[1].done = 2;
+      sc[0].fail = sc[1].fail = 5;
+    }
   }
+  if (SEG) return;
   Acc<T> vv[1] = {v};
   P bt[1];
   block_total_acc<T, 1>(vv, bt);
   if (threadIdx.x == 0) cta_part[blockIdx.x] = bt[0];
 }
 
+#define TG_CG_PRODUCT_PARAMS                                                                                  \
+  int ntiles, const long long *__restrict__ blob_off, const unsigned char *__restrict__ blob, int cap, int keep, \
+      const typename Vec4<T>::type *__restrict__ p, typename Vec4<T>::type *__restrict__ q,                  \
+      typename Vec4<T>::type *__restrict__ push, typename Partial<T>::type *__restrict__ cta_part,            \
+      double *__restrict__ node_dot, PcgScalars *sc, int *status
+#define TG_CG_PRODUCT_ARGS ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, node_dot, sc, status
+
 template <typename T, int NST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
-    pcg_cg_spmv_kernel(int ntiles, const long long* __restrict__ blob_off, const unsigned char* __restrict__ blob,
-                       int cap, int keep, const typename Vec4<T>::type* __restrict__ p,
-                       typename Vec4<T>::type* __restrict__ q, typename Vec4<T>::type* __restrict__ push,
-                       typename Partial<T>::type* __restrict__ cta_part, PcgScalars* sc, int* status) {
-  cg_product<T, NST, false>(ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, sc, status);
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_cg_spmv_kernel(TG_CG_PRODUCT_PARAMS) {
+  cg_product<T, NST, false, false>(TG_CG_PRODUCT_ARGS);
 }
 
 template <typename T, int NST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
-    pcg_cg_push_kernel(int ntiles, const long long* __restrict__ blob_off, const unsigned char* __restrict__ blob,
-                       int cap, int keep, const typename Vec4<T>::type* __restrict__ p,
-                       typename Vec4<T>::type* __restrict__ q, typename Vec4<T>::type* __restrict__ push,
-                       typename Partial<T>::type* __restrict__ cta_part, PcgScalars* sc, int* status) {
-  cg_product<T, NST, true>(ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, sc, status);
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_cg_push_kernel(TG_CG_PRODUCT_PARAMS) {
+  cg_product<T, NST, true, false>(TG_CG_PRODUCT_ARGS);
 }
+
+// the segmented batch's product on the push storage
+template <typename T, int NST>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_seg_push_kernel(TG_CG_PRODUCT_PARAMS) {
+  cg_product<T, NST, true, true>(TG_CG_PRODUCT_ARGS);
+}
+#undef TG_CG_PRODUCT_PARAMS
+#undef TG_CG_PRODUCT_ARGS
 
 // One CTA per SM, one node per thread per pass: 1024 (FP32, 64 registers)
 // or 512 (FP64) nodes in flight per SM cover the L2 latency of the vector
@@ -568,13 +598,16 @@ struct CgProduct {
 };
 
 template <typename T>
-int product_shape(Context* c, const CgStore<T>& st, CgProduct& pr) {
+int product_shape(Context* c, const CgStore<T>& st, CgProduct& pr, bool seg = false) {
   pr.cap = (int)((st.cap + 127) / 128 * 128);
   int optin = 0;
   if (!ok(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attribute"))
     return TG_ERR_CUDA;
   pr.nst = c->spmv_stages == 3 && 3 * (size_t)pr.cap + 1024 <= (size_t)optin ? 3 : 2;
-  if (st.push)
+  if (seg)
+    pr.fn = pr.nst == 3 ? reinterpret_cast<void*>(pcg_seg_push_kernel<T, 3>)
+                        : reinterpret_cast<void*>(pcg_seg_push_kernel<T, 2>);
+  else if (st.push)
     pr.fn = pr.nst == 3 ? reinterpret_cast<void*>(pcg_cg_push_kernel<T, 3>)
                         : reinterpret_cast<void*>(pcg_cg_push_kernel<T, 2>);
   else
@@ -632,7 +665,8 @@ struct CgArgs {
   const int* lptr;
   const uint8_t* mask;
   int pstride;
-  void* pargs[11];
+  double* node_dot = nullptr;
+  void* pargs[12];
   void* vargs[16];
   const void* vfn;
   CgArgs(Context* c, const CgStore<T>& st, const CgProduct& pr, const T* minv) {
@@ -662,7 +696,7 @@ struct CgArgs {
     lptr = st.lptr;
     mask = c->d_mask;
     pstride = st.pstride;
-    void* pa[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &pushw, &cta_part, &sc, &status};
+    void* pa[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &pushw, &cta_part, &node_dot, &sc, &status};
     void* va[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc, &pushr, &lptr, &mask, &pstride};
     std::memcpy(pargs, pa, sizeof(pa));
     std::memcpy(vargs, va, sizeof(va));
@@ -869,6 +903,77 @@ void cg_free(Context* c) {
   if (c->cg_graph) cudaGraphExecDestroy(c->cg_graph);
   c->cg_graph = nullptr;
   c->cg_graph_key = -1;
+}
+
+namespace {
+template <typename T>
+int seg_push_t(Context* c, const void* z, void* w, double* node_dot, PcgScalars* gate) {
+  using V = typename Vec4<T>::type;
+  CgStore<T> st;
+  int s = cg_store<T>(c, st);
+  if (s) return s;
+  if (!st.push) {
+    c->err = "segmented push product without the push storage";
+    return TG_ERR_ARG;
+  }
+  CgProduct pr;
+  s = product_shape<T>(c, st, pr, true);
+  if (s) return s;
+  int ntiles = st.ntiles, cap = pr.cap, keep = pr.keep;
+  const long long* off = st.off;
+  const unsigned char* blob = st.blob;
+  const V* p = (const V*)z;
+  V* q = (V*)w;
+  V* push = st.pushbuf;
+  typename Partial<T>::type* cta_part = nullptr;
+  int* status = c->d_status;
+  void* args[] = {&ntiles, &off, &blob, &cap, &keep, &p, &q, &push, &cta_part, &node_dot, &gate, &status};
+  const cudaError_t e = cudaLaunchKernel(pr.fn, dim3(pr.grid), dim3(256), args, pr.smem, c->stream);
+  c->launches++;
+  return ok(c, e, "pcg_seg_push_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+}  // namespace
+
+// Average device time of standalone launches of the segmented batch's push
+// product on the current tangent (a zero gate, a scratch node_dot).
+int time_seg_push(Context* c, int reps, double* ms) {
+  const int precision = c->tangent_precision;
+  if (precision != TG_MIXED && precision != TG_FP64) {
+    c->err = "form the tangent first";
+    return TG_ERR_ARG;
+  }
+  int s = pcg_vectors(c, precision);
+  if (!s) s = push_prepare(c, precision);
+  if (s) return s;
+  double* nd = nullptr;
+  if (!dalloc(c, &nd, (size_t)c->nnd)) return TG_ERR_OOM;
+  if (!ok(c, cudaMemsetAsync(c->d_pcg, 0, sizeof(PcgScalars), c->stream), "gate")) {
+    dfree(c, nd);
+    return TG_ERR_CUDA;
+  }
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double total = 0.0;
+  for (int k = 0; k < reps + 1 && !s; ++k) {
+    cudaEventRecord(a, c->stream);
+    s = launch_seg_push(c, precision, c->d_z, c->d_q, nd, c->d_pcg);
+    cudaEventRecord(b, c->stream);
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    if (k > 0) total += t;  // the first launch also sets the shapes up
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  dfree(c, nd);
+  *ms = total / reps;
+  return s;
+}
+
+int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate) {
+  if (precision == TG_MIXED) return seg_push_t<float>(c, z, w, node_dot, gate);
+  return seg_push_t<double>(c, z, w, node_dot, gate);
 }
 
 int pcg_solve_cg(Context* c, int precision, const double4_32a* d_rhs, double rel_tol, int max_it, int precond,

@@ -200,21 +200,62 @@ __global__ void __launch_bounds__(256) seg_alpha_kernel(const int4* __restrict__
   }
 }
 
-template <typename T>
+// With the push storage (PUSH) the product's w holds the upper part of A z:
+// a node's w is completed from its push slots (rank planes of pstride, in
+// rank order, the prescribed dofs left out), and a 128-byte plane line whose
+// nodes all lie in this warp's pass and this chunk is dropped from L2 once
+// read (chunks start at any node, so lines at their edges are left as they
+// are: another CTA may still read them).
+template <typename T, bool PUSH>
 __global__ void __launch_bounds__(256) seg_update_kernel(
     const int4* __restrict__ chunks, const int* __restrict__ seg_chunk0, const T* __restrict__ minv,
     typename Vec4<T>::type* __restrict__ x, typename Vec4<T>::type* __restrict__ r,
     typename Vec4<T>::type* __restrict__ z, typename Vec4<T>::type* __restrict__ p,
     typename Vec4<T>::type* __restrict__ s, const typename Vec4<T>::type* __restrict__ w, double* part,
-    unsigned int* count, SegScalars* ssc, SegControl* ctl, PcgScalars* gate) {
+    unsigned int* count, SegScalars* ssc, SegControl* ctl, PcgScalars* gate,
+    const typename Vec4<T>::type* __restrict__ push, const int* __restrict__ lptr, const uint8_t* __restrict__ mask,
+    int pstride) {
   using V = typename Vec4<T>::type;
   const int4 ch = chunks[blockIdx.x];
   const int sg = ch.x;
   if (((volatile SegScalars*)ssc)[sg].done) return;
   const T alpha = T(ssc[sg].alpha), beta = T(ssc[sg].beta);
+  const int lane = threadIdx.x & 31;
   Acc<T> v[2];
-  for (int n = ch.y + threadIdx.x; n < ch.z; n += blockDim.x) {
-    const V zn = z[n], pn = p[n], sn = s[n], wn = w[n], xn = x[n], rn = r[n];
+  // warps iterate together (the push lines are dropped per warp)
+  for (int nb = ch.y + (int)(threadIdx.x & ~31u); nb < ch.z; nb += blockDim.x) {
+    const int n = nb + lane;
+    const bool live = n < ch.z;
+    V wn = mk<V, T>(T(0), T(0), T(0));
+    if (live) wn = w[n];
+    if (PUSH) {
+      const uint64_t keep = l2_policy_evict_last();
+      T s0 = T(0), s1 = T(0), s2 = T(0);
+      const int cnt = live ? lptr[n + 1] - lptr[n] : 0;
+#pragma unroll 4
+      for (int k = 0; k < cnt; ++k) {
+        const V pv = ld_hint(push + ((long long)k * pstride + n), keep);
+        s0 += pv.x;
+        s1 += pv.y;
+        s2 += pv.z;
+      }
+      if (live) {
+        const uint8_t m = mask[n];
+        wn = mk<V, T>(wn.x + ((m & 1) ? s0 : T(0)), wn.y + ((m & 2) ? s1 : T(0)), wn.z + ((m & 4) ? s2 : T(0)));
+      }
+      constexpr int kLine = 128 / (int)sizeof(V);  // slots per line
+      // the largest count over the kLine nodes from this lane on (the
+      // warp base need not be line aligned)
+      int lc = 0;
+#pragma unroll
+      for (int j = 0; j < kLine; ++j) lc = max(lc, __shfl_sync(0xffffffffu, cnt, (lane + j) & 31));
+      __syncwarp();
+      const int last = min(nb + 31, ch.z - 1);  // the warp pass's last node of this chunk
+      if ((n % kLine) == 0 && n >= ch.y && n + kLine - 1 <= last)
+        for (int k = 0; k < lc; ++k) l2_discard(push + ((long long)k * pstride + n));
+    }
+    if (!live) continue;
+    const V zn = z[n], pn = p[n], sn = s[n], xn = x[n], rn = r[n];
     T B[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) B[k] = minv[(long long)n * 9 + k];
@@ -322,20 +363,40 @@ template <typename T>
 int capture_seg_chunk(Context* c, const T* minv, int precision) {
   using V = typename Vec4<T>::type;
   SegSolve& S = c->seg;
+  const bool push = push_active(c);
   SpmvPlan plan;
-  int s = spmv_plan(c, precision, plan);
-  if (s) return s;
+  if (!push) {
+    const int s = spmv_plan(c, precision, plan);
+    if (s) return s;
+  }
+  const PushStore& ps = c->push;
+  const V* pushbuf = reinterpret_cast<const V*>(precision == TG_MIXED ? ps.d_push32 : ps.d_push64);
   cudaGraph_t graph;
   if (!ok(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return TG_ERR_CUDA;
   cudaError_t le = cudaSuccess;
-  for (int k = 0; k < kSegChunk && le == cudaSuccess; ++k) {
-    spmv_run(c, precision, plan, c->d_z, c->d_q, c->d_partials, S.d_gate, S.d_node_dot);
+  int ls = TG_OK;
+  for (int k = 0; k < kSegChunk && le == cudaSuccess && !ls; ++k) {
+    if (push)
+      ls = launch_seg_push(c, precision, c->d_z, c->d_q, S.d_node_dot, S.d_gate);
+    else
+      spmv_run(c, precision, plan, c->d_z, c->d_q, c->d_partials, S.d_gate, S.d_node_dot);
     seg_alpha_kernel<<<S.nchunks, 256, 0, c->stream>>>(S.d_chunk, S.d_seg_chunk0, S.d_node_dot, S.d_part, S.d_count,
                                                       S.d_sc, S.d_ctl, S.d_gate);
-    seg_update_kernel<T><<<S.nchunks, 256, 0, c->stream>>>(S.d_chunk, S.d_seg_chunk0, minv, (V*)c->d_x, (V*)c->d_r,
-                                                          (V*)c->d_z, (V*)c->d_p, (V*)S.d_s, (const V*)c->d_q,
-                                                          S.d_part, S.d_count, S.d_sc, S.d_ctl, S.d_gate);
+    if (push)
+      seg_update_kernel<T, true><<<S.nchunks, 256, 0, c->stream>>>(
+          S.d_chunk, S.d_seg_chunk0, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z, (V*)c->d_p, (V*)S.d_s,
+          (const V*)c->d_q, S.d_part, S.d_count, S.d_sc, S.d_ctl, S.d_gate, pushbuf, ps.d_lptr, c->d_mask,
+          ps.pstride);
+    else
+      seg_update_kernel<T, false><<<S.nchunks, 256, 0, c->stream>>>(
+          S.d_chunk, S.d_seg_chunk0, minv, (V*)c->d_x, (V*)c->d_r, (V*)c->d_z, (V*)c->d_p, (V*)S.d_s,
+          (const V*)c->d_q, S.d_part, S.d_count, S.d_sc, S.d_ctl, S.d_gate, nullptr, nullptr, nullptr, 0);
     le = cudaGetLastError();
+  }
+  if (ls) {
+    cudaGraph_t g2;
+    if (cudaStreamEndCapture(c->stream, &g2) == cudaSuccess) cudaGraphDestroy(g2);
+    return ls;
   }
   const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
   if (!ok(c, le, "capture launch") || !ok(c, ee, "end capture")) {
@@ -392,7 +453,13 @@ int solve_seg_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it
                                                 max_it);
   c->launches += 2;
   if (!ok(c, cudaGetLastError(), "seg init")) return TG_ERR_CUDA;
-  const int key = precision * 2 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0);
+  if (push_active(c)) {
+    // the push storage's values follow the last assembly (before the
+    // capture: the graph replays only the iteration)
+    s = push_prepare(c, precision);
+    if (s) return s;
+  }
+  const int key = precision * 4 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0) + (push_active(c) ? 2 : 0);
   if (!S.graph || S.graph_key != key || S.graph_x != c->d_x) {
     s = capture_seg_chunk<T>(c, minv, precision);
     if (s) return s;

@@ -222,9 +222,9 @@ struct Context {
   SymStore sym;
   PushStore push;
   // single-reduction PCG on the symmetric push storage: 1 (tg_pcg_form 3), 0
-  // (forms 1, 2), -1 automatic (the default: the push storage for meshes of
-  // at least kPushAutoBlocks block nonzeros, whose product amortises its
-  // build; the full storage below)
+  // (forms 1, 2), -1 automatic (the default: the push storage for segmented
+  // batches and for meshes of at least kPushAutoBlocks block nonzeros, whose
+  // product amortises its build; the full storage below)
   int cg_push = -1;
   long long tangent_serial = 0; // assemblies so far (values of derived storages follow it)
   int* d_contrib_ptr = nullptr; // nnzb+1
@@ -434,10 +434,17 @@ void cg_free(Context* c);  // the captured iterations
 // symmetric push storage: structure (once per mesh) and values of the last
 // assembly in the given precision (pushfmt.cu)
 int push_prepare(Context* c, int precision);
+// the product of a segmented batch's per-RVE solves on the push storage:
+// w's upper part, the pushes, each row's own z.w (pcg_cg.cu)
+int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate);
 constexpr long long kPushAutoBlocks = 1000000;
+// Segmented batches take the push storage at any size under the default, so
+// an RVE solved alone and the same RVE in a batch run the same kernels
+// (bitwise the same iterates).
 inline bool push_active(const Context* c) {
-  return c->cg_push > 0 || (c->cg_push < 0 && c->nnzb >= kPushAutoBlocks);
+  return c->cg_push > 0 || (c->cg_push < 0 && (c->nseg > 0 || c->nnzb >= kPushAutoBlocks));
 }
+int time_seg_push(Context* c, int reps, double* ms);  // standalone segmented push product (pcg_cg.cu)
 void push_free(Context* c);
 int time_cg_kernel(Context* c, int which, int reps, double* ms);  // 0 product, 1 vector kernel
 // PCG with every work vector, partial sum and scalar in caller scratch

@@ -175,13 +175,17 @@ class Context:
         self.sym_mode = 0
 
     def product_kernel(self):
-        """Name of the kernel the single-vector solve multiplies with."""
+        """Name of the kernel the single-vector solve multiplies with (a
+        segmented batch: the kernel of its per-RVE solves)."""
+        segmented = getattr(self, "nseg", 0) > 0
+        form = self.effective_form()
+        if segmented:
+            return "pcg_seg_push_kernel" if form == 3 else "pcg_spmv_kernel"
         if self.sym_mode and not getattr(self, "composed", False):
             return "pcg_spmv_sym_kernel"
-        form = self.effective_form()
-        if form == 3 and not getattr(self, "composed", False):
+        if form == 3:
             return "pcg_cg_push_kernel"
-        if form in (1, 2) and not getattr(self, "composed", False):
+        if form in (1, 2):
             return "pcg_cg_spmv_kernel"
         return "pcg_spmv_kernel"
 

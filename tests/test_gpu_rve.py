@@ -160,3 +160,24 @@ def test_macro_tangent_matches_oracle_finite_differences(batch):
         assert rel_err(C64[r], C64[r].T) < 1e-9, r
     Cm, _ = b.ctx.macro_tangent(b.vol0, precision=lib.MIXED, lin_rel_tol=1e-7)
     assert rel_err(Cm, C64) < 1e-5
+
+
+@pytest.mark.parametrize("prec", [lib.MIXED, lib.FP64])
+def test_push_and_full_storage_batches_agree(batch, prec):
+    """The batch's per-RVE solves on the symmetric push storage (the
+    default: upper blocks streamed, transposed products pushed to the lower
+    rows and added by the update kernel) and on the full storage (form 1)
+    reach the same states to the Newton tolerance, with the same RVE
+    statuses; the push product's kernel is the one timed for the batch."""
+    ns, Fs = batch
+    out = {}
+    for form in (-1, 1):
+        b = rve.RVEBatch(ns, Fs)
+        b.setup()
+        b.ctx.pcg_form(form)
+        rc, rep, rel, P = b.solve(precision=prec, rel_tol=1e-10, lin_rel_tol=1e-10 if prec == lib.FP64 else 1e-6)
+        assert rc == 0 and np.all(b.status == 0) and rel.max() < 1e-10
+        out[form] = (P, b.ctx.get_u(), b.ctx.product_kernel())
+    assert out[-1][2] == "pcg_seg_push_kernel" and out[1][2] == "pcg_spmv_kernel"
+    assert rel_err(out[-1][0], out[1][0]) < 1e-8
+    assert rel_err(out[-1][1], out[1][1]) < 1e-8
