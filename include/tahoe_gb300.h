@@ -309,9 +309,14 @@ int tg_segment_solver(tg_context* ctx, int per_rve);
  * K_ii du_i = -K_ib (dF X)_b is solved (PCG with params' precision,
  * preconditioner, lin_rel_tol, lin_max_it) and dP = (1/V0) sum_a (K du)_a (x)
  * X_a.  C is nseg*81 doubles, C[s*81 + (3j+J)*9 + (3k+L)] = dP_jJ/dF_kL;
- * vol0 as for tg_segment_average_stress.  No reference counterpart (FE^2 is
- * not in the reference; the definition is checked against finite
- * differences of the averaged stress). */
+ * vol0 as for tg_segment_average_stress.  The nine solves run as one
+ * multi-vector PCG over the whole batch: each right-hand side stops when its
+ * residual norm over the batch falls below lin_rel_tol times its initial
+ * norm over the batch (not per RVE), so an RVE's tangent in a batch agrees
+ * with the same RVE's tangent computed alone to about lin_rel_tol times the
+ * batch's spread of RVE sizes (1e-5 at lin_rel_tol 1e-7 in the tests).  No
+ * reference counterpart (FE^2 is not in the reference; the definition is
+ * checked against finite differences of the averaged stress). */
 int tg_segment_macro_tangent(tg_context* ctx, const tg_newton_params* params, const double* vol0, double* C,
                              int* pcg_iterations);
 
