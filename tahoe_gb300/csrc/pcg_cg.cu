@@ -188,14 +188,24 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
                                            typename Vec4<T>::type* __restrict__ q,
                                            typename Vec4<T>::type* __restrict__ push,
                                            typename Partial<T>::type* __restrict__ cta_part,
-                                           double* __restrict__ node_dot, PcgScalars* sc, int* status) {
+                                           double* __restrict__ node_dot, PcgScalars* sc, int* status,
+                                           const uint8_t* __restrict__ tile_act) {
   using P = typename Partial<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[NST];
   __shared__ int released[NST];  // warps done with the stage, over the whole launch
   __shared__ int nissued[NST];   // copies issued into the stage
   __shared__ int abort_flag;
+  __shared__ int last_k;         // position of the last tile issued
+  // SEG: the CTA's tiles that hold rows of an RVE still iterating (bit k:
+  // tile t0 + k G), from the batch's per-tile flags; the tiles of converged
+  // RVEs are neither copied nor multiplied
+  constexpr int kActWords = SEG ? 256 : 1;
+  __shared__ unsigned act_bits[kActWords];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int t0 = blockIdx.x, G = gridDim.x;
+  const int nk = t0 < ntiles ? (ntiles - t0 + G - 1) / G : 0;  // this CTA's tiles
+  const bool skip_tiles = SEG && tile_act && nk <= kActWords * 32;
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NST; ++k) {
@@ -205,9 +215,27 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
     }
     fence_mbar_init();
     abort_flag = 0;
+    last_k = -1;
+  }
+  if (SEG) {
+    for (int w = threadIdx.x; w < kActWords; w += blockDim.x) act_bits[w] = 0u;
+    __syncthreads();
+    if (skip_tiles)
+      for (int k = threadIdx.x; k < nk; k += blockDim.x)
+        if (tile_act[t0 + (long long)k * G]) atomicOr(&act_bits[k >> 5], 1u << (k & 31));
   }
   __syncthreads();
-  const int t0 = blockIdx.x, G = gridDim.x;
+  // the first active position >= k (nk if none); every position without
+  // the flags
+  auto next_k = [&](int k) {
+    if (!skip_tiles) return k;
+    while (k < nk) {
+      const unsigned w = act_bits[k >> 5] >> (k & 31);
+      if (w) return k + __ffs((int)w) - 1;
+      k = (k | 31) + 1;
+    }
+    return nk;
+  };
   // tile t into stage st (one thread)
   auto issue = [&](int t, int st) {
     nissued[st] += 1;
@@ -228,8 +256,14 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
       if (nissued[k] > 0) mbar_wait(&bars[k], (unsigned)((nissued[k] - 1) & 1), kWaitLimit);
   };
   // the first NST tiles (the matrix does not depend on the last vector kernel)
-  if (threadIdx.x == 0)
-    for (int k = 0; k < NST && t0 + k * G < ntiles; ++k) issue(t0 + k * G, k);
+  if (threadIdx.x == 0) {
+    int k = next_k(0);
+    for (int st = 0; st < NST && k < nk; ++st) {
+      issue(t0 + k * G, st);
+      last_k = k;
+      k = next_k(k + 1);
+    }
+  }
   griddep_wait();  // u and the scalars of the last vector kernel
   griddep_launch();
   if (skip_launch(sc, SEG ? 0 : 1)) {
@@ -244,7 +278,8 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
   // wait for the slowest one (the largest stall of the product).
   Acc<T> v;
   int it = 0;
-  for (int t = t0; t < ntiles; ++it, t += G) {
+  for (int k = next_k(0); k < nk; k = next_k(k + 1), ++it) {
+    const int t = t0 + k * G;
     const int s = it % NST;
     if (!mbar_wait(&bars[s], (unsigned)((it / NST) & 1), kWaitLimit)) atomicOr(&abort_flag, 1);
     __syncwarp();
@@ -260,10 +295,13 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
       const int done = atomicAdd(&released[s], 1);
       if (done == (it / NST + 1) * nwarps - 1) {  // the last warp of this use of the stage
         __threadfence_block();
-        const int tn = t + NST * G;
-        if (tn < ntiles) {
+        // stages are released in tile order, so the next tile to stage is
+        // the active one after the last issued
+        const int kn = next_k(last_k + 1);
+        if (kn < nk) {
+          last_k = kn;
           fence_async_smem();  // the stage was last read through generic loads
-          issue(tn, s);
+          issue(t0 + kn * G, s);
         }
       }
     }
@@ -293,8 +331,8 @@ __device__ __forceinline__ void cg_product(int ntiles, const long long* __restri
   int ntiles, const long long *__restrict__ blob_off, const unsigned char *__restrict__ blob, int cap, int keep, \
       const typename Vec4<T>::type *__restrict__ p, typename Vec4<T>::type *__restrict__ q,                  \
       typename Vec4<T>::type *__restrict__ push, typename Partial<T>::type *__restrict__ cta_part,            \
-      double *__restrict__ node_dot, PcgScalars *sc, int *status
-#define TG_CG_PRODUCT_ARGS ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, node_dot, sc, status
+      double *__restrict__ node_dot, PcgScalars *sc, int *status, const uint8_t *__restrict__ tile_act
+#define TG_CG_PRODUCT_ARGS ntiles, blob_off, blob, cap, keep, p, q, push, cta_part, node_dot, sc, status, tile_act
 
 template <typename T, int NST>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_cg_spmv_kernel(TG_CG_PRODUCT_PARAMS) {
@@ -666,7 +704,8 @@ struct CgArgs {
   const uint8_t* mask;
   int pstride;
   double* node_dot = nullptr;
-  void* pargs[12];
+  const uint8_t* tile_act = nullptr;
+  void* pargs[13];
   void* vargs[16];
   const void* vfn;
   CgArgs(Context* c, const CgStore<T>& st, const CgProduct& pr, const T* minv) {
@@ -696,7 +735,7 @@ struct CgArgs {
     lptr = st.lptr;
     mask = c->d_mask;
     pstride = st.pstride;
-    void* pa[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &pushw, &cta_part, &node_dot, &sc, &status};
+    void* pa[] = {&ntiles, &off, &blob, &cap, &keep, &pu, &qw, &pushw, &cta_part, &node_dot, &sc, &status, &tile_act};
     void* va[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc, &pushr, &lptr, &mask, &pstride};
     std::memcpy(pargs, pa, sizeof(pa));
     std::memcpy(vargs, va, sizeof(va));
@@ -907,7 +946,7 @@ void cg_free(Context* c) {
 
 namespace {
 template <typename T>
-int seg_push_t(Context* c, const void* z, void* w, double* node_dot, PcgScalars* gate) {
+int seg_push_t(Context* c, const void* z, void* w, double* node_dot, PcgScalars* gate, const uint8_t* tile_act) {
   using V = typename Vec4<T>::type;
   CgStore<T> st;
   int s = cg_store<T>(c, st);
@@ -927,7 +966,7 @@ int seg_push_t(Context* c, const void* z, void* w, double* node_dot, PcgScalars*
   V* push = st.pushbuf;
   typename Partial<T>::type* cta_part = nullptr;
   int* status = c->d_status;
-  void* args[] = {&ntiles, &off, &blob, &cap, &keep, &p, &q, &push, &cta_part, &node_dot, &gate, &status};
+  void* args[] = {&ntiles, &off, &blob, &cap, &keep, &p, &q, &push, &cta_part, &node_dot, &gate, &status, &tile_act};
   const cudaError_t e = cudaLaunchKernel(pr.fn, dim3(pr.grid), dim3(256), args, pr.smem, c->stream);
   c->launches++;
   return ok(c, e, "pcg_seg_push_kernel") ? TG_OK : TG_ERR_CUDA;
@@ -971,9 +1010,10 @@ int time_seg_push(Context* c, int reps, double* ms) {
   return s;
 }
 
-int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate) {
-  if (precision == TG_MIXED) return seg_push_t<float>(c, z, w, node_dot, gate);
-  return seg_push_t<double>(c, z, w, node_dot, gate);
+int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate,
+                    const uint8_t* tile_act) {
+  if (precision == TG_MIXED) return seg_push_t<float>(c, z, w, node_dot, gate, tile_act);
+  return seg_push_t<double>(c, z, w, node_dot, gate, tile_act);
 }
 
 int pcg_solve_cg(Context* c, int precision, const double4_32a* d_rhs, double rel_tol, int max_it, int precond,

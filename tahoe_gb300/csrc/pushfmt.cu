@@ -371,6 +371,7 @@ int push_build(Context* c) {
   if (tiles.back() != n) tiles.push_back(n);
   const int nt = (int)tiles.size() - 1;
   ps.ntiles = nt;
+  ps.h_tile_row = tiles;
   if (!dalloc(c, &ps.d_tile_row, (size_t)nt + 1) || !dalloc(c, &ps.d_off32, (size_t)nt + 1) ||
       !dalloc(c, &ps.d_off64, (size_t)nt + 1))
     return TG_ERR_OOM;

@@ -29,6 +29,7 @@
 // The reference has no FE^2 driver (each RVE would be its own element group
 // and solver, NLSolver.cpp:675-755 per RVE); this is that independence,
 // kept while the batch shares one matrix stream.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -303,6 +304,20 @@ __global__ void __launch_bounds__(256) seg_update_kernel(
   }
 }
 
+// A push tile takes part in the next product while one of its RVEs (its
+// rows' first to last) still iterates; the tiles of converged or failed RVEs
+// are skipped (RVEs share no blocks, so nothing an iterating RVE reads comes
+// from them).  Read by the product only: the flags hold for its whole launch.
+__global__ void seg_tile_active_kernel(int ntiles, const int2* __restrict__ tile_seg,
+                                       const SegScalars* __restrict__ ssc, uint8_t* __restrict__ act) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const int2 r = tile_seg[t];
+  uint8_t a = 0;
+  for (int sg = r.x; sg <= r.y && !a; ++sg) a = ssc[sg].done == 0 ? 1 : 0;
+  act[t] = a;
+}
+
 // the solution back to the unscaled right-hand side; an RVE that broke
 // down takes no update
 template <typename T>
@@ -359,11 +374,46 @@ int ensure_seg(Context* c) {
   return TG_OK;
 }
 
+// first and last RVE of every push tile's rows (per mesh and partition)
+int seg_tile_ranges(Context* c) {
+  SegSolve& S = c->seg;
+  const PushStore& ps = c->push;
+  if (S.d_tile_seg && S.tile_seg_n == ps.ntiles) return TG_OK;
+  if (S.d_tile_seg) dfree(c, S.d_tile_seg);
+  if (S.d_tile_act) dfree(c, S.d_tile_act);
+  S.d_tile_seg = nullptr;
+  S.d_tile_act = nullptr;
+  const std::vector<int>& tr = ps.h_tile_row;
+  const std::vector<int>& sn = c->h_seg_node;
+  if ((int)tr.size() != ps.ntiles + 1 || (int)sn.size() != c->nseg + 1) {
+    c->err = "segmented solve: push tiles or RVE partition missing";
+    return TG_ERR_ARG;
+  }
+  std::vector<int2> rng(ps.ntiles);
+  for (int t = 0; t < ps.ntiles; ++t) {
+    // RVE of a row: the last RVE whose first node is at most the row
+    auto seg_of = [&](int row) { return (int)(std::upper_bound(sn.begin(), sn.end(), row) - sn.begin()) - 1; };
+    rng[t] = make_int2(seg_of(tr[t]), seg_of(tr[t + 1] - 1));
+  }
+  if (!dalloc(c, &S.d_tile_seg, (size_t)ps.ntiles) || !dalloc(c, &S.d_tile_act, (size_t)ps.ntiles))
+    return TG_ERR_OOM;
+  if (!ok(c, cudaMemcpyAsync(S.d_tile_seg, rng.data(), sizeof(int2) * ps.ntiles, cudaMemcpyHostToDevice, c->stream),
+          "tile ranges") ||
+      !ok(c, cudaStreamSynchronize(c->stream), "sync"))
+    return TG_ERR_CUDA;
+  S.tile_seg_n = ps.ntiles;
+  return TG_OK;
+}
+
 template <typename T>
 int capture_seg_chunk(Context* c, const T* minv, int precision) {
   using V = typename Vec4<T>::type;
   SegSolve& S = c->seg;
   const bool push = push_active(c);
+  if (push) {
+    const int sr = seg_tile_ranges(c);
+    if (sr) return sr;
+  }
   SpmvPlan plan;
   if (!push) {
     const int s = spmv_plan(c, precision, plan);
@@ -376,9 +426,11 @@ int capture_seg_chunk(Context* c, const T* minv, int precision) {
   cudaError_t le = cudaSuccess;
   int ls = TG_OK;
   for (int k = 0; k < kSegChunk && le == cudaSuccess && !ls; ++k) {
-    if (push)
-      ls = launch_seg_push(c, precision, c->d_z, c->d_q, S.d_node_dot, S.d_gate);
-    else
+    if (push) {
+      seg_tile_active_kernel<<<(S.tile_seg_n + 255) / 256, 256, 0, c->stream>>>(S.tile_seg_n, S.d_tile_seg, S.d_sc,
+                                                                                S.d_tile_act);
+      ls = launch_seg_push(c, precision, c->d_z, c->d_q, S.d_node_dot, S.d_gate, S.d_tile_act);
+    } else
       spmv_run(c, precision, plan, c->d_z, c->d_q, c->d_partials, S.d_gate, S.d_node_dot);
     seg_alpha_kernel<<<S.nchunks, 256, 0, c->stream>>>(S.d_chunk, S.d_seg_chunk0, S.d_node_dot, S.d_part, S.d_count,
                                                       S.d_sc, S.d_ctl, S.d_gate);
@@ -472,7 +524,7 @@ int solve_seg_t(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it
   int last = 0;
   for (int k = 0; k < max_chunks && nact > 0; ++k) {
     if (!ok(c, cudaGraphLaunch(S.graph, st), "graph launch")) return TG_ERR_CUDA;
-    c->launches += 3 * kSegChunk;
+    c->launches += (push_active(c) ? 4 : 3) * kSegChunk;
     last = k & 1;
     if (!ok(c, cudaMemcpyAsync(&c->h_pcg[last], S.d_gate, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st), "copy") ||
         !ok(c, cudaEventRecord(c->ev_poll[last], st), "event"))
@@ -538,7 +590,8 @@ void seg_free(Context* c) {
   SegSolve& S = c->seg;
   if (S.graph) cudaGraphExecDestroy(S.graph);
   for (void* p : {(void*)S.d_chunk, (void*)S.d_seg_chunk0, (void*)S.d_sc, (void*)S.d_count, (void*)S.d_part,
-                  (void*)S.d_node_dot, S.d_s, (void*)S.d_active, (void*)S.d_ctl, (void*)S.d_gate})
+                  (void*)S.d_node_dot, S.d_s, (void*)S.d_active, (void*)S.d_ctl, (void*)S.d_gate,
+                  (void*)S.d_tile_seg, (void*)S.d_tile_act})
     if (p) dfree(c, p);
   S = SegSolve{};
   c->seg_active.clear();

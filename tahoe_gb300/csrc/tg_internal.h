@@ -112,6 +112,7 @@ struct PushStore {
   int pstride = 0;           // nnd rounded up to 8 (128-byte aligned planes)
   long long cap32 = 0, cap64 = 0;  // largest tile, bytes
   std::vector<long long> h_off32, h_off64;
+  std::vector<int> h_tile_row;  // ntiles+1 first row of each tile
   long long* d_off32 = nullptr;
   long long* d_off64 = nullptr;
   unsigned char* d_blob32 = nullptr;
@@ -143,6 +144,9 @@ struct SegSolve {
   uint8_t* d_active = nullptr;    // nseg: 1 = the solve iterates the RVE
   SegControl* d_ctl = nullptr;
   PcgScalars* d_gate = nullptr;   // done = 1 once no RVE iterates (the product returns at once)
+  int2* d_tile_seg = nullptr;     // per push tile: first and last RVE of its rows
+  uint8_t* d_tile_act = nullptr;  // per push tile: 1 while one of its RVEs iterates
+  int tile_seg_n = 0;             // push tiles the two arrays were built for
   cudaGraphExec_t graph = nullptr;
   int graph_key = -1;
   void* graph_x = nullptr;
@@ -436,7 +440,8 @@ void cg_free(Context* c);  // the captured iterations
 int push_prepare(Context* c, int precision);
 // the product of a segmented batch's per-RVE solves on the push storage:
 // w's upper part, the pushes, each row's own z.w (pcg_cg.cu)
-int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate);
+int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate,
+                    const uint8_t* tile_act = nullptr);
 constexpr long long kPushAutoBlocks = 1000000;
 // Segmented batches take the push storage at any size under the default, so
 // an RVE solved alone and the same RVE in a batch run the same kernels

