@@ -31,7 +31,8 @@ class GPUSolidElementT : public ElementT {
  public:
   /* formulation: TG_SMALL_STRAIN, TG_TOTAL_LAGRANGIAN or
    * TG_UPDATED_LAGRANGIAN, matching ElementT; precision: TG_MIXED (FP32
-   * tangent and PCG, FP64 residual) or TG_FP64 */
+   * tangent and PCG, double-float or FP64 residual, tg_form_residual_precision)
+   * or TG_FP64 */
   GPUSolidElementT(const ElementSupportT& support, int formulation, int precision = TG_MIXED)
       : ElementT(support), fForm(formulation), fPrecision(precision) {
     if (tg_create(&fCtx, 0) != TG_OK) ExceptionT::GeneralFail("GPUSolidElementT", "no CUDA device");
@@ -61,13 +62,15 @@ class GPUSolidElementT : public ElementT {
   }
 
   /* SolidElementT::RHSDriver: the whole group's internal forces on the
-   * device.  No external force is uploaded to the library, so its residual
-   * is -Fint; Tahoe's nodal and traction forces are assembled by their own
-   * managers as before. */
+   * device, in the arithmetic of the group's precision (TG_MIXED: the
+   * double-float element forces of a total-Lagrangian Simo group).  No
+   * external force is uploaded to the library, so its residual is -Fint;
+   * Tahoe's nodal and traction forces are assembled by their own managers as
+   * before. */
   virtual void RHSDriver(void) {
     Check(tg_set_iteration(fCtx, this->IterationNumber()));
     double norm = 0.0;
-    const int s = tg_form_residual(fCtx, fR.Pointer(), &norm);
+    const int s = tg_form_residual_precision(fCtx, fPrecision, fR.Pointer(), &norm);
     if (s == TG_ERR_BAD_JACOBIAN) ExceptionT::BadJacobianDet("GPUSolidElementT::RHSDriver");
     Check(s);
     this->ElementSupport().AssembleRHS(this->Group(), fR, fEqAll);
