@@ -13,7 +13,9 @@
 // only" assembly (MSRMatrixT::Assemble, MSRMatrixT.cpp:96-143).  The diagonal block's (block-)Jacobi inverse is
 // produced in the same pass (DiagonalMatrixT, DiagonalMatrixT.cpp:91,313):
 // minv[0 .. 9*nnd) holds the Jacobi inverse, minv[9*nnd .. 18*nnd) the 3x3
-// block-Jacobi inverse, so the solve can pick either.
+// block-Jacobi inverse, so the solve can pick either, and the Jacobi
+// inverse's diagonal follows as one padded 4-vector per node
+// (minv_diag_offset).
 #include <type_traits>
 
 #include "tg_internal.h"
@@ -120,6 +122,12 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
           minv[(long long)I * 9 + k] = Dg[k];
           minv[((long long)nnd + I) * 9 + k] = B[k];
         }
+        V4 dv;
+        dv.x = Dg[0];
+        dv.y = Dg[4];
+        dv.z = Dg[8];
+        dv.w = T(0);
+        reinterpret_cast<V4*>(minv + minv_diag_offset(nnd))[I] = dv;
       }
     }
   }

@@ -99,10 +99,10 @@ int form_tangent(Context* c, int precision) {
   const size_t keN = (size_t)c->nel * kKeStride;
   if (precision == TG_MIXED) {
     if (!c->d_Ke32 && !dalloc(c, &c->d_Ke32, keN)) return TG_ERR_OOM;
-    if (!c->d_minv32 && !dalloc(c, &c->d_minv32, (size_t)c->nnd * 18)) return TG_ERR_OOM;
+    if (!c->d_minv32 && !dalloc(c, &c->d_minv32, minv_values(c->nnd))) return TG_ERR_OOM;
   } else {
     if (!c->d_Ke64 && !dalloc(c, &c->d_Ke64, keN)) return TG_ERR_OOM;
-    if (!c->d_minv64 && !dalloc(c, &c->d_minv64, (size_t)c->nnd * 18)) return TG_ERR_OOM;
+    if (!c->d_minv64 && !dalloc(c, &c->d_minv64, minv_values(c->nnd))) return TG_ERR_OOM;
   }
   {
     const int sb = ensure_blob(c, precision);

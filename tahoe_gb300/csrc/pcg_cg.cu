@@ -352,6 +352,35 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) pcg_seg_push_kern
 #undef TG_CG_PRODUCT_PARAMS
 #undef TG_CG_PRODUCT_ARGS
 
+// The preconditioner block of one node: the 3x3 (block-)Jacobi inverse, or
+// with DIAG (Jacobi) its diagonal from the compact 4-vector per node.
+template <typename T, bool DIAG>
+struct PrecBlock {
+  T b[DIAG ? 3 : 9];
+  __device__ __forceinline__ void load(const T* __restrict__ minv, int n) {
+    if constexpr (DIAG) {
+      const typename Vec4<T>::type d = reinterpret_cast<const typename Vec4<T>::type*>(minv)[n];
+      b[0] = d.x;
+      b[1] = d.y;
+      b[2] = d.z;
+    } else {
+#pragma unroll
+      for (int m = 0; m < 9; ++m) b[m] = minv[(long long)n * 9 + m];
+    }
+  }
+  __device__ __forceinline__ void apply(T rx, T ry, T rz, T& zx, T& zy, T& zz) const {
+    if constexpr (DIAG) {
+      zx = b[0] * rx;
+      zy = b[1] * ry;
+      zz = b[2] * rz;
+    } else {
+      zx = b[0] * rx + b[1] * ry + b[2] * rz;
+      zy = b[3] * rx + b[4] * ry + b[5] * rz;
+      zz = b[6] * rx + b[7] * ry + b[8] * rz;
+    }
+  }
+};
+
 // One CTA per SM, one node per thread per pass: 1024 (FP32, 64 registers)
 // or 512 (FP64) nodes in flight per SM cover the L2 latency of the vector
 // pass (its vectors stay L2-resident), and one CTA per SM keeps the partials
@@ -366,7 +395,10 @@ struct CgShape {
 // part of A u only: a node's w is completed here from its push slots, added
 // in slot order, with the dofs of prescribed rows left out (the stored upper
 // blocks keep their prescribed columns, whose transposes would reach them).
-template <typename T, bool PUSH>
+//
+// DIAG: Jacobi, minv the compact diagonal (minv_diag_offset); otherwise the
+// node's 3x3 block.
+template <typename T, bool PUSH, bool DIAG>
 __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
     int nnd, const T* __restrict__ minv, typename Vec4<T>::type* __restrict__ x,
     typename Vec4<T>::type* __restrict__ r, typename Vec4<T>::type* __restrict__ u,
@@ -420,15 +452,14 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
   // released this kernel only after its own wait for it)
   const int n0 = blockIdx.x * blockDim.x + threadIdx.x;
   V u0, p0, s0, x0, r0;
-  T B0[9];
+  PrecBlock<T, DIAG> B0;
   if (n0 < nnd) {
     u0 = u[n0];
     p0 = p[n0];
     s0 = s[n0];
     x0 = x[n0];
     r0 = r[n0];
-#pragma unroll
-    for (int m = 0; m < 9; ++m) B0[m] = minv[(long long)n0 * 9 + m];
+    B0.load(minv, n0);
   }
   griddep_wait();  // w, the CTA partials and the scalars of the product
   griddep_launch();
@@ -525,7 +556,7 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
   const bool first = it == 0;
   Acc<T> acc[2];
   auto update = [&](int n, const V& un, const V& wn, const V& pn, const V& sn, const V& xn, const V& rn,
-                    const T (&B)[9]) {
+                    const PrecBlock<T, DIAG>& B) {
     V pv, sv;
     if (first) {  // p = u, s = w (p and s hold nothing yet)
       pv = un;
@@ -535,9 +566,8 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
       sv = mk<V, T>(wn.x + b_ * sn.x, wn.y + b_ * sn.y, wn.z + b_ * sn.z);
     }
     const T rx = rn.x - a_ * sv.x, ry = rn.y - a_ * sv.y, rz = rn.z - a_ * sv.z;
-    const T zx = B[0] * rx + B[1] * ry + B[2] * rz;
-    const T zy = B[3] * rx + B[4] * ry + B[5] * rz;
-    const T zz = B[6] * rx + B[7] * ry + B[8] * rz;
+    T zx, zy, zz;
+    B.apply(rx, ry, rz, zx, zy, zz);
     p[n] = pv;
     s[n] = sv;
     x[n] = mk<V, T>(xn.x + a_ * pv.x, xn.y + a_ * pv.y, xn.z + a_ * pv.z);
@@ -556,9 +586,8 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
     const V wn = w_of(n);
     if (n < nnd) {
       const V un = u[n], pn = p[n], sn = s[n], xn = x[n], rn = r[n];
-      T B[9];
-#pragma unroll
-      for (int m = 0; m < 9; ++m) B[m] = minv[(long long)n * 9 + m];
+      PrecBlock<T, DIAG> B;
+      B.load(minv, n);
       update(n, un, wn, pn, sn, xn, rn, B);
     }
   }
@@ -571,10 +600,10 @@ __global__ void __launch_bounds__(CgShape<T>::threads, 1) pcg_cg_vector_kernel(
 }
 
 // as many CTAs as are resident at once (grid-stride over the nodes)
-template <typename T, bool PUSH>
+template <typename T, bool PUSH, bool DIAG>
 int vec_grid(Context* c, int* grid) {
   int per_sm = 0;
-  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_cg_vector_kernel<T, PUSH>,
+  if (!ok(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_cg_vector_kernel<T, PUSH, DIAG>,
                                                            CgShape<T>::threads, 0),
           "occupancy"))
     return TG_ERR_CUDA;
@@ -708,7 +737,7 @@ struct CgArgs {
   void* pargs[13];
   void* vargs[16];
   const void* vfn;
-  CgArgs(Context* c, const CgStore<T>& st, const CgProduct& pr, const T* minv) {
+  CgArgs(Context* c, const CgStore<T>& st, const CgProduct& pr, const T* minv, bool diag) {
     ntiles = st.ntiles;
     cap = pr.cap;
     keep = pr.keep;
@@ -739,14 +768,17 @@ struct CgArgs {
     void* va[] = {&nnd, &mv, &x, &r, &u, &p, &sv, &w, &dpart, &ndp, &vpart, &sc, &pushr, &lptr, &mask, &pstride};
     std::memcpy(pargs, pa, sizeof(pa));
     std::memcpy(vargs, va, sizeof(va));
-    vfn = st.push ? reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, true>)
-                  : reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, false>);
+    vfn = st.push ? (diag ? reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, true, true>)
+                          : reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, true, false>))
+                  : (diag ? reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, false, true>)
+                          : reinterpret_cast<const void*>(pcg_cg_vector_kernel<T, false, false>));
   }
   CgArgs(const CgArgs&) = delete;
 };
 
+// minv: the vector kernel's preconditioner (the compact diagonal with diag)
 template <typename T>
-int capture(Context* c, int precision, const T* minv) {
+int capture(Context* c, int precision, const T* minv, bool diag) {
   CgStore<T> st;
   int s = cg_store<T>(c, st);
   if (s) return s;
@@ -754,9 +786,10 @@ int capture(Context* c, int precision, const T* minv) {
   s = product_shape<T>(c, st, pr);
   if (s) return s;
   int nv = 0;
-  s = st.push ? vec_grid<T, true>(c, &nv) : vec_grid<T, false>(c, &nv);
+  s = st.push ? (diag ? vec_grid<T, true, true>(c, &nv) : vec_grid<T, true, false>(c, &nv))
+              : (diag ? vec_grid<T, false, true>(c, &nv) : vec_grid<T, false, false>(c, &nv));
   if (s) return s;
-  CgArgs<T> A(c, st, pr, minv);
+  CgArgs<T> A(c, st, pr, minv, diag);
   // every launch after the first of the chunk depends programmatically on
   // the one before it
   cudaLaunchAttribute at[1];
@@ -831,7 +864,9 @@ int solve_cg_t(Context* c, int precision, const double4_32a* d_rhs, double rel_t
   }
   const int key = precision * 4 + (precond == TG_PRECOND_BLOCK_JACOBI ? 1 : 0) + (push_active(c) ? 2 : 0);
   if (!c->cg_graph || c->cg_graph_key != key) {
-    s = capture<T>(c, precision, minv);
+    // Jacobi: the vector kernel reads the compact diagonal
+    const bool diag = precond != TG_PRECOND_BLOCK_JACOBI;
+    s = capture<T>(c, precision, diag ? minv_base + minv_diag_offset(c->nnd) : minv, diag);
     if (s) return s;
     c->cg_graph_key = key;
   }
@@ -877,9 +912,13 @@ int time_cg_t(Context* c, int precision, int which, int reps, double* ms) {
     c->cg_s_precision = precision;
     cg_free(c);
   }
+  // Jacobi, as the solves the bench times (the vector kernel on the compact
+  // diagonal)
   const T* minv = std::is_same<T, float>::value ? (const T*)c->d_minv32 : (const T*)c->d_minv64;
   s = pcg_start(c, precision, c->d_R, minv, 1e-30, 1 << 30);
   if (s) return s;
+  const T* vminv = minv + minv_diag_offset(c->nnd);
+  const bool diag = true;
   PcgScalars h;
   if (!ok(c, cudaMemcpyAsync(&h, c->d_pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c->stream), "scalars") ||
       !ok(c, cudaStreamSynchronize(c->stream), "sync"))
@@ -893,9 +932,10 @@ int time_cg_t(Context* c, int precision, int which, int reps, double* ms) {
   s = product_shape<T>(c, st, pr);
   if (s) return s;
   int nv = 0;
-  s = st.push ? vec_grid<T, true>(c, &nv) : vec_grid<T, false>(c, &nv);
+  s = st.push ? (diag ? vec_grid<T, true, true>(c, &nv) : vec_grid<T, true, false>(c, &nv))
+              : (diag ? vec_grid<T, false, true>(c, &nv) : vec_grid<T, false, false>(c, &nv));
   if (s) return s;
-  CgArgs<T> A(c, st, pr, minv);
+  CgArgs<T> A(c, st, pr, vminv, diag);
   void** pargs = A.pargs;
   void** vargs = A.vargs;
   const void* vfn = A.vfn;

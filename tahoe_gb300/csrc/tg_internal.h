@@ -367,6 +367,13 @@ int ensure_blob(Context* c, int precision);
 
 // blob geometry shared by host and device code
 __host__ __device__ inline int ceil4(int n) { return (n + 3) & ~3; }
+// Preconditioner storage of one precision (values of T): the Jacobi inverse
+// as 3x3 blocks [0, 9 nnd), the block-Jacobi inverse [9 nnd, 18 nnd), then
+// from minv_diag_offset the Jacobi inverse's diagonal as one padded 4-vector
+// per node (what the single-vector PCG reads with Jacobi: 16 instead of 36
+// bytes per node in FP32)
+__host__ __device__ inline long long minv_diag_offset(int nnd) { return (18LL * nnd + 3) / 4 * 4; }
+inline size_t minv_values(int nnd) { return (size_t)minv_diag_offset(nnd) + 4 * (size_t)nnd; }
 __host__ __device__ inline long long blob_tile_bytes(int nrows, int nb, int elem) {
   const long long pstride = ((long long)nb * elem + 15) / 16 * 16 / elem;
   return 16 + 4LL * ceil4(nrows + 1) + 4LL * ceil4(nb) + 9LL * pstride * elem;
