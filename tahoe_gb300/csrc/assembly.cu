@@ -26,6 +26,94 @@ namespace {
 
 __device__ __forceinline__ int upper_slot(int a, int b) { return a * 8 - a * (a - 1) / 2 + (b - a); }
 
+// The value of global block j: its element contributions in the
+// destination-sorted order, rows of prescribed dofs zeroed (columns are kept,
+// so a product with a prescribed-increment vector gives the coupling
+// K_fp du_p; PCG vectors are zero at prescribed dofs, so the kept columns
+// never enter the solve).
+template <typename T>
+__device__ __forceinline__ void block_value(int j, uint8_t mI, const int* __restrict__ cptr,
+                                            const int* __restrict__ contrib, const T* __restrict__ Ke, T acc[9]) {
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double4_32a>::type;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) acc[k] = T(0);
+  const int c1 = cptr[j + 1];
+  for (int c = cptr[j]; c < c1; ++c) {
+    const int code = contrib[c];
+    const int e = code >> 6, a = (code >> 3) & 7, b = code & 7;
+    // the element block's three padded rows: one aligned vector load each
+    const V4* src = reinterpret_cast<const V4*>(
+        Ke + ((long long)e * kSlots + (a <= b ? upper_slot(a, b) : upper_slot(b, a))) * kKeBlock);
+    const V4 k0 = src[0], k1 = src[1], k2 = src[2];
+    const T m[9] = {k0.x, k0.y, k0.z, k1.x, k1.y, k1.z, k2.x, k2.y, k2.z};
+    if (a <= b) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] += m[k];
+    } else {
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) acc[p * 3 + q] += m[q * 3 + p];
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+    if (!((mI >> p) & 1))
+#pragma unroll
+      for (int q = 0; q < 3; ++q) acc[p * 3 + q] = T(0);
+}
+
+// (block-)Jacobi inverse of row I's diagonal block; inactive dofs get
+// identity in the inverse's input and zero in its output.
+template <typename T>
+__device__ __forceinline__ void write_inverses(int I, int nnd, uint8_t mI, const T acc[9], T* __restrict__ minv) {
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double4_32a>::type;
+  T A[9];
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      A[p * 3 + q] = (((mI >> p) & 1) && ((mI >> q) & 1)) ? acc[p * 3 + q] : (p == q ? T(1) : T(0));
+  // Jacobi: inverse diagonal; block-Jacobi: inverse of the 3x3 block
+  T B[9], Dg[9];
+  const T d = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+              A[2] * (A[3] * A[7] - A[4] * A[6]);
+  const T id = T(1) / d;
+  B[0] = (A[4] * A[8] - A[5] * A[7]) * id;
+  B[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  B[3] = (A[5] * A[6] - A[3] * A[8]) * id;
+  B[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  B[6] = (A[3] * A[7] - A[4] * A[6]) * id;
+  B[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Dg[k] = T(0);
+  Dg[0] = T(1) / A[0];
+  Dg[4] = T(1) / A[4];
+  Dg[8] = T(1) / A[8];
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      if (!((mI >> p) & 1) || !((mI >> q) & 1)) {
+        B[p * 3 + q] = T(0);
+        Dg[p * 3 + q] = T(0);
+      }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    minv[(long long)I * 9 + k] = Dg[k];
+    minv[((long long)nnd + I) * 9 + k] = B[k];
+  }
+  V4 dv;
+  dv.x = Dg[0];
+  dv.y = Dg[4];
+  dv.z = Dg[8];
+  dv.w = T(0);
+  reinterpret_cast<V4*>(minv + minv_diag_offset(nnd))[I] = dv;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __restrict__ rowptr,
                                                        const int* __restrict__ col,
@@ -34,7 +122,6 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
                                                        const uint8_t* __restrict__ mask, unsigned char* __restrict__ blob,
                                                        const long long* __restrict__ blob_off,
                                                        const int* __restrict__ row_tile, T* __restrict__ minv) {
-  using V4 = typename std::conditional<sizeof(T) == 4, float4, double4_32a>::type;
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nnd; I += warps) {
@@ -48,87 +135,40 @@ __global__ void __launch_bounds__(256) assemble_kernel(int nnd, const int* __res
     const int tb0 = rowptr[trow0];
     for (int j = r0 + lane; j < r1; j += 32) {
       T acc[9];
-#pragma unroll
-      for (int k = 0; k < 9; ++k) acc[k] = T(0);
-      const int c1 = cptr[j + 1];
-      for (int c = cptr[j]; c < c1; ++c) {
-        const int code = contrib[c];
-        const int e = code >> 6, a = (code >> 3) & 7, b = code & 7;
-        // the element block's three padded rows: one aligned vector load each
-        const V4* src = reinterpret_cast<const V4*>(
-            Ke + ((long long)e * kSlots + (a <= b ? upper_slot(a, b) : upper_slot(b, a))) * kKeBlock);
-        const V4 k0 = src[0], k1 = src[1], k2 = src[2];
-        const T m[9] = {k0.x, k0.y, k0.z, k1.x, k1.y, k1.z, k2.x, k2.y, k2.z};
-        if (a <= b) {
-#pragma unroll
-          for (int k = 0; k < 9; ++k) acc[k] += m[k];
-        } else {
-#pragma unroll
-          for (int p = 0; p < 3; ++p)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) acc[p * 3 + q] += m[q * 3 + p];
-        }
-      }
-      const int J = col[j];
-      // rows of prescribed dofs are zeroed; columns are kept so that a
-      // product with a prescribed-increment vector gives the coupling
-      // K_fp du_p (PCG vectors are zero at prescribed dofs, so the kept
-      // columns never enter the solve)
-#pragma unroll
-      for (int p = 0; p < 3; ++p)
-        if (!((mI >> p) & 1))
-#pragma unroll
-          for (int q = 0; q < 3; ++q) acc[p * 3 + q] = T(0);
+      block_value<T>(j, mI, cptr, contrib, Ke, acc);
 #pragma unroll
       for (int k = 0; k < 9; ++k) planes[(long long)k * ps + (j - tb0)] = acc[k];
-      if (J == I) {
-        // (block-)Jacobi inverse of the diagonal block; inactive dofs get
-        // identity in the inverse's input and zero in its output.
-        T A[9];
+      if (col[j] == I) write_inverses<T>(I, nnd, mI, acc, minv);
+    }
+  }
+}
+
+// The same for the upper blocks only, written straight into the symmetric
+// push storage's tiles (when the solve streams that storage, the full one
+// is assembled only on demand): 16 lanes per row (an upper row holds about
+// 14 blocks, the row's diagonal first), values bitwise those of the full
+// assembly.
+template <typename T>
+__global__ void __launch_bounds__(256) assemble_upper_kernel(
+    int nnd, const int* __restrict__ rowptr, const int* __restrict__ diag, const int* __restrict__ urow,
+    const int* __restrict__ tile_row, const int* __restrict__ row_tile, const long long* __restrict__ off,
+    unsigned char* __restrict__ pblob, const int* __restrict__ cptr, const int* __restrict__ contrib,
+    const T* __restrict__ Ke, const uint8_t* __restrict__ mask, T* __restrict__ minv) {
+  const int sub = threadIdx.x & 15;
+  const int groups = (gridDim.x * blockDim.x) >> 4;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 4; I < nnd; I += groups) {
+    const uint8_t mI = mask[I];
+    const int t = row_tile[I];
+    const int r0 = tile_row[t], nrows = tile_row[t + 1] - r0;
+    const int k0 = urow[r0], nb = urow[tile_row[t + 1]] - k0, ps = ceil4(nb);
+    T* planes = reinterpret_cast<T*>(pblob + off[t] + 16 + 4 * ceil4(nrows + 1) + 8 * ceil4(nb));
+    const int jd = diag[I], je = rowptr[I + 1], kr = urow[I] - k0;
+    for (int j = jd + sub; j < je; j += 16) {
+      T acc[9];
+      block_value<T>(j, mI, cptr, contrib, Ke, acc);
 #pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-          for (int q = 0; q < 3; ++q)
-            A[p * 3 + q] = (((mI >> p) & 1) && ((mI >> q) & 1)) ? acc[p * 3 + q] : (p == q ? T(1) : T(0));
-        // Jacobi: inverse diagonal; block-Jacobi: inverse of the 3x3 block
-        T B[9], Dg[9];
-        const T d = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
-                    A[2] * (A[3] * A[7] - A[4] * A[6]);
-        const T id = T(1) / d;
-        B[0] = (A[4] * A[8] - A[5] * A[7]) * id;
-        B[1] = (A[2] * A[7] - A[1] * A[8]) * id;
-        B[2] = (A[1] * A[5] - A[2] * A[4]) * id;
-        B[3] = (A[5] * A[6] - A[3] * A[8]) * id;
-        B[4] = (A[0] * A[8] - A[2] * A[6]) * id;
-        B[5] = (A[2] * A[3] - A[0] * A[5]) * id;
-        B[6] = (A[3] * A[7] - A[4] * A[6]) * id;
-        B[7] = (A[1] * A[6] - A[0] * A[7]) * id;
-        B[8] = (A[0] * A[4] - A[1] * A[3]) * id;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Dg[k] = T(0);
-        Dg[0] = T(1) / A[0];
-        Dg[4] = T(1) / A[4];
-        Dg[8] = T(1) / A[8];
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-          for (int q = 0; q < 3; ++q)
-            if (!((mI >> p) & 1) || !((mI >> q) & 1)) {
-              B[p * 3 + q] = T(0);
-              Dg[p * 3 + q] = T(0);
-            }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          minv[(long long)I * 9 + k] = Dg[k];
-          minv[((long long)nnd + I) * 9 + k] = B[k];
-        }
-        V4 dv;
-        dv.x = Dg[0];
-        dv.y = Dg[4];
-        dv.z = Dg[8];
-        dv.w = T(0);
-        reinterpret_cast<V4*>(minv + minv_diag_offset(nnd))[I] = dv;
-      }
+      for (int k = 0; k < 9; ++k) planes[(long long)k * ps + kr + (j - jd)] = acc[k];
+      if (j == jd) write_inverses<T>(I, nnd, mI, acc, minv);
     }
   }
 }
@@ -244,6 +284,49 @@ int launch_assemble(Context* c, int precision) {
                                                          c->d_blob_off64, c->d_row_tile, c->d_minv64);
   c->launches++;
   return ok(c, cudaGetLastError(), "assemble_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+// Upper blocks into the push storage (its structure built first); the
+// push storage's values are then those of the current tangent.
+int launch_assemble_upper(Context* c, int precision) {
+  int s = push_structure(c, precision);
+  if (s) return s;
+  PushStore& ps = c->push;
+  const bool f32 = precision == TG_MIXED;
+  int per_sm = 0;
+  if (!ok(c, f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, assemble_upper_kernel<float>, 256, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, assemble_upper_kernel<double>, 256, 0),
+          "occupancy"))
+    return TG_ERR_CUDA;
+  const int rows_per_block = 16;
+  int grid = (c->nnd + rows_per_block - 1) / rows_per_block;
+  grid = std::max(1, std::min(grid, c->num_sms * std::max(per_sm, 1)));
+  if (f32)
+    assemble_upper_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, ps.d_diag, ps.d_urow,
+                                                              ps.d_tile_row, ps.d_row_tile, ps.d_off32, ps.d_blob32,
+                                                              c->d_contrib_ptr, c->d_contrib, c->d_Ke32, c->d_mask,
+                                                              c->d_minv32);
+  else
+    assemble_upper_kernel<double><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, ps.d_diag, ps.d_urow,
+                                                               ps.d_tile_row, ps.d_row_tile, ps.d_off64, ps.d_blob64,
+                                                               c->d_contrib_ptr, c->d_contrib, c->d_Ke64, c->d_mask,
+                                                               c->d_minv64);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "assemble_upper_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+
+// The full storage of the current tangent, assembled from its element
+// blocks (still on the device) when the tangent went to the push storage
+// only.
+int ensure_full_assembly(Context* c) {
+  const int precision = c->tangent_precision;
+  if (precision != TG_MIXED && precision != TG_FP64) return TG_OK;
+  long long& serial = precision == TG_MIXED ? c->full_serial32 : c->full_serial64;
+  if (serial == c->tangent_serial) return TG_OK;
+  int s = ensure_blob(c, precision);
+  if (!s) s = launch_assemble(c, precision);
+  if (!s) serial = c->tangent_serial;
+  return s;
 }
 
 int launch_set_prescribed(Context* c, int n, const int* d_idx, const double* d_val) {

@@ -1182,7 +1182,11 @@ __global__ void expand_ke_kernel(int first, int count, const double* __restrict_
 }  // namespace
 
 int launch_element_dump(Context* c, int first, int count, double* dKe, double* dfint) {
-  int s = residual_impl(c, 0);
+  // the FP64 element blocks are re-formed here at the current state: a full
+  // storage the current FP64 tangent has not built yet is built first, from
+  // that tangent's blocks
+  int s = c->tangent_precision == TG_FP64 ? ensure_full_assembly(c) : TG_OK;
+  if (!s) s = residual_impl(c, 0);
   if (s) return s;
   s = launch_tangent(c, TG_FP64);
   if (s) return s;

@@ -768,6 +768,10 @@ __global__ void gather_solution_kernel(int neq, const int* __restrict__ slot, co
 }  // namespace
 
 int launch_lift_rhs(Context* c, const double4_32a* d_v, double4_32a* d_rhs, bool zero_base, int nvec) {
+  {
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
+  }
   const double4_32a* base = zero_base ? nullptr : c->d_R;
   Grids g = grids(c);
   const dim3 grid(std::min((c->nnd + 7) / 8, c->num_sms * 8), nvec);
@@ -804,6 +808,10 @@ int launch_gather_solution(Context* c, double* d_eq) {
 // (alpha = 0: x and r unchanged; the product is q = A p).
 template <typename T>
 int time_pcg_t(Context* c, int which, int reps, double* ms) {
+  {
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
+  }
   using V = typename Vec4<T>::type;
   const int precision = std::is_same<T, float>::value ? TG_MIXED : TG_FP64;
   int s = ensure_vectors<T>(c, precision);
@@ -869,6 +877,10 @@ template <typename T>
 int solve_scratch_t(Context* c, const double* d_rhs_eq, double* d_du_eq, unsigned char* scratch, double rel_tol,
                     int max_it, int precond, int* iters, double* rel_res) {
   using V = typename Vec4<T>::type;
+  {
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
+  }
   // scratch layout: scalars | partials | rhs (nodal FP64) | x r z p q
   unsigned char* cur = scratch;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(cur);
@@ -983,6 +995,11 @@ void spmv_run(Context* c, int precision, const SpmvPlan& P, const void* p, void*
 
 int pcg_solve(Context* c, const double4_32a* d_rhs, double rel_tol, int max_it, int precond, int* iters,
               double* rel_res) {
+  // a solve that streams the full storage: its values from the last tangent
+  if (!push_solve(c)) {
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
+  }
   // a batch of RVEs: one Krylov solve per RVE over the shared matrix stream
   if (c->nseg > 0 && c->seg_pcg_mode) return pcg_solve_segmented(c, d_rhs, rel_tol, max_it, precond, iters, rel_res);
   const int prec = c->tangent_precision;

@@ -621,6 +621,11 @@ int mrhs_solve_t(Context* c, const double4_32a* d_b, const double4_32a* d_v, dou
 // formed at the current state.
 int macro_tangent_mrhs(Context* c, int precision, int precond, double rel_tol, int max_it, const double* d_vol,
                        double* d_C, int* iters) {
+  {
+    // the multi-vector product streams the full storage
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
+  }
   const size_t nb = sizeof(double4_32a) * c->nnd * kNR;
   double4_32a *d_v = nullptr, *d_b = nullptr;
   if (!ok(c, cudaMallocAsync((void**)&d_v, nb, c->stream), "alloc") ||

@@ -104,15 +104,25 @@ int form_tangent(Context* c, int precision) {
     if (!c->d_Ke64 && !dalloc(c, &c->d_Ke64, keN)) return TG_ERR_OOM;
     if (!c->d_minv64 && !dalloc(c, &c->d_minv64, minv_values(c->nnd))) return TG_ERR_OOM;
   }
-  {
-    const int sb = ensure_blob(c, precision);
-    if (sb) return sb;
-  }
   int s = launch_tangent(c, precision);
-  if (!s) s = launch_assemble(c, precision);
-  if (!s) ++c->tangent_serial;
-  // the symmetric stream format of the single-vector product
-  if (!s && sym_active(c)) s = sym_convert(c, precision);
+  if (!s && push_solve(c)) {
+    // the solve streams the push storage: its upper blocks are assembled
+    // straight into it, the full storage only when something reads it
+    s = launch_assemble_upper(c, precision);
+    if (!s) {
+      ++c->tangent_serial;
+      (precision == TG_MIXED ? c->push.serial32 : c->push.serial64) = c->tangent_serial;
+    }
+  } else if (!s) {
+    s = ensure_blob(c, precision);
+    if (!s) s = launch_assemble(c, precision);
+    if (!s) {
+      ++c->tangent_serial;
+      (precision == TG_MIXED ? c->full_serial32 : c->full_serial64) = c->tangent_serial;
+    }
+    // the symmetric stream format of the single-vector product
+    if (!s && sym_active(c)) s = sym_convert(c, precision);
+  }
   if (!s) s = check_status(c);
   if (!s) c->tangent_precision = precision;
   return s;
@@ -127,6 +137,10 @@ extern "C" {
 int tg_get_tangent_csr(tg_context* c, int upper_only, double* vals) {
   if (!c || !vals || c->tangent_precision < 0) return TG_ERR_ARG;
   if (set_device(c) || ensure_host_mesh(c)) return TG_ERR_CUDA;
+  {
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
+  }
   // decode the tile-contiguous storage: tile t, local block jl, plane k
   const bool f32 = c->tangent_precision == TG_MIXED;
   const std::vector<long long>& off = f32 ? c->h_blob_off32 : c->h_blob_off64;
@@ -814,9 +828,16 @@ int tg_time_kernel(tg_context* c, int which, int reps, double* ms) {
     cudaEventRecord(a, c->stream);
     if (which == 2) s = launch_tangent(c, c->tangent_precision);
     else if (which == 3) {
-      s = launch_assemble(c, c->tangent_precision);
-      if (!s) ++c->tangent_serial;
-      if (!s && sym_active(c)) s = sym_convert(c, c->tangent_precision);
+      // the assembly the solve uses (the values do not change: the same
+      // element blocks, the same order)
+      if (push_solve(c)) {
+        s = launch_assemble_upper(c, c->tangent_precision);
+      } else {
+        s = ensure_blob(c, c->tangent_precision);
+        if (!s) s = launch_assemble(c, c->tangent_precision);
+        if (!s) (c->tangent_precision == TG_MIXED ? c->full_serial32 : c->full_serial64) = c->tangent_serial;
+        if (!s && sym_active(c)) s = sym_convert(c, c->tangent_precision);
+      }
     }
     else s = launch_residual(c, which == 5 ? kResidualDoubleFloat : kResidualFP64);
     cudaEventRecord(b, c->stream);

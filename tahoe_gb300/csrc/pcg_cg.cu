@@ -635,6 +635,8 @@ int cg_store(Context* c, CgStore<T>& st) {
   const bool f32 = std::is_same<T, float>::value;
   st.push = push_active(c);
   if (!st.push) {
+    const int sf = ensure_full_assembly(c);
+    if (sf) return sf;
     st.ntiles = c->ntiles;
     st.cap = f32 ? c->blob_cap32 : c->blob_cap64;
     st.h_off = f32 ? &c->h_blob_off32 : &c->h_blob_off64;

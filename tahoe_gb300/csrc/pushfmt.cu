@@ -442,17 +442,25 @@ int push_blob(Context* c, int precision) {
 
 }  // namespace
 
-int push_prepare(Context* c, int precision) {
+int push_structure(Context* c, int precision) {
   PushStore& ps = c->push;
   if (!ps.built) {
     const int s = push_build(c);
     if (s) return s;
   }
+  return push_blob(c, precision);
+}
+
+int push_prepare(Context* c, int precision) {
+  PushStore& ps = c->push;
   const bool f32 = precision == TG_MIXED;
-  int s = push_blob(c, precision);
+  int s = push_structure(c, precision);
   if (s) return s;
   long long& serial = f32 ? ps.serial32 : ps.serial64;
   if (serial == c->tangent_serial) return TG_OK;
+  // copied from the full storage (assembled there for another solve)
+  s = ensure_full_assembly(c);
+  if (s) return s;
   const int grid = std::max(1, std::min((c->nnd + 7) / 8, c->num_sms * 16));
   if (f32)
     push_convert_kernel<float><<<grid, 256, 0, c->stream>>>(c->nnd, c->d_rowptr, ps.d_diag, ps.d_urow, c->d_blob32,

@@ -231,6 +231,7 @@ struct Context {
   // product amortises its build; the full storage below)
   int cg_push = -1;
   long long tangent_serial = 0; // assemblies so far (values of derived storages follow it)
+  long long full_serial32 = -1, full_serial64 = -1;  // tangent serial of the full storage's values
   int* d_contrib_ptr = nullptr; // nnzb+1
   int* d_contrib = nullptr;     // nel*64: e*64 + a*8 + b
   std::vector<int> h_rowptr, h_col;
@@ -445,6 +446,10 @@ void cg_free(Context* c);  // the captured iterations
 // symmetric push storage: structure (once per mesh) and values of the last
 // assembly in the given precision (pushfmt.cu)
 int push_prepare(Context* c, int precision);
+int push_structure(Context* c, int precision);  // structure and tiles of one precision, no values
+// upper-only assembly into the push storage; the full storage on demand
+int launch_assemble_upper(Context* c, int precision);
+int ensure_full_assembly(Context* c);
 // the product of a segmented batch's per-RVE solves on the push storage:
 // w's upper part, the pushes, each row's own z.w (pcg_cg.cu)
 int launch_seg_push(Context* c, int precision, const void* z, void* w, double* node_dot, PcgScalars* gate,
@@ -457,6 +462,11 @@ inline bool push_active(const Context* c) {
   return c->cg_push > 0 || (c->cg_push < 0 && (c->nseg > 0 || c->nnzb >= kPushAutoBlocks));
 }
 int time_seg_push(Context* c, int reps, double* ms);  // standalone segmented push product (pcg_cg.cu)
+// the next single-vector (or segmented batch) solve streams the push storage
+inline bool push_solve(const Context* c) {
+  if (c->nseg > 0 && c->seg_pcg_mode) return push_active(c);
+  return c->pcg_form == 1 && !sym_active(c) && push_active(c);
+}
 void push_free(Context* c);
 int time_cg_kernel(Context* c, int which, int reps, double* ms);  // 0 product, 1 vector kernel
 // PCG with every work vector, partial sum and scalar in caller scratch

@@ -111,8 +111,21 @@ def assembly_bytes(nel, nnzb, nnd, s_val):
     """Algorithmic bytes of one assembly launch: element blocks (36 blocks of
     3 rows padded to 4 values per element) read once, the 64 contribution
     codes per element and their segment pointers, the column indices, the
-    block values written once, the preconditioner inverses written."""
-    return nel * 36 * 12 * s_val + nel * 64 * 4 + (nnzb + 1) * 4 + nnzb * 9 * s_val + nnzb * 4 + nnd * 18 * s_val
+    block values written once, the preconditioner inverses (two 3x3 blocks
+    and Jacobi's diagonal as a padded 4-vector per node) written."""
+    return (nel * 36 * 12 * s_val + nel * 64 * 4 + (nnzb + 1) * 4 + nnzb * 9 * s_val + nnzb * 4 +
+            nnd * 22 * s_val)
+
+
+def assembly_bytes_upper(nel, nnzb, nnd, s_val):
+    """Algorithmic bytes of one upper-only assembly into the push storage:
+    element blocks read once (every upper element block lands in one upper
+    global block), 36 contribution codes per element and the upper blocks'
+    segment pointers, per row its diagonal position and upper pointer, the
+    nu = (nnzb + nnd) / 2 upper block values written, the preconditioner
+    inverses written."""
+    nu = (nnzb + nnd) // 2
+    return nel * 36 * 12 * s_val + nel * 36 * 4 + (nu + nnd) * 4 + nu * 9 * s_val + nnd * 12 + nnd * 22 * s_val
 
 
 def cg_vector_bytes(nnd, s_val):
