@@ -443,7 +443,8 @@ int tg_tuning_get(const tg_context* ctx, int* tile_blocks, int* stages, int* tan
 int tg_timer_start(tg_context* ctx);
 int tg_timer_stop(tg_context* ctx, double* ms);
 /* average device time of `reps` standalone launches of one hot kernel on the
- * current state: 0 PCG product, 1 PCG vector kernel (the kernels of the form
+ * current state: 0 PCG product, 1 PCG vector kernel, each launch timed right
+ * after an untimed product launch as in the solve (the kernels of the form
  * the single-vector solve runs, tg_pcg_form), 2 element tangent, 3 assembly,
  * 4 element residual (+gather) in FP64, 5 the same in the mixed form's
  * arithmetic (tg_form_residual_precision) */

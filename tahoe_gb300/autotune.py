@@ -12,6 +12,12 @@ themselves (CUDA events, tg_time_kernel) on the current state:
   * the element tangent: elements per CTA (one thread per upper node-pair
     block of each element).
 
+When the solve streams the symmetric push storage (tg_pcg_form 3, the
+default on meshes of a million block nonzeros and more), the product has
+the one launch shape of that storage: the full-storage and symmetric-format
+sweeps are skipped (they would time the same product for every candidate)
+and only the tangent is tuned.
+
 Results are cached per (GPU, precision, formulation, mesh-size bucket) in a
 JSON table, so a serving process tunes once per kind of mesh.  Element
 matrices do not depend on the tangent shape (bitwise), and a different tile
@@ -37,9 +43,12 @@ _DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_buil
 
 def signature(ctx, precision, formulation, gpu="gpu0"):
     """Cache key: mesh sizes bucketed to powers of two (shapes are chosen for
-    the size class, not the exact mesh)."""
+    the size class, not the exact mesh), and whether the solve streams the
+    push storage."""
     b = lambda x: 1 << max(0, int(math.log2(max(1, x))))
-    return "%s|p%d|f%d|nnd%d|nel%d" % (gpu, precision, formulation, b(ctx.nnd), b(ctx.nel))
+    form = getattr(ctx, "effective_form", None)
+    push = "|push" if form is not None and form() == 3 else ""
+    return "%s|p%d|f%d|nnd%d|nel%d%s" % (gpu, precision, formulation, b(ctx.nnd), b(ctx.nel), push)
 
 
 def pick(timings):
@@ -77,6 +86,9 @@ class Tuner:
 
     @staticmethod
     def apply(ctx, cfg):
+        if cfg.get("push"):  # the push storage's product keeps its one shape
+            ctx.tangent_config(cfg["tangent_epb"])
+            return
         ctx.spmv_config(cfg["tile_blocks"], cfg["stages"])
         ctx.spmv_release(cfg.get("release", 0))
         ctx.spmv_symmetric(cfg.get("sym", 0), cfg.get("sym_tile", 0))
@@ -93,6 +105,9 @@ class Tuner:
             self.apply(ctx, cfg)
             return dict(cfg, cached=True)
         timer = timer or (lambda c, which, reps: c.time_kernel(which, reps))
+        form = getattr(ctx, "effective_form", None)
+        if form is not None and form() == 3:
+            return self._tune_tangent_only(ctx, precision, key, timer)
         spmv = {}
         for t in self.tiles:
             for s in self.stages:
@@ -145,5 +160,25 @@ class Tuner:
         out = dict(cfg, cached=False)
         out["spmv_sweep"] = {"%dx%dr%d" % k: v for k, v in spmv.items()}
         out["spmv_sweep"].update({"sym%dx%d" % k: v for k, v in sym.items()})
+        out["tangent_sweep"] = {str(k): v for k, v in tang.items()}
+        return out
+
+    def _tune_tangent_only(self, ctx, precision, key, timer):
+        """The push storage's solve: the product keeps its one shape (timed
+        for the record), the tangent's elements per CTA are tuned."""
+        cur = ctx.tuning()
+        ctx.tangent(precision)
+        spmv_ms = timer(ctx, KERNEL_SPMV, self.reps)
+        tang = {}
+        for e in self.epbs:
+            ctx.tangent_config(e)
+            tang[e] = timer(ctx, KERNEL_TANGENT, max(3, self.reps // 4))
+        epb, tang_ms = pick(tang)
+        cfg = {"tile_blocks": cur["tile_blocks"], "stages": cur["stages"], "release": 0, "sym": 0, "sym_tile": 0,
+               "tangent_epb": epb, "spmv_ms": spmv_ms, "tangent_ms": tang_ms, "push": True}
+        ctx.tangent_config(epb)
+        self.table[key] = cfg
+        self.save()
+        out = dict(cfg, cached=False)
         out["tangent_sweep"] = {str(k): v for k, v in tang.items()}
         return out

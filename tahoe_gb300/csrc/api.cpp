@@ -510,8 +510,13 @@ int tg_spmv_symmetric(tg_context* c, int on, int tile_blocks) {
   c->sym_mode = on;
   if (tile_blocks) c->sym_tile_blocks = tile_blocks;
   drop_graphs(c);  // the captured iterations bake in the product
-  // values of the current tangent in the (re-)built format
-  if (sym_active(c) && c->tangent_precision >= 0) return sym_convert(c, c->tangent_precision);
+  // values of the current tangent in the (re-)built format, converted from
+  // the full storage (assembled first when the tangent went to the push
+  // storage only)
+  if (sym_active(c) && c->tangent_precision >= 0) {
+    const int s = ensure_full_assembly(c);
+    return s ? s : sym_convert(c, c->tangent_precision);
+  }
   return TG_OK;
 }
 

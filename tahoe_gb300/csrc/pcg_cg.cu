@@ -950,9 +950,13 @@ int time_cg_t(Context* c, int precision, int which, int reps, double* ms) {
     // both scalar states at the first iteration (the product hands [1] to [0])
     cudaMemcpyAsync(c->d_pcg, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->d_pcg + 1, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream);
-    if (which == 1 && k == 0) {  // the product's partials for the vector launches
+    // each vector launch follows an untimed product launch, as in the solve:
+    // the product's partials, and on the push storage its pushed products,
+    // are then where the vector kernel finds them in the PCG (the L2)
+    if (which == 1) {
       e = cudaLaunchKernel(pr.fn, dim3(pr.grid), dim3(256), pargs, pr.smem, c->stream);
-      continue;
+      c->launches++;
+      if (k == 0 || e != cudaSuccess) continue;
     }
     cudaEventRecord(a, c->stream);
     e = which == 0 ? cudaLaunchKernel(pr.fn, dim3(pr.grid), dim3(256), pargs, pr.smem, c->stream)

@@ -90,3 +90,35 @@ def test_full_storage_kept_when_symmetric_is_slower(tmp_path):
     ctx = FakeCtx()
     out = t.tune(ctx, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=timer)
     assert out["sym"] == 0 and ctx.cfg["sym"] == 0
+
+
+class FakePushCtx(FakeCtx):
+    """A context whose solve streams the push storage (form 3)."""
+
+    def effective_form(self):
+        return 3
+
+    def tuning(self):
+        return {"tile_blocks": self.cfg["tile_blocks"], "stages": self.cfg["stages"],
+                "tangent_epb": self.cfg["tangent_epb"]}
+
+    def spmv_config(self, t, s):
+        raise AssertionError("the push storage's product has no full-storage shape to sweep")
+
+    def spmv_symmetric(self, on, tile_blocks=0):
+        raise AssertionError("the push storage's solve is not switched to the symmetric format")
+
+
+def test_push_storage_tunes_the_tangent_only(tmp_path):
+    t = autotune.Tuner(cache_path=str(tmp_path / "tuning.json"), reps=4)
+    ctx = FakePushCtx()
+    out = t.tune(ctx, lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=fake_timer)
+    assert out["push"] and not out["cached"]
+    assert (out["tangent_epb"], out["sym"], out["tile_blocks"], out["stages"]) == (4, 0, 640, 2)
+    assert ctx.cfg["tangent_epb"] == 4 and ctx.tangents >= 1
+    again = t.tune(FakePushCtx(), lib.MIXED, lib.TOTAL_LAGRANGIAN, timer=fake_timer)
+    assert again["cached"] and again["tangent_epb"] == 4
+    # the key tells the push storage's tuning from the full storage's
+    assert autotune.signature(ctx, lib.MIXED, lib.TOTAL_LAGRANGIAN) != \
+        autotune.signature(FakeCtx(), lib.MIXED, lib.TOTAL_LAGRANGIAN)
+

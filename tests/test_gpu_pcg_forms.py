@@ -125,6 +125,33 @@ def test_push_storage_follows_every_assembly(precision):
     c.pcg_form(1)
 
 
+@pytest.mark.parametrize("precision", [lib.MIXED, lib.FP64])
+def test_symmetric_format_after_a_push_only_tangent(precision):
+    """A tangent assembled for the push storage alone (upper blocks; the full
+    storage is assembled when something reads it), then the symmetric stream
+    format switched on: its values come from this tangent -- the full storage
+    still holds an older one -- so its solve equals form 1's."""
+    m = _model()
+    c, R = _system(m, precision, lib.PRECOND_JACOBI)  # full storage at the first state
+    c.set_u(c.get_u() * 1.5)
+    R2, _ = c.residual()
+    c.pcg_form(3)
+    c.tangent(precision)  # upper blocks into the push storage only
+    c.spmv_symmetric(1, 512)
+    assert c.product_kernel() == "pcg_spmv_sym_kernel"
+    tol = 1e-9
+    du_s, its_s, rr, rc = c.pcg(R2, rel_tol=tol, max_it=20000, precond=lib.PRECOND_JACOBI)
+    assert rc == 0
+    c.spmv_symmetric(0, 512)
+    c.pcg_form(1)
+    du_f, its_f, rr, rc = c.pcg(R2, rel_tol=tol, max_it=20000, precond=lib.PRECOND_JACOBI)
+    assert rc == 0
+    bound = 2e-4 if precision == lib.MIXED else 1e-6
+    assert np.abs(du_s - du_f).max() <= bound * np.abs(du_f).max()
+    assert abs(its_s - its_f) <= max(3, 0.05 * its_f)
+    c.pcg_form(-1)
+
+
 def test_l2_priorities_leave_the_iterates_bitwise_unchanged():
     m = _model(16)
     c, R = _system(m, lib.MIXED, lib.PRECOND_JACOBI)
