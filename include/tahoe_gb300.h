@@ -179,7 +179,11 @@ int tg_apply_update(tg_context* ctx);
  * cached per device for the life of the process and assumes the device's
  * primary context (do not call it after cudaDeviceReset or under another
  * driver context).  All calls on a device share the array: calls that overlap
- * on the GPU race. */
+ * on the GPU race.  The solve reads the full matrix storage: a tangent formed
+ * for the push storage alone (tg_pcg_form 3; the default picks it only on
+ * meshes of a million block nonzeros and more, above this call's limit) has
+ * its full storage assembled, and allocated if it never was, by the first
+ * call. */
 int tg_pcg_solve_noalloc(tg_context* ctx, const double* rhs_device, double* du_device, double rel_tol, int max_it,
                          int precond, int* iterations, double* rel_res);
 
