@@ -168,6 +168,7 @@ int alloc_mesh(Context* c, int nnd, int nel, int neq, long long nnzb) {
   c->d_Ke64 = nullptr;
   c->d_geo = nullptr;
   c->d_geo_ff = nullptr;
+  c->d_elem_src = nullptr;
   c->d_xyz = nullptr;
   c->d_blob32 = c->d_blob64 = nullptr;
   c->nseg = 0;

@@ -31,6 +31,7 @@ struct TplDev {
   const int* contrib;     // nel*64
   const int* row_tile;    // nnd
   int nnd, nel, neq, nnzb;
+  int geo_off;            // first element in the template geometry pool
 };
 
 struct MeshTemplate {
@@ -62,6 +63,7 @@ struct ComposeOut {
   int* row_tile;
   int* seg_node;
   int* seg_elem;
+  int* elem_src;  // each element's element in the template geometry pool
   int nnd, nel;
   int nnzb;
 };
@@ -141,7 +143,10 @@ __global__ void __launch_bounds__(256) compose_kernel(const TplDev* __restrict__
   copy_add(o.row_tile + I.node_off, T.row_tile, T.nnd, I.tile_off, start, stride);
   copy_add(o.nptr + I.node_off, T.nptr, T.nnd, I.elem_off * 8, start, stride);
   copy_add(o.rowptr + I.node_off, T.rowptr, T.nnd, I.nnzb_off, start, stride);
-  for (int k = start; k < T.nel; k += stride) o.block[I.elem_off + k] = T.block[k];
+  for (int k = start; k < T.nel; k += stride) {
+    o.block[I.elem_off + k] = T.block[k];
+    o.elem_src[I.elem_off + k] = T.geo_off + k;
+  }
   copy_add(o.conn + I.elem_off * 8, T.conn, T.nel * 8, I.node_off, start, stride);
   copy_add(o.nlist + I.elem_off * 8, T.nlist, T.nel * 8, I.elem_off * 8, start, stride);
   copy_add(o.eq_slot + I.eq_off, T.eq_slot, T.neq, I.node_off * 4, start, stride);
@@ -190,7 +195,44 @@ void free_templates(Context* c) {
     delete t;
   }
   c->templates.clear();
+  for (TplGeoPool* p : {&c->tpl_geo_ff, &c->tpl_geo64}) {
+    if (p->d) cudaFreeAsync(p->d, c->stream);
+    *p = TplGeoPool{};
+  }
+  c->tpl_elems = 0;
 }
+
+// The geometry planes of every resident template in one pool (25 planes of
+// 8 points per template element), rebuilt when templates were added since;
+// the templates' pool offsets never change.  Without room for it the pool
+// stays empty and batch meshes form their own planes.
+template <typename G>
+int template_geometry_pool(Context* c, TplGeoPool& pool) {
+  const int nt = (int)c->templates.size();
+  if (pool.d && pool.count == nt) return TG_OK;
+  if (pool.d) cudaFreeAsync(pool.d, c->stream);
+  pool = TplGeoPool{};
+  const long long elems = c->tpl_elems;
+  G* g = nullptr;
+  if (elems <= 0 || cudaMallocAsync((void**)&g, sizeof(G) * (size_t)elems * 8 * kGeoPlanes, c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return TG_OK;
+  }
+  for (const MeshTemplate* t : c->templates) {
+    const TplDev& d = t->dev;
+    const int s = launch_geometry<G>(c, d.X, d.nnd, d.conn, d.nel, g, elems * 8, (long long)d.geo_off * 8);
+    if (s) {
+      cudaFreeAsync(g, c->stream);
+      return s;
+    }
+  }
+  pool.d = g;
+  pool.elems = elems;
+  pool.count = nt;
+  return TG_OK;
+}
+template int template_geometry_pool<float2>(Context*, TplGeoPool&);
+template int template_geometry_pool<double>(Context*, TplGeoPool&);
 
 int launch_affine_prescribed(Context* c, const double* d_F) {
   affine_prescribed_kernel<<<(c->nnd + 255) / 256, 256, 0, c->stream>>>(c->nnd, c->nseg, c->d_seg_node, d_F, c->d_X,
@@ -269,6 +311,12 @@ int tg_template_add(tg_context* c, int nnd, const double* coords, int nel, const
   d.nel = nel;
   d.neq = neq;
   d.nnzb = t->rowptr[nnd];
+  if ((c->tpl_elems + nel) * 8 * kGeoPlanes >= (1LL << 31)) {
+    c->err = "too many template elements for the 32-bit geometry pool";
+    delete t;
+    return TG_ERR_CAPACITY;
+  }
+  d.geo_off = (int)c->tpl_elems;
   double* X;
   int *cn, *es, *np, *nl, *rp, *cl, *cp, *ct;
   int8_t* bk;
@@ -316,6 +364,7 @@ int tg_template_add(tg_context* c, int nnd, const double* coords, int nel, const
   }
   *template_id = (int)c->templates.size();
   c->templates.push_back(t);
+  c->tpl_elems += nel;
   return TG_OK;
 }
 
@@ -384,6 +433,7 @@ int tg_mesh_compose(tg_context* c, int count, const int* template_ids) {
               dalloc(c, &c->d_row_tile, (size_t)nnd) && dalloc(c, &c->d_blob_off32, (size_t)ntiles + 1) &&
               dalloc(c, &c->d_blob_off64, (size_t)ntiles + 1) && dalloc(c, &c->d_seg_node, (size_t)count + 1) &&
               dalloc(c, &c->d_seg_elem, (size_t)count + 1) && dalloc(c, &c->d_seg_out, (size_t)count * 9) &&
+              dalloc(c, &c->d_elem_src, (size_t)nel) &&
               dalloc(c, &d_tpl, (size_t)ntpl) && dalloc(c, &d_inst, (size_t)count);
   if (!good) return TG_ERR_OOM;
   cudaStream_t st = c->stream;
@@ -395,7 +445,7 @@ int tg_mesh_compose(tg_context* c, int count, const int* template_ids) {
   if (!good) return TG_ERR_CUDA;
   ComposeOut o{c->d_X, c->d_conn, c->d_block, c->d_mask, c->d_eq_slot, c->d_node_elem_ptr, c->d_node_elem,
                c->d_rowptr, c->d_col, c->d_contrib_ptr, c->d_contrib, c->d_row_tile, c->d_seg_node, c->d_seg_elem,
-               (int)nnd, (int)nel, (int)nnzb};
+               c->d_elem_src, (int)nnd, (int)nel, (int)nnzb};
   compose_kernel<<<dim3(8, count), 256, 0, st>>>(d_tpl, d_inst, count, o);
   c->launches++;
   if (!ok(c, cudaGetLastError(), "compose_kernel")) return TG_ERR_CUDA;

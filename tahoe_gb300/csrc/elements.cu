@@ -325,7 +325,8 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
                                                        J2View j2, int iteration, int commit_state,
                                                        double4_32a* __restrict__ fint, int* status,
                                                        double* __restrict__ ip_sig,
-                                                       const double* __restrict__ geo) {
+                                                       const double* __restrict__ geo,
+                                                       const int* __restrict__ geo_src, long long gstride) {
   __shared__ double sX[kResElems][8][3];
   __shared__ double sU[kResElems][8][3];
   const int tid = threadIdx.x;
@@ -361,12 +362,13 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
   if (valid) {
     if (geo) {
       // reference-configuration gradients and w det J, formed once per mesh
-      const long long nip = (long long)nel * 8, k = (long long)e * 8 + ip;
+      // (or per template of a composed mesh)
+      const long long k = (geo_src ? (long long)geo_src[e] : (long long)e) * 8 + ip;
 #pragma unroll
       for (int l = 0; l < 3; ++l)
 #pragma unroll
-        for (int a = 0; a < 8; ++a) g[l][a] = geo[(l * 8 + a) * nip + k];
-      wdet = geo[24 * nip + k];
+        for (int a = 0; a < 8; ++a) g[l][a] = geo[(l * 8 + a) * gstride + k];
+      wdet = geo[24 * gstride + k];
     } else {
       wdet = point_gradients<double>(sX[le], ip, g);  // weight 1 (HexahedronT.cpp:1545)
     }
@@ -978,9 +980,10 @@ J2View j2view(Context* c) {
 __device__ __forceinline__ void put_geo(double* p, double v) { *p = v; }
 __device__ __forceinline__ void put_geo(float2* p, double v) { *p = ff::to_float2(ff::from_double(v)); }
 
+// Planes of `stride` points, this mesh's points from `off` on.
 template <typename G>
 __global__ void geometry_kernel(const double* __restrict__ X, int nnd, const int* __restrict__ conn, int nel,
-                                G* __restrict__ geo) {
+                                G* __restrict__ geo, long long stride, long long off) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nip = (long long)nel * 8;
   if (k >= nip) return;
@@ -999,9 +1002,24 @@ __global__ void geometry_kernel(const double* __restrict__ X, int nnd, const int
 #pragma unroll
   for (int l = 0; l < 3; ++l)
 #pragma unroll
-    for (int a = 0; a < 8; ++a) put_geo(&geo[(l * 8 + a) * nip + k], g[l][a]);
-  put_geo(&geo[24 * nip + k], d);
+    for (int a = 0; a < 8; ++a) put_geo(&geo[(l * 8 + a) * stride + off + k], g[l][a]);
+  put_geo(&geo[24 * stride + off + k], d);
 }
+
+}  // namespace
+
+template <typename G>
+int launch_geometry(Context* c, const double* X, int nnd, const int* conn, int nel, G* geo, long long stride,
+                    long long off) {
+  const long long nip = (long long)nel * 8;
+  geometry_kernel<G><<<(unsigned)((nip + 255) / 256), 256, 0, c->stream>>>(X, nnd, conn, nel, geo, stride, off);
+  c->launches++;
+  return ok(c, cudaGetLastError(), "geometry_kernel") ? TG_OK : TG_ERR_CUDA;
+}
+template int launch_geometry<float2>(Context*, const double*, int, const int*, int, float2*, long long, long long);
+template int launch_geometry<double>(Context*, const double*, int, const int*, int, double*, long long, long long);
+
+namespace {
 
 // the geometry planes of the mesh, formed on first use after a mesh change;
 // without room for them the slot stays empty and the caller goes without
@@ -1013,10 +1031,8 @@ int geometry_planes(Context* c, G*& slot) {
   if (cudaMallocAsync((void**)&g, n * sizeof(G), c->stream) == cudaSuccess &&
       cudaStreamSynchronize(c->stream) == cudaSuccess) {
     c->allocations.push_back(g);
-    const long long nip = (long long)c->nel * 8;
-    geometry_kernel<G><<<(unsigned)((nip + 255) / 256), 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->nel, g);
-    c->launches++;
-    if (!ok(c, cudaGetLastError(), "geometry_kernel")) return TG_ERR_CUDA;
+    const int s = launch_geometry<G>(c, c->d_X, c->nnd, c->d_conn, c->nel, g, (long long)c->nel * 8, 0);
+    if (s) return s;
     slot = g;
   } else {
     cudaGetLastError();
@@ -1036,18 +1052,40 @@ bool ff_residual_applies(const Context* c) {
 
 int residual_impl(Context* c, int commit_state, double* d_ip_sig = nullptr, int arith = kResidualFP64) {
   if (arith == kResidualDoubleFloat && !d_ip_sig && ff_residual_applies(c)) {
+    if (c->composed && c->d_elem_src) {
+      // a batch mesh reads its templates' planes
+      const int s = template_geometry_pool<float2>(c, c->tpl_geo_ff);
+      if (s) return s;
+      if (c->tpl_geo_ff.d)
+        return launch_residual_ff(c, (const float2*)c->tpl_geo_ff.d, c->d_elem_src, c->tpl_geo_ff.elems * 8);
+    }
     const int s = geometry_planes(c, c->d_geo_ff);
     if (s) return s;
-    if (c->d_geo_ff) return launch_residual_ff(c, c->d_geo_ff);
+    if (c->d_geo_ff) return launch_residual_ff(c, c->d_geo_ff, nullptr, (long long)c->nel * 8);
   }
-  // without room for the planes the kernel forms the gradients itself
-  // (bitwise the same values)
-  const int s = geometry_planes(c, c->d_geo);
-  if (s) return s;
+  // a batch mesh reads its templates' planes; without room for the planes
+  // the kernel forms the gradients itself (bitwise the same values)
+  const double* geo = nullptr;
+  const int* geo_src = nullptr;
+  long long gstride = (long long)c->nel * 8;
+  if (c->composed && c->d_elem_src) {
+    const int s = template_geometry_pool<double>(c, c->tpl_geo64);
+    if (s) return s;
+    if (c->tpl_geo64.d) {
+      geo = (const double*)c->tpl_geo64.d;
+      geo_src = c->d_elem_src;
+      gstride = c->tpl_geo64.elems * 8;
+    }
+  }
+  if (!geo) {
+    const int s = geometry_planes(c, c->d_geo);
+    if (s) return s;
+    geo = c->d_geo;
+  }
   const int grid = (c->nel + kResElems - 1) / kResElems;
   residual_kernel<<<grid, 256, 0, c->stream>>>(c->d_X, c->nnd, c->d_conn, c->d_block, c->nel, c->d_u, c->mats,
                                                j2view(c), c->iteration, commit_state, c->d_fint, c->d_status,
-                                               d_ip_sig, c->d_geo);
+                                               d_ip_sig, geo, geo_src, gstride);
   c->launches++;
   return ok(c, cudaGetLastError(), "residual_kernel") ? TG_OK : TG_ERR_CUDA;
 }

@@ -20,7 +20,9 @@
 //   2. thread (e, a): f_a = sum_p Q_p dN_a/dX(p), the force on node a as a sum
 //      over the element's points (no shuffle reduction).
 // The reference-configuration gradients dN_a/dX and w det J come from the
-// per-mesh double-float geometry planes (25 planes of nel*8 float2).
+// per-mesh double-float geometry planes (25 planes of nel*8 float2), or for
+// a batch mesh composed from resident templates from the templates' planes
+// (one pool; each element indexes its template element's points).
 #include "ff.cuh"
 #include "tg_internal.h"
 
@@ -41,7 +43,8 @@ constexpr size_t kFFSmem = sizeof(float2) * (24 * kGRow + 9 * kFFThreads + kFFTh
 __global__ void __launch_bounds__(kFFThreads, 3)
     residual_tl_ff_kernel(const int* __restrict__ conn, const int8_t* __restrict__ blk, int nel,
                           const double4_32a* __restrict__ u, MatTable mt, const float2* __restrict__ geo,
-                          double4_32a* __restrict__ fint, int* status) {
+                          const int* __restrict__ src, long long gstride, double4_32a* __restrict__ fint,
+                          int* status) {
   extern __shared__ float2 ff_smem[];
   float2* sG = ff_smem;                    // [24][kGRow]: dN_a/dX_l of every point, row l*8+a
   float2* sQ = sG + 24 * kGRow;            // [9][kFFThreads]: Q of every point
@@ -50,15 +53,16 @@ __global__ void __launch_bounds__(kFFThreads, 3)
   const int le = tid >> 3, p = tid & 7;
   const int e = blockIdx.x * kFFElems + le;
   const bool valid = e < nel;
-  const long long nip = (long long)nel * 8;
-  const long long k = (long long)blockIdx.x * kFFThreads + tid;  // this thread's point
+  // this thread's point in the planes: its own, or its element's in the
+  // template pool
+  const long long k = valid ? (src ? (long long)src[e] * 8 + p : (long long)e * 8 + p) : 0;
 
   // stage the gradients (coalesced rows) and the element displacements
 #pragma unroll 8
-  for (int row = 0; row < 24; ++row) sG[row * kGRow + tid] = valid ? geo[row * nip + k] : make_float2(0.f, 0.f);
+  for (int row = 0; row < 24; ++row) sG[row * kGRow + tid] = valid ? geo[row * gstride + k] : make_float2(0.f, 0.f);
   dfloat wdet = ff::make(0.f, 0.f);
   if (valid) {
-    wdet = ff::from_float2(geo[24 * nip + k]);
+    wdet = ff::from_float2(geo[24 * gstride + k]);
     const double4_32a un = u[conn[(long long)e * 8 + p]];
     sU[tid * 3 + 0] = ff::to_float2(ff::from_double(un.x));
     sU[tid * 3 + 1] = ff::to_float2(ff::from_double(un.y));
@@ -188,14 +192,14 @@ __global__ void __launch_bounds__(kFFThreads, 3)
 
 }  // namespace
 
-int launch_residual_ff(Context* c, const float2* d_geo_ff) {
+int launch_residual_ff(Context* c, const float2* d_geo_ff, const int* src, long long gstride) {
   static_assert(kFFSmem <= 227 * 1024, "shared memory of the double-float residual");
   if (!ok(c, cudaFuncSetAttribute(residual_tl_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFFSmem),
           "residual_tl_ff_kernel smem"))
     return TG_ERR_CUDA;
   const int grid = (c->nel + kFFElems - 1) / kFFElems;
   residual_tl_ff_kernel<<<grid, kFFThreads, kFFSmem, c->stream>>>(c->d_conn, c->d_block, c->nel, c->d_u, c->mats,
-                                                                   d_geo_ff, c->d_fint, c->d_status);
+                                                                   d_geo_ff, src, gstride, c->d_fint, c->d_status);
   c->launches++;
   return ok(c, cudaGetLastError(), "residual_tl_ff_kernel") ? TG_OK : TG_ERR_CUDA;
 }

@@ -72,6 +72,13 @@ struct ResidScalars {
 };
 
 struct MeshTemplate;  // a resident template mesh (compose.cu)
+// geometry planes (25 planes of 8 points per element) of every resident
+// template: the element-major offsets are the templates' pool offsets
+struct TplGeoPool {
+  void* d = nullptr;
+  long long elems = 0;  // elements the pool holds
+  int count = 0;        // templates it covers
+};
 
 // Symmetric stream format of the single-vector PCG product (symspmv.cu):
 // upper node blocks only, lower blocks read as transposes of their upper
@@ -253,6 +260,7 @@ struct Context {
   double* d_minv64 = nullptr;
   double* d_geo = nullptr;      // 25 planes over nel*8 points: dN/dX (3x8), w det J (residual)
   float2* d_geo_ff = nullptr;   // the same planes as double-floats (hi, lo), for the double-float residual
+  int* d_elem_src = nullptr;    // composed mesh: every element's element in the template geometry pool
   double* d_xyz = nullptr;      // nnd*3: staging of caller (x, y, z) nodal arrays
   float* d_Ke32 = nullptr;      // nel*432: 36 upper node-pair blocks, rows padded to 4
   double* d_Ke64 = nullptr;
@@ -321,6 +329,11 @@ struct Context {
 
   // resident mesh templates (tg_template_add) and the composed mesh
   std::vector<MeshTemplate*> templates;
+  // geometry planes of every resident template, one pool per arithmetic
+  // (a composed mesh's elements share their template's planes: the batch
+  // mesh copies the template's coordinates and connectivity verbatim)
+  TplGeoPool tpl_geo_ff, tpl_geo64;
+  long long tpl_elems = 0;      // elements of every template added (pool offsets, append-only)
   bool composed = false;           // mesh built by tg_mesh_compose (host copies on demand)
   std::vector<int> h_inst_tpl;     // template of every instance of the composed mesh
 
@@ -412,7 +425,16 @@ enum : int { kResidualFP64 = 0, kResidualDoubleFloat = 1 };
 constexpr int kGeoPlanes = 25;  // per point: dN_a/dX_l (24), w det J
 int launch_residual(Context* c, int arith = kResidualFP64);  // fint per element + gather + norm
 // the total-Lagrangian Simo element forces in double-float (residual_ff.cu)
-int launch_residual_ff(Context* c, const float2* d_geo_ff);
+// src: each element's element in the planes (nullptr: the element itself);
+// gstride: points per plane
+int launch_residual_ff(Context* c, const float2* d_geo_ff, const int* src, long long gstride);
+// the template geometry pool of one arithmetic (G float2: double-float,
+// double: FP64), built for every resident template (compose.cu)
+template <typename G>
+int template_geometry_pool(Context* c, TplGeoPool& pool);
+template <typename G>
+int launch_geometry(Context* c, const double* X, int nnd, const int* conn, int nel, G* geo, long long stride,
+                    long long off);
 int launch_tangent(Context* c, int precision);   // Ke per element
 int launch_assemble(Context* c, int precision);
 int launch_blob_structure(Context* c, int precision);

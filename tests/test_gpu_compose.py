@@ -1,6 +1,7 @@
 """Batch meshes composed on the device from resident templates against the
-same batch uploaded as one concatenated mesh: equation pattern, residual and
-assembled tangent bit-exact, affine boundary values equal, and the solved
+same batch uploaded as one concatenated mesh: equation pattern, residual (FP64
+and the mixed form's double-float residual on the templates' pooled geometry
+planes) and assembled tangent bit-exact, affine boundary values equal, and the solved
 RVE stresses equal; a lane context reused across batches of different size
 gives what a fresh context gives."""
 import numpy as np
@@ -53,6 +54,11 @@ def test_affine_values_and_residual_tangent_bit_exact(pair):
         c.set_iteration(0)
     Ra = up.ctx.residual()
     Rb = res.ctx.residual()
+    assert np.array_equal(Ra[0], Rb[0]) and Ra[1] == Rb[1]
+    # the mixed form's double-float residual: the uploaded mesh forms its own
+    # geometry planes, the composed one reads its templates' pooled planes
+    Ra = up.ctx.residual(precision=lib.MIXED)
+    Rb = res.ctx.residual(precision=lib.MIXED)
     assert np.array_equal(Ra[0], Rb[0]) and Ra[1] == Rb[1]
     for prec in (lib.FP64, lib.MIXED):
         up.ctx.tangent(prec)
