@@ -34,7 +34,9 @@
 // search, exclusive scans for the upper and lower row pointers, k G tiles of
 // equal upper block count (G the product's resident CTAs), the tile byte
 // offsets on the host from the tiles' sizes, then the structure in one pass.
-// Values are copied from the full-storage tiles after every assembly.
+// Values are assembled straight into the tiles when the solve streams this
+// storage (assemble_upper_kernel), or converted from the full-storage tiles
+// when the tangent went to the full storage and a solve here needs it.
 #include <algorithm>
 #include <vector>
 

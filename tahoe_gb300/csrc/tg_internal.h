@@ -108,9 +108,10 @@ struct SymStore {
 // local row pointers, columns, push slots, nine value planes}.  The product
 // adds A_IJ u_J into row I and stores A_IJ^T u_I (J > I) at the block's push
 // slot, k pstride + J with k the rank of I among row J's lower columns; the
-// vector kernel adds row J's lptr[J+1] - lptr[J] slots in rank order.  Built on the device from the
-// node-block CSR (composed meshes included), values converted from the
-// full-storage tiles after every assembly.
+// vector kernel adds row J's lptr[J+1] - lptr[J] slots in rank order.  Built
+// on the device from the node-block CSR (composed meshes included); values
+// assembled straight into it when the solve streams it, else converted from
+// the full-storage tiles when a solve first needs them.
 struct PushStore {
   bool built = false;
   int ntiles = 0;
