@@ -728,6 +728,10 @@ __global__ void __launch_bounds__(256) lift_rhs_kernel(int nnd, const int* __res
     const int e1 = rp[I - r0 + 1];
     for (int j = rp[I - r0] + lane; j < e1; j += 32) {
       const double4_32a vj = v[cl[j]];
+      // v is a prescribed increment, zero away from the prescribed nodes: a
+      // zero column block adds a signed zero to a sum that is never -0, so
+      // skipping it (and its value reads) leaves the result bitwise the same
+      if (vj.x == 0.0 && vj.y == 0.0 && vj.z == 0.0) continue;
       const T* vv = pl + j;
       a0 += (double)vv[0 * ps] * vj.x + (double)vv[1 * ps] * vj.y + (double)vv[2 * ps] * vj.z;
       a1 += (double)vv[3 * ps] * vj.x + (double)vv[4 * ps] * vj.y + (double)vv[5 * ps] * vj.z;
