@@ -64,3 +64,26 @@ def test_tuned_shapes_applied_and_solution_unchanged(tmp_path):
     # cached: same shapes re-applied without timing
     out2 = autotune.Tuner(cache_path=str(tmp_path / "t.json")).tune(c, lib.MIXED, lib.TOTAL_LAGRANGIAN)
     assert out2["cached"] and out2["tile_blocks"] == out["tile_blocks"]
+
+
+def test_push_storage_tunes_the_tangent_only(tmp_path):
+    """With the solve on the symmetric push storage the tuner leaves the
+    product's storage and shapes alone (no full-storage or symmetric-format
+    sweep) and tunes the tangent: the solve after tuning is bitwise the one
+    before it."""
+    c = _ctx()
+    c.pcg_form(3)
+    c.tangent(lib.MIXED)
+    R, _ = c.residual()
+    du0, its0 = c.pcg(R, rel_tol=1e-7)[:2]
+    shapes = c.tuning()
+    out = autotune.Tuner(cache_path=str(tmp_path / "t.json"), reps=3).tune(c, lib.MIXED, lib.TOTAL_LAGRANGIAN)
+    assert out["push"] and out["sym"] == 0 and not out["cached"]
+    now = c.tuning()
+    assert (now["tile_blocks"], now["stages"]) == (shapes["tile_blocks"], shapes["stages"])
+    assert now["tangent_epb"] == out["tangent_epb"]
+    assert c.effective_form() == 3 and c.product_kernel() == "pcg_cg_push_kernel"
+    c.tangent(lib.MIXED)
+    du1, its1 = c.pcg(R, rel_tol=1e-7)[:2]
+    assert np.array_equal(du0, du1) and its0 == its1
+    c.pcg_form(-1)
